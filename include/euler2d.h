@@ -1,0 +1,233 @@
+/*
+ * euler2d.h - C ABI of the GB300 (sm_103a) 2D Euler MUSCL finite-volume solver.
+ *
+ * This is the drop-in boundary for pyHype's hot path: the per-block residual
+ * (FiniteVolumeMethod.dUdt), the explicit Runge-Kutta driver
+ * (ExplicitRungeKutta.integrate), the ghost/halo + boundary-condition fill
+ * (Blocks.apply_boundary_condition) and the CFL time step (Solver.get_dt).
+ * Everything is plain C: integers, doubles, pointers and sizes.  No torch or CUDA
+ * runtime types appear in the signatures (streams are passed as void*).
+ *
+ * Memory model.  e2d_create copies the block table and the geometry planes from
+ * host memory into device memory owned by the handle; all blocks of a problem live
+ * in one GPU's HBM.  States cross the boundary either as host buffers
+ * (e2d_set_state / e2d_get_state) or as device buffers owned by the caller
+ * (the *_device variants).  A state is structure-of-arrays: 4 planes (rho, rho*u,
+ * rho*v, E) of `ncells` doubles each, block b occupying
+ * [cell_offset[b], cell_offset[b] + nx*ny) of every plane in row-major (y, x) order.
+ *
+ * Threading.  One host thread drives one handle; calls on a handle are
+ * stream-ordered on the handle's stream.  Handles are independent.
+ *
+ * Errors.  Every call returns 0 on success or a negative E2D_ERR_* code;
+ * e2d_last_error() returns a thread-local message for the last failure.
+ */
+#ifndef EULER2D_H
+#define EULER2D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define E2D_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------------- */
+#define E2D_OK 0
+#define E2D_ERR_INVALID (-1)      /* bad argument / inconsistent block table      */
+#define E2D_ERR_CUDA (-2)         /* CUDA runtime error (message in last_error)   */
+#define E2D_ERR_UNREALIZABLE (-3) /* rho <= 0 or E <= 0 after a step              */
+#define E2D_ERR_TIMEOUT (-4)      /* a bounded device wait gave up                */
+#define E2D_ERR_UNSUPPORTED (-5)  /* option not built into this library           */
+#define E2D_ERR_NOMEM (-6)        /* device allocation failed                     */
+
+/* ---- scheme choices (string keys of pyhype/solver_config.py:64-92) ----------- */
+enum e2d_flux { E2D_FLUX_ROE = 0, E2D_FLUX_HLLL = 1, E2D_FLUX_HLLE = 2 };
+enum e2d_limiter {
+  E2D_LIM_VENKATAKRISHNAN = 0,
+  E2D_LIM_BARTH_JESPERSEN = 1,
+  E2D_LIM_VAN_ALBADA = 2,
+  E2D_LIM_VAN_LEER = 3
+};
+enum e2d_recon { E2D_RECON_CONSERVATIVE = 0, E2D_RECON_PRIMITIVE = 1 };
+enum e2d_precision { E2D_FP64 = 0, E2D_FP32 = 1 };
+
+/* ---- block sides: how the ghost cells and the outside flux state are formed --- */
+enum e2d_side_kind {
+  /* inter-block side (BC None + neighbour): ghost = the neighbour's adjacent cells;
+     the outside state of the boundary flux is that ghost cell average
+     (pyhype/blocks/ghost.py:187-216, pyhype/fvm/base.py:305-325)                  */
+  E2D_SIDE_NEIGHBOR = 0,
+  /* BC None and no neighbour: ghost = copy of the block's own boundary cells,
+     outside state = that copy (first order)                                        */
+  E2D_SIDE_COPY = 1,
+  /* "Reflection" / "Slipwall": normal velocity flipped in the wall frame, applied to
+     the ghost (conservative) and to the block's own limited boundary-face state
+     (pyhype/boundary_conditions/funcs.py:28-43)                                    */
+  E2D_SIDE_REFLECT = 2,
+  /* "OutletDirichlet": no-op BC; ghost = own boundary cells, outside state = own
+     limited boundary-face state (pyhype/blocks/ghost.py:250-254)                   */
+  E2D_SIDE_OUTLET = 3,
+  /* fixed state (PrimitiveDirichletBC with a uniform state): ghost and outside
+     state are constants given per side in E2DBlock.dirichlet_*                      */
+  E2D_SIDE_DIRICHLET = 4,
+  /* per-cell mix of REFLECT and DIRICHLET along one side, with an optional moving
+     switch point (double-Mach-reflection walls, inflow and the exact-shock top
+     boundary); parameters in E2DBlock.mixed                                         */
+  E2D_SIDE_MIXED = 5
+};
+enum e2d_side { E2D_E = 0, E2D_W = 1, E2D_N = 2, E2D_S = 3 };
+
+/* Per-cell switch along a MIXED side: cells whose centroid coordinate along the side
+   (x for N/S sides, y for E/W sides) is below  x0 + speed * t  use kind_below, the
+   others kind_above (each E2D_SIDE_REFLECT or E2D_SIDE_DIRICHLET).  t is the
+   solver time at the start of the step (the reference passes no stage time to its
+   boundary conditions).                                                            */
+typedef struct {
+  double x0;
+  double speed;
+  int32_t kind_below;
+  int32_t kind_above;
+  double ghost_below[4];   /* conservative ghost state for a DIRICHLET cell   */
+  double face_below[4];    /* reconstruction-variable outside state           */
+  double ghost_above[4];
+  double face_above[4];
+} E2DMixedSide;
+
+typedef struct {
+  int32_t nx, ny;
+  int32_t is_cartesian;      /* pyhype/blocks/quad_block.py:96-113               */
+  int32_t side_kind[4];      /* e2d_side_kind per E, W, N, S                     */
+  int32_t neighbor[4];       /* block index for E2D_SIDE_NEIGHBOR, else -1       */
+  int32_t instance;          /* independent-problem id (batched runs), else 0    */
+  int64_t cell_offset;       /* start of this block in every cell plane          */
+  int64_t vface_offset;      /* start in the vertical-face planes, ny*(nx+1)      */
+  int64_t hface_offset;      /* start in the horizontal-face planes, (ny+1)*nx    */
+  double dirichlet_ghost[4][4]; /* per side: conservative ghost state (DIRICHLET) */
+  double dirichlet_face[4][4];  /* per side: outside state in recon variables    */
+  E2DMixedSide mixed[4];
+  /* centroid coordinate along each side for MIXED sides, host pointer to
+     ny (E/W) or nx (N/S) doubles; ignored otherwise                              */
+  const double* side_coord[4];
+} E2DBlock;
+
+typedef struct {
+  int32_t nblocks;
+  int32_t flux;              /* e2d_flux     */
+  int32_t limiter;           /* e2d_limiter  */
+  int32_t recon;             /* e2d_recon    */
+  int32_t precision;         /* e2d_precision */
+  int32_t ninstances;        /* >= 1; per-instance dt when > 1 */
+  double gamma;              /* 1.4                                     */
+  double gm1;                /* gamma - 1 as formed by the host (1.4-1) */
+  double cfl;
+} E2DConfig;
+
+/* Geometry planes (host pointers), each the concatenation over blocks.
+   Cell planes hold sum(nx*ny) doubles, vertical-face planes sum(ny*(nx+1)),
+   horizontal-face planes sum((ny+1)*nx).                                          */
+enum e2d_cell_plane {
+  E2D_G_A = 0,      /* cell area                                               */
+  E2D_G_INV_A,      /* 1.0 / A                                                 */
+  E2D_G_HX_E,       /* quadrature point - centroid, x, east side               */
+  E2D_G_HX_W,
+  E2D_G_HX_N,
+  E2D_G_HX_S,
+  E2D_G_HY_E,       /* quadrature point - centroid, y                          */
+  E2D_G_HY_W,
+  E2D_G_HY_N,
+  E2D_G_HY_S,
+  E2D_G_CFL_DX,     /* east-west face-midpoint distance                        */
+  E2D_G_CFL_DY,     /* north-south face-midpoint distance                      */
+  E2D_G_NCELL
+};
+enum e2d_face_plane {
+  E2D_F_L = 0,      /* face length                                              */
+  E2D_F_LC,         /* L * cos(theta)                                          */
+  E2D_F_LS,         /* L * sin(theta)                                          */
+  E2D_F_COS,        /* cos(theta)                                              */
+  E2D_F_SIN,        /* sin(theta)                                              */
+  E2D_F_NFACE
+};
+typedef struct {
+  const double* cell[E2D_G_NCELL];
+  const double* vface[E2D_F_NFACE];
+  const double* hface[E2D_F_NFACE];
+} E2DGeometry;
+
+/* Result of the positivity check (pyhype/solvers/Euler2D.py:310-318). */
+typedef struct {
+  int32_t ok;           /* 1 if every cell has rho > 0 and E > 0              */
+  int32_t block;        /* first offending block, -1 if ok                    */
+  int64_t cell;         /* first offending cell index within that block       */
+  int64_t nbad;         /* number of offending cells                          */
+} E2DRealizability;
+
+/* Optional per-operator outputs of one residual evaluation (device pointers, NULL to
+   skip).  Cell quantities are 4 cell planes (reconstruction variables); face
+   quantities are 4 planes over all vertical (ny*(nx+1) per block) or horizontal
+   ((ny+1)*nx per block) faces.                                                     */
+typedef struct {
+  double* gx;           /* Green-Gauss gradient (greengauss.py:110-155)            */
+  double* gy;
+  double* phi;          /* limiter value (limiters/base.py:147-187)                */
+  double* vL;           /* left/right primitive states fed to the x-sweep flux,     */
+  double* vR;           /*   rotated into the face frame (fvm/base.py:327-390)      */
+  double* hL;           /* same for the y-sweep (fvm/base.py:392-486)               */
+  double* hR;
+  double* vflux_raw;    /* flux function output in the face frame                   */
+  double* hflux_raw;
+  double* vflux;        /* flux rotated back to the x/y frame                        */
+  double* hflux;
+} E2DDebug;
+
+typedef struct E2DSolver* E2DHandle;
+
+int e2d_abi_version(void);
+const char* e2d_last_error(void);
+
+/* ---- lifecycle ---------------------------------------------------------------- */
+/* Replaces Blocks.build + QuadBlock construction (pyhype/blocks/base.py:515-572). */
+int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* geo,
+               E2DHandle* out);
+int e2d_destroy(E2DHandle h);
+/* Use a caller stream (cudaStream_t as void*); NULL selects the handle's own. */
+int e2d_set_stream(E2DHandle h, void* stream);
+int64_t e2d_num_cells(E2DHandle h);
+
+/* ---- state transfer ------------------------------------------------------------- */
+int e2d_set_state(E2DHandle h, const double* host_soa);
+int e2d_get_state(E2DHandle h, double* host_soa);
+int e2d_set_state_device(E2DHandle h, const double* dev_soa);
+int e2d_get_state_device(E2DHandle h, double* dev_soa);
+
+/* ---- time integration ---------------------------------------------------------- */
+/* Butcher rows of ExplicitRungeKutta (pyhype/time_marching/explicit_runge_kutta.py:
+   91-274): nstages rows, row s holds a[s][0..s]; row-major nstages x nstages.     */
+int e2d_set_tableau(E2DHandle h, int32_t nstages, const double* a);
+/* Solver.get_dt without the t_final clamp: CFL * min over all cells of all blocks
+   (pyhype/solvers/base.py:114-136, pyhype/blocks/quad_block.py:423-436).
+   Batched problems write one value per instance.                                  */
+int e2d_compute_dt(E2DHandle h, double* dt_host);
+/* One ExplicitRungeKutta.integrate(dt) including the ghost/BC refresh after every
+   stage; t is the solver time at the start of the step (moving BCs).              */
+int e2d_step(E2DHandle h, double dt, double t);
+/* The Euler2D._solve loop (pyhype/solvers/Euler2D.py:361-376): dt -> clamp to
+   t_final - t -> step -> realizability, until t >= t_final or max_steps.  Time is
+   non-dimensional (t_final already multiplied by a_inf).  *t_inout is updated.
+   Returns E2D_ERR_UNREALIZABLE (with *real filled) if a step produced rho<=0 or
+   E<=0.                                                                            */
+int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps,
+            int32_t* steps_done, E2DRealizability* real);
+int e2d_check_realizable(E2DHandle h, E2DRealizability* out);
+
+/* ---- per-operator entry points (parity testing) ---------------------------------- */
+/* dUdt of the current state (FiniteVolumeMethod.dUdt, pyhype/fvm/base.py:108-139)
+   into a caller device buffer of 4 cell planes; optional intermediates in dbg.    */
+int e2d_residual(E2DHandle h, double* dudt_dev, const E2DDebug* dbg);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EULER2D_H */

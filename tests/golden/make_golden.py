@@ -1,0 +1,373 @@
+"""Generate the golden fixtures in this directory by running the pyHype reference itself.
+
+The reference (pure Python + numba + mpi4py + matplotlib) is imported unmodified from
+its source tree through the import shim in ``_refshim.py`` (identity ``njit``, a
+one-rank MPI world, stub plotting).  Each case builds an ``Euler2D`` solver with the
+reference's own ``SolverConfig``/mesh dictionaries/initial conditions, runs the
+reference's own step loop (``Solver.get_dt`` -> ``ExplicitRungeKutta.integrate`` ->
+``t += dt``; ``pyhype/solvers/Euler2D.py:361-376``) and records:
+
+* the initial conservative state of every block (after ``_pre_process_solve``),
+* the dt of every step and a fingerprint of the state after every step,
+* full states after selected steps,
+* for ``ops_*`` cases, the per-operator intermediates of one residual evaluation
+  (gradients, limiter, the primitive L/R face states fed to the flux, the fluxes and
+  dUdt) captured from the reference objects,
+* the reference's mesh geometry (to pin the host geometry builder bit for bit).
+
+Usage (in a container that holds the reference sources)::
+
+    python tests/golden/make_golden.py            # every case
+    python tests/golden/make_golden.py p100 m2x4_40
+
+The fixtures are committed; this script is the record of how they were made.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import _refshim  # noqa: E402
+
+_refshim.install()
+sys.path.insert(0, _refshim.REFERENCE_ROOT)
+
+from pyhype.solvers import Euler2D  # noqa: E402
+from pyhype.solver_config import SolverConfig  # noqa: E402
+from pyhype.fluids import Air  # noqa: E402
+from pyhype.states import ConservativeState, PrimitiveState  # noqa: E402
+from pyhype.mesh.rectangular import RectagularMeshGenerator  # noqa: E402
+from pyhype.initial_conditions.base import InitialCondition  # noqa: E402
+from pyhype.time_marching.explicit_runge_kutta import ExplicitRungeKutta  # noqa: E402
+from pyhype.utils.utils import Direction  # noqa: E402
+
+
+# --------------------------------------------------------------------------------------
+# fingerprints (shared with the tests: a canonical +0.0 is added so -0.0 == +0.0)
+# --------------------------------------------------------------------------------------
+def fingerprint(arrays) -> str:
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(np.asarray(a, dtype=np.float64) + 0.0).tobytes())
+    return h.hexdigest()[:32]
+
+
+# --------------------------------------------------------------------------------------
+# initial conditions (the explosion one is the reference example's, restated so the
+# generator does not depend on the examples package layout)
+# --------------------------------------------------------------------------------------
+class ExplosionIC(InitialCondition):
+    """examples/explosion/initial_condition.py:32-61 with an optional background flow."""
+
+    def __init__(self, u0=0.0, v0=0.0, lo=3.0, hi=7.0, ylo=None, yhi=None):
+        self.u0, self.v0, self.lo, self.hi = u0, v0, lo, hi
+        self.ylo = lo if ylo is None else ylo
+        self.yhi = hi if yhi is None else yhi
+
+    def apply_to_block(self, block):
+        left = PrimitiveState(
+            fluid=block.config.fluid,
+            array=np.array([4.6968, self.u0, self.v0, 404400.0]).reshape((1, 1, 4)),
+        ).to_type(ConservativeState)
+        right = PrimitiveState(
+            fluid=block.config.fluid,
+            array=np.array([1.1742, self.u0, self.v0, 101100.0]).reshape((1, 1, 4)),
+        ).to_type(ConservativeState)
+        xc = np.logical_and(block.mesh.x >= self.lo, block.mesh.x <= self.hi)
+        yc = np.logical_and(block.mesh.y >= self.ylo, block.mesh.y <= self.yhi)
+        block.state.data = np.where(np.logical_and(xc, yc), left.data, right.data)
+        block.state.make_non_dimensional()
+
+
+class DMRExampleIC(InitialCondition):
+    """examples/dmr/initial_condition.py:32-59."""
+
+    def apply_to_block(self, block):
+        left = PrimitiveState(
+            fluid=block.config.fluid,
+            array=np.array([8, 8.25, 0.0, 116.5]).reshape((1, 1, 4)),
+        ).to_type(ConservativeState)
+        right = PrimitiveState(
+            fluid=block.config.fluid,
+            array=np.array([1.4, 0.0, 0.0, 1.0]).reshape((1, 1, 4)),
+        ).to_type(ConservativeState)
+        block.state.data = np.where(block.mesh.x <= 0.95, left.data, right.data)
+        block.state.make_non_dimensional()
+
+
+def single_block(x0, x1, y0, y1, bce="Reflection", bcw="Reflection", bcn="Reflection", bcs="Reflection"):
+    return {
+        0: {
+            "nBLK": 0,
+            "NW": [x0, y1],
+            "NE": [x1, y1],
+            "SW": [x0, y0],
+            "SE": [x1, y0],
+            "NeighborE": None,
+            "NeighborW": None,
+            "NeighborN": None,
+            "NeighborS": None,
+            "NeighborNE": None,
+            "NeighborNW": None,
+            "NeighborSE": None,
+            "NeighborSW": None,
+            "BCTypeE": bce,
+            "BCTypeW": bcw,
+            "BCTypeN": bcn,
+            "BCTypeS": bcs,
+            "BCTypeNE": None,
+            "BCTypeNW": None,
+            "BCTypeSE": None,
+            "BCTypeSW": None,
+        }
+    }
+
+
+def dmr_example_mesh():
+    """examples/dmr/mesh.py:4-33 (skewed 4x1 block layout)."""
+    from pyhype.mesh.base import QuadMeshGenerator
+
+    k = 1
+    a = 2 / np.sqrt(3)
+    d = np.tan(30 * np.pi / 180)
+    return QuadMeshGenerator(
+        nx_blk=4,
+        ny_blk=1,
+        BCE=["OutletDirichlet"],
+        BCW=["OutletDirichlet"],
+        BCN=["OutletDirichlet"],
+        BCS=["OutletDirichlet", "Slipwall", "Slipwall", "Slipwall"],
+        top_x=[0, k, 2 * k, 3 * k, 4 * k],
+        bot_x=[0, k, 2 * k, 3 * k, 4 * k],
+        top_y=[a, a, a + d, a + 2 * d, a + 3 * d],
+        bot_y=[0, 0, d, 2 * d, 3 * d],
+        left_x=[0, 0],
+        left_y=[0, a],
+        right_x=[4 * k, 4 * k],
+        right_y=[3 * d, a + 3 * d],
+    )
+
+
+def rect_mesh(nbx, nby, east, north, bc="Reflection"):
+    return RectagularMeshGenerator.generate(
+        BCE=[bc], BCW=[bc], BCN=[bc], BCS=[bc],
+        east=east, west=0.0, north=north, south=0.0,
+        n_blocks_horizontal=nbx, n_blocks_vertical=nby,
+    )
+
+
+AIR = Air(a_inf=343.0, rho_inf=1.0)
+
+BASE = dict(
+    fvm_type="MUSCL",
+    fvm_spatial_order=2,
+    fvm_num_quadrature_points=1,
+    fvm_gradient_type="GreenGauss",
+    fvm_flux_function_type="Roe",
+    fvm_slope_limiter_type="Venkatakrishnan",
+    time_integrator="RK4",
+    interface_interpolation="arithmetic_average",
+    reconstruction_type=ConservativeState,
+    CFL=0.8,
+    t_final=1.0,
+    nghost=1,
+    use_JIT=True,
+)
+
+MOVING = dict(u0=120.0, v0=-80.0, lo=2.0, hi=5.0, ylo=3.0, yhi=6.5)
+
+# name -> (config overrides, mesh factory, ic factory, steps, snapshot steps, ops step, custom tableau)
+CASES = {
+    "ops_explosion_cons": (dict(nx=24, ny=20), lambda: single_block(0, 10, 0, 10), lambda: ExplosionIC(), 6, "all", 3, None),
+    "p100": (dict(nx=100, ny=100), lambda: single_block(0, 10, 0, 10), lambda: ExplosionIC(), 100, (1, 10, 100), None, None),
+    "m2x4_40": (dict(nx=40, ny=40), lambda: rect_mesh(2, 4, 10.0, 20.0), lambda: ExplosionIC(), 12, (1, 4, 12), 2, None),
+    "m2x4_150": (dict(nx=150, ny=150), lambda: rect_mesh(2, 4, 10.0, 20.0), lambda: ExplosionIC(), 2, (), None, None),
+    "lim_bj": (dict(nx=20, ny=16, fvm_slope_limiter_type="BarthJespersen"), lambda: single_block(0, 10, 0, 8), lambda: ExplosionIC(**MOVING), 5, "all", 2, None),
+    "lim_va": (dict(nx=20, ny=16, fvm_slope_limiter_type="VanAlbada"), lambda: single_block(0, 10, 0, 8), lambda: ExplosionIC(**MOVING), 5, "all", 2, None),
+    "lim_vl": (dict(nx=20, ny=16, fvm_slope_limiter_type="VanLeer"), lambda: single_block(0, 10, 0, 8), lambda: ExplosionIC(**MOVING), 5, "all", 2, None),
+    "hlll_cons": (dict(nx=20, ny=16, fvm_flux_function_type="HLLL"), lambda: single_block(0, 10, 0, 8), lambda: ExplosionIC(**MOVING), 5, "all", 2, None),
+    "hlll_prim": (dict(nx=20, ny=16, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState), lambda: single_block(0, 10, 0, 8), lambda: ExplosionIC(**MOVING), 5, "all", 2, None),
+    "roe_prim": (dict(nx=20, ny=16, reconstruction_type=PrimitiveState), lambda: single_block(0, 10, 0, 8), lambda: ExplosionIC(**MOVING), 5, "all", 2, None),
+    "bc_mixed": (dict(nx=20, ny=16), lambda: single_block(0, 10, 0, 8, bce="Slipwall", bcw="OutletDirichlet", bcn="Reflection", bcs=None), lambda: ExplosionIC(**MOVING), 6, "all", 2, None),
+    "m2x2_prim_hlll": (dict(nx=16, ny=12, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState, fvm_slope_limiter_type="VanAlbada"), lambda: rect_mesh(2, 2, 10.0, 8.0, bc="OutletDirichlet"), lambda: ExplosionIC(**MOVING), 5, "all", 2, None),
+    "dmr_example": (dict(nx=12, ny=12, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState, time_integrator="RK2", CFL=0.4), dmr_example_mesh, lambda: DMRExampleIC(), 5, "all", 2, None),
+    "ssprk2_hlll": (dict(nx=20, ny=16, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState, CFL=0.4), lambda: single_block(0, 10, 0, 8), lambda: ExplosionIC(**MOVING), 4, "all", None, [[1], [0.5, 0.5]]),
+}
+for _ti in ("ExplicitEuler1", "RK2", "Ralston2", "RK3", "RK3SSP", "Ralston3", "Ralston4", "DormandPrince5"):
+    CASES["ti_" + _ti] = (dict(nx=16, ny=16, time_integrator=_ti, CFL=0.4), lambda: single_block(0, 10, 0, 10), lambda: ExplosionIC(**MOVING), 3, "all", None, None)
+
+
+def mesh_dict_of(mesh):
+    return mesh.dict if hasattr(mesh, "dict") else mesh
+
+
+def encode_mesh(mesh_cfg, out):
+    """Store the mesh dictionary (corners, neighbours, string BC kinds) in arrays."""
+    names = sorted(mesh_cfg.keys())
+    out["blk_ids"] = np.array(names, dtype=np.int64)
+    corners = np.zeros((len(names), 4, 2))
+    nbr = np.full((len(names), 4), -1, dtype=np.int64)
+    bc = np.empty((len(names), 4), dtype="U16")
+    for k, n in enumerate(names):
+        d = mesh_cfg[n]
+        for c, key in enumerate(("SW", "SE", "NW", "NE")):
+            corners[k, c] = d[key]
+        for s, side in enumerate("EWNS"):
+            v = d["Neighbor" + side]
+            nbr[k, s] = -1 if v is None else v
+            b = d["BCType" + side]
+            bc[k, s] = "None" if b is None else str(b)
+    out["corners"] = corners
+    out["neighbors"] = nbr
+    out["bc"] = bc
+
+
+def record_geometry(solver, out):
+    for bnum, blk in solver._blocks.blocks.items():
+        m = blk.mesh
+        p = f"geo{bnum}_"
+        out[p + "nodes_x"] = m.nodes.x[:, :, 0]
+        out[p + "nodes_y"] = m.nodes.y[:, :, 0]
+        out[p + "xc"] = m.x[:, :, 0]
+        out[p + "yc"] = m.y[:, :, 0]
+        out[p + "A"] = m.A[:, :, 0]
+        out[p + "dx"] = m.dx[:, :, 0]
+        out[p + "dy"] = m.dy[:, :, 0]
+        for side in "EWNS":
+            f = m.face[getattr(Direction, {"E": "east", "W": "west", "N": "north", "S": "south"}[side])]
+            out[p + f"L{side}"] = f.L[:, :, 0]
+            out[p + f"th{side}"] = f.theta[:, :, 0]
+            out[p + f"nx{side}"] = f.norm.x[:, :, 0]
+            out[p + f"ny{side}"] = f.norm.y[:, :, 0]
+            q = blk.qp[getattr(Direction, {"E": "east", "W": "west", "N": "north", "S": "south"}[side])][0]
+            out[p + f"qx{side}"] = q.x[:, :, 0]
+            out[p + f"qy{side}"] = q.y[:, :, 0]
+            # the run-time rotation evaluates np.sin/np.cos on numpy float64 scalars
+            # (pyhype/utils/utils.py:75-85); record that scalar path for the theta arrays
+            th = f.theta[:, :, 0]
+            out[p + f"cos_scalar{side}"] = np.array([np.cos(v) for v in th.ravel()]).reshape(th.shape)
+            out[p + f"sin_scalar{side}"] = np.array([np.sin(v) for v in th.ravel()]).reshape(th.shape)
+        out[p + "is_cartesian"] = np.array(bool(blk.is_cartesian))
+
+
+def capture_ops(solver, out, tag):
+    """One residual evaluation per block, with every intermediate recorded."""
+    for bnum, blk in solver._blocks.blocks.items():
+        p = f"{tag}{bnum}_"
+        recon = blk.recon_block
+        fvm = recon.fvm
+        recon.from_block(blk)
+        out[p + "recon"] = recon.state.data.copy()
+        for side in "EWNS":
+            g = recon.ghost[getattr(Direction, {"E": "east", "W": "west", "N": "north", "S": "south"}[side])]
+            out[p + f"ghost{side}"] = g.state.data.copy()
+        fvm.gradient.compute(recon)
+        out[p + "gx"] = recon.grad.x.copy()
+        out[p + "gy"] = recon.grad.y.copy()
+        fvm.compute_limiter()
+        out[p + "phi"] = fvm.limiter.phi.copy()
+
+        captured = {}
+
+        def wrap(fn, key):
+            def inner(WL, WR):
+                captured[key + "L"] = WL.data.copy()
+                captured[key + "R"] = WR.data.copy()
+                res = fn(WL=WL, WR=WR)
+                captured[key + "F"] = np.array(res, copy=True)
+                return res
+
+            return inner
+
+        fx, fy = fvm.flux_function_x, fvm.flux_function_y
+        fvm.flux_function_x = wrap(fx, "x")
+        fvm.flux_function_y = wrap(fy, "y")
+        try:
+            fvm._evaluate_east_west_flux()
+            fvm._evaluate_north_south_flux()
+        finally:
+            fvm.flux_function_x, fvm.flux_function_y = fx, fy
+        ny, nx = blk.state.data.shape[:2]
+        out[p + "xL"] = captured["xL"].reshape(ny, nx + 1, 4)
+        out[p + "xR"] = captured["xR"].reshape(ny, nx + 1, 4)
+        out[p + "xF"] = captured["xF"].reshape(ny, nx + 1, 4)
+        out[p + "yL"] = captured["yL"].reshape(nx, ny + 1, 4)
+        out[p + "yR"] = captured["yR"].reshape(nx, ny + 1, 4)
+        out[p + "yF"] = captured["yF"].reshape(nx, ny + 1, 4)
+        for side, key in (("E", Direction.east), ("W", Direction.west), ("N", Direction.north), ("S", Direction.south)):
+            out[p + f"flux{side}"] = fvm.Flux[key][0].copy()
+        out[p + "dUdt"] = blk.dUdt().copy()
+
+
+def run_case(name):
+    overrides, mesh_f, ic_f, steps, snaps, ops_step, tableau = CASES[name]
+    cfg_kwargs = dict(BASE)
+    cfg_kwargs.update(overrides)
+    cfg = SolverConfig(initial_condition=ic_f(), fluid=AIR, **cfg_kwargs)
+    mesh = mesh_f()
+    solver = Euler2D(config=cfg, mesh_config=mesh)
+    if tableau is not None:
+        solver._time_integrator = ExplicitRungeKutta(cfg, a=tableau)
+    out = {}
+    encode_mesh(mesh_dict_of(mesh), out)
+    out["nx"] = np.array(cfg.nx)
+    out["ny"] = np.array(cfg.ny)
+    out["cfl"] = np.array(cfg.CFL)
+    out["t_final"] = np.array(cfg.t_final)
+    out["flux"] = np.array(cfg.fvm_flux_function_type)
+    out["limiter"] = np.array(cfg.fvm_slope_limiter_type)
+    out["recon"] = np.array(cfg.reconstruction_type.__name__)
+    out["integrator"] = np.array(cfg.time_integrator if tableau is None else "custom")
+    a = solver._time_integrator.a
+    tab = np.zeros((len(a), len(a)))
+    for i, row in enumerate(a):
+        tab[i, : len(row)] = row
+    out["tableau"] = tab
+    record_geometry(solver, out)
+    solver._pre_process_solve()
+    bnums = sorted(solver._blocks.blocks.keys())
+    out["ic"] = np.stack([solver._blocks[b].state.data.copy() for b in bnums])
+    dts, fps, ts = [], [], []
+    t0 = time.time()
+    for step in range(1, steps + 1):
+        if ops_step is not None and step == ops_step:
+            capture_ops(solver, out, "ops")
+            out["ops_state"] = np.stack([solver._blocks[b].state.data.copy() for b in bnums])
+        dt = solver.get_dt()
+        solver._update_solution_blocks(dt)
+        solver._realizability_check()
+        solver.t += dt
+        solver.num_time_step += 1
+        dts.append(dt)
+        ts.append(solver.t)
+        st = [solver._blocks[b].state.data for b in bnums]
+        fps.append(fingerprint(st))
+        if snaps == "all" or step in snaps:
+            out[f"state_{step}"] = np.stack([s.copy() for s in st])
+        if step == steps:
+            out["sums_final"] = np.array([[s[:, :, k].sum() for k in range(4)] for s in st])
+    out["dts"] = np.array(dts)
+    out["ts"] = np.array(ts)
+    out["fingerprints"] = np.array(fps)
+    out["steps"] = np.array(steps)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: {steps} steps in {time.time() - t0:.1f}s -> {os.path.getsize(path) / 1e3:.0f} kB", flush=True)
+
+
+if __name__ == "__main__":
+    names = sys.argv[1:] or list(CASES)
+    if len(names) > 1 and os.environ.get("GOLDEN_SERIAL") is None:
+        import multiprocessing as mp
+
+        with mp.get_context("spawn").Pool(min(len(names), os.cpu_count() or 1)) as pool:
+            pool.map(run_case, names)
+    else:
+        for n in names:
+            run_case(n)
