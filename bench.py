@@ -1,0 +1,379 @@
+#!/usr/bin/env python
+"""Benchmark: cell-stage updates/s of the GB300 FP64 MUSCL/RK4 path.
+
+Workload (the multiblock explosion throughput configuration): domain [0,10]x[0,20] as
+2x4 blocks of 1024x1024 cells (8,388,608 cells), ideal gas gamma 1.4, explosion
+initial condition, MUSCL order 2 with Green-Gauss gradients, Venkatakrishnan limiter,
+Roe flux, conservative reconstruction, reflecting walls, RK4 at CFL 0.8, FP64.
+A step is one RK4 step (4 residual evaluations) of every block, CFL dt included.
+
+  value   device-resident throughput: K steps of the device time loop (e2d_run),
+          timed with CUDA events on the solver's stream.  Each stage streams
+          ~2.5 GB (state, geometry, face arrays), so the working set exceeds the
+          129 MB L2 between iterations without a flush.
+  e2e     the same metric through the C ABI with host buffers: each step copies the
+          state from pinned host memory (e2d_set_state), steps once (e2d_run) and
+          copies the state back (e2d_get_state).
+  roofline  the dominant kernel's algorithmic FP64 flops per launch divided by its
+          CUDA-event duration, against this GPU's measured DFMA rate.
+  cpu_baseline  the CPU oracle (a C restatement of the reference algorithm) on
+          every host core, timed on one full step of the same workload.
+
+``--impl reference`` times the reference algorithm's CPU implementation (the same C
+restatement, all host threads) on the same workload and prints its own line.
+Multi-GPU: replicas only (each rank advances its own copy of the workload; there is
+no inter-GPU exchange in this single-GPU path); value sums the ranks' cells.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "multiblock explosion 2x4 blocks x 1024x1024 cells, Roe/Venkatakrishnan/Green-Gauss/RK4, CFL 0.8"
+METRIC = "cell-stage updates/s (FP64 plain, multiblock explosion 2x4x1024^2, RK4)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=1024, help="cells per block side")
+    ap.add_argument("--cpu-steps", type=int, default=1, help="RK4 steps in the CPU-baseline sample")
+    return ap.parse_args()
+
+
+def make_solver(n: int, device_solver: bool = True):
+    """Euler2D for the workload with the initial condition applied (state on host)."""
+    from pyhype_gb300.fluids import Air
+    from pyhype_gb300.initial_conditions import ExplosionInitialCondition
+    from pyhype_gb300.mesh import RectagularMeshGenerator
+    from pyhype_gb300.solver_config import SolverConfig
+    from pyhype_gb300.states import ConservativeState
+
+    air = Air(a_inf=343.0, rho_inf=1.0)
+    cfg = SolverConfig(
+        fvm_type="MUSCL", fvm_spatial_order=2, fvm_num_quadrature_points=1, fvm_gradient_type="GreenGauss",
+        fvm_flux_function_type="Roe", fvm_slope_limiter_type="Venkatakrishnan", time_integrator="RK4",
+        initial_condition=ExplosionInitialCondition(), interface_interpolation="arithmetic_average",
+        reconstruction_type=ConservativeState, CFL=0.8, t_final=0.07, fluid=air, nx=n, ny=n, nghost=1,
+    )
+    mesh = RectagularMeshGenerator.generate(["Reflection"], ["Reflection"], ["Reflection"], ["Reflection"],
+                                            east=10.0, west=0.0, north=20.0, south=0.0,
+                                            n_blocks_horizontal=2, n_blocks_vertical=4)
+    if device_solver:
+        from pyhype_gb300.solvers import Euler2D
+
+        s = Euler2D(config=cfg, mesh_config=mesh)
+        s.apply_initial_condition()
+        return s, cfg
+    # host-only: problem + initial state for the CPU arm
+    from pyhype_gb300.problem import problem_from_config
+    from pyhype_gb300.solvers import HostBlock
+
+    P = problem_from_config(cfg, mesh.dict)
+    blocks = []
+    for k, blk in enumerate(P.block_ids):
+        d = mesh.dict[blk]
+        hb = HostBlock(cfg, blk, P.block_geometry[k], {c: d[c] for c in ("NE", "NW", "SE", "SW")}, {}, {})
+        cfg.initial_condition.apply_to_block(hb)
+        blocks.append(hb.state.data)
+    return (P, P.to_soa(blocks)), cfg
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in getattr(self, "lines", []):
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax = float(p[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, p[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(n: int, steps: int):
+    """The CPU oracle on every host core, one full RK4 step of the workload per sample."""
+    from oracle.oracle import Oracle, lib
+    from pyhype_gb300.time_marching import tableau
+
+    (P, U), cfg = make_solver(n, device_solver=False)
+    threads = os.cpu_count() or 1
+    O = Oracle(P, threads=threads)
+    a = tableau("RK4")
+    dt = float(O.dt(U)[0])
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        U = O.step(U, a, dt, 0.0)
+    el = time.perf_counter() - t0
+    used = lib().oracle_max_threads()
+    return {
+        "value": P.ncell * 4 * steps / el,
+        "unit": "cell-stage updates/s",
+        "cores": int(used),
+        "kind": "port",
+        "sample": f"{steps} RK4 step(s) of the full {P.ncell}-cell workload, {el:.2f} s wall on {used} threads",
+    }
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: the reference algorithm's CPU implementation (C restatement,
+    all host threads) on the same workload; rank 0 only."""
+    if rank != 0:
+        return
+    from oracle.oracle import Oracle, lib
+    from pyhype_gb300.time_marching import tableau
+
+    (P, U), cfg = make_solver(args.n, device_solver=False)
+    O = Oracle(P, threads=os.cpu_count() or 1)
+    a = tableau("RK4")
+    t = 0.0
+    for _ in range(args.warmup):
+        dt = float(O.dt(U)[0])
+        U = O.step(U, a, dt, t)
+        t += dt
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dt = float(O.dt(U)[0])
+        U = O.step(U, a, dt, t)
+        t += dt
+    el = time.perf_counter() - t0
+    value = P.ncell * 4 * args.steps / el
+    used = int(lib().oracle_max_threads())
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "cell-stage updates/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": P.ncell, "l2": "working set > L2"},
+        "cpu_baseline": {"value": value, "unit": "cell-stage updates/s", "cores": used, "kind": "port",
+                         "sample": f"every step is one full RK4 step of the workload on {used} host threads"},
+        "e2e": {"value": value, "unit": "cell-stage updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from pyhype_gb300 import _native
+    from pyhype_gb300.roofline import BYTES_PER_CELL_STAGE_FP64, kernel_flops
+
+    torch.cuda.set_device(local)
+    solver, cfg = make_solver(args.n)
+    dev = solver.device
+    P = solver.problem
+    stream = torch.cuda.Stream()
+    dev.set_stream(stream.cuda_stream)
+    solver.upload()
+    L = _native.load()
+    L.e2d_bench_fp64_peak.argtypes = [ctypes.c_int32, ctypes.c_void_p]
+    L.e2d_bench_kernels.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+
+    t = 0.0
+    t_final = 1e30
+    t, _ = dev.run(t, t_final, max_steps=args.warmup)
+    torch.cuda.synchronize()
+    barrier(ws)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        t, done = dev.run(t, t_final, max_steps=args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    assert done == args.steps
+    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(ms, ws)
+    stages = 4
+    value = ws * P.ncell * stages * args.steps / (ms * 1e-3)
+
+    # e2e through the C ABI with host buffers (pinned), one step per call
+    host = torch.empty((4, P.ncell), dtype=torch.float64, pin_memory=True)
+    dev.get_state(host.numpy())
+    e2e_steps = max(3, min(args.steps, 10))
+    barrier(ws)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(e2e_steps):
+        L.e2d_set_state(dev.h, ctypes.c_void_p(host.data_ptr()))
+        t, _ = dev.run(t, t_final, max_steps=1)
+        L.e2d_get_state(dev.h, ctypes.c_void_p(host.data_ptr()))
+    f1.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = max_over_ranks(f0.elapsed_time(f1), ws)
+    e2e_value = ws * P.ncell * stages * e2e_steps / (ms_e2e * 1e-3)
+    nbytes = 4 * P.ncell * 8
+
+    # per-kernel event timing + measured FP64 rate -> roofline of the dominant kernel
+    kms = np.zeros(5)
+    kcnt = np.zeros(5, dtype=np.int64)
+    code = L.e2d_bench_kernels(dev.h, 2, kms.ctypes.data, kcnt.ctypes.data)
+    if code != 0:
+        raise RuntimeError(L.e2d_last_error().decode())
+    names = ["dt", "reconstruct", "flux", "update", "bookkeeping"]
+    share = kms * kcnt
+    dom = int(np.argmax(share))
+    peak_fma = ctypes.c_double(0.0)
+    peak_add = ctypes.c_double(0.0)
+    L.e2d_bench_fp64_peak(0, ctypes.byref(peak_fma))
+    L.e2d_bench_fp64_peak(1, ctypes.byref(peak_add))
+    flops = kernel_flops(names[dom], P.ncell, P.nvface, P.nhface)
+    achieved = flops / (kms[dom] * 1e-3) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_per_cell.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            tr = json.load(fh)
+        if names[dom] in tr:
+            traffic = tr[names[dom]] * P.ncell
+    peaks = {}
+    ppath = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(ppath):
+        with open(ppath) as fh:
+            peaks = json.load(fh)
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    step_ms = ms / args.steps
+    hbm_achieved = P.ncell * stages * BYTES_PER_CELL_STAGE_FP64 / (step_ms * 1e-3) / 1e9
+
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "cell-stage updates/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": step_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": P.ncell, "blocks": P.nblocks, "stages_per_step": stages,
+                   "l2": "inputs larger than L2 (state 268 MB, ~2.5 GB streamed per stage)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "e2e": {"value": e2e_value, "unit": "cell-stage updates/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes, "steps": e2e_steps},
+        "roofline": {
+            "bound": "fp64", "kernel": names[dom], "achieved": achieved, "peak": peak_fma.value,
+            "unit": "TFLOP/s", "frac": achieved / peak_fma.value if peak_fma.value else None,
+            "traffic": traffic,
+            "peak_source": "measured in-run: DFMA chains over all SMs (2 flops per DFMA); DADD rate "
+                           f"{peak_add.value:.3f} TFLOP/s",
+            "kernel_ms": {n: float(x) for n, x in zip(names, kms)},
+            "kernel_share": {n: float(s / share.sum()) for n, s in zip(names, share)},
+            "flops_per_launch": flops,
+            "hbm": {"achieved_gbs": hbm_achieved, "peak_gbs": hbm_peak,
+                    "frac": hbm_achieved / hbm_peak, "bytes_per_cell_stage": BYTES_PER_CELL_STAGE_FP64,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"},
+        },
+        "gpu_launches": int(args.steps * (3 + 3 * stages)),
+        "clocks": clocks,
+    }
+    if rank == 0 and ws == 1:
+        try:
+            line["cpu_baseline"] = cpu_baseline(args.n, args.cpu_steps)
+        except Exception as exc:  # the GPU number stands without it
+            line["cpu_baseline"] = {"value": None, "error": str(exc)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

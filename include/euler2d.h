@@ -31,6 +31,12 @@
 extern "C" {
 #endif
 
+#if defined(__GNUC__)
+#define E2D_API __attribute__((visibility("default")))
+#else
+#define E2D_API
+#endif
+
 #define E2D_ABI_VERSION 1
 
 /* ---- status codes ---------------------------------------------------------- */
@@ -184,48 +190,48 @@ typedef struct {
 
 typedef struct E2DSolver* E2DHandle;
 
-int e2d_abi_version(void);
-const char* e2d_last_error(void);
+E2D_API int e2d_abi_version(void);
+E2D_API const char* e2d_last_error(void);
 
 /* ---- lifecycle ---------------------------------------------------------------- */
 /* Replaces Blocks.build + QuadBlock construction (pyhype/blocks/base.py:515-572). */
-int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* geo,
+E2D_API int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* geo,
                E2DHandle* out);
-int e2d_destroy(E2DHandle h);
+E2D_API int e2d_destroy(E2DHandle h);
 /* Use a caller stream (cudaStream_t as void*); NULL selects the handle's own. */
-int e2d_set_stream(E2DHandle h, void* stream);
-int64_t e2d_num_cells(E2DHandle h);
+E2D_API int e2d_set_stream(E2DHandle h, void* stream);
+E2D_API int64_t e2d_num_cells(E2DHandle h);
 
 /* ---- state transfer ------------------------------------------------------------- */
-int e2d_set_state(E2DHandle h, const double* host_soa);
-int e2d_get_state(E2DHandle h, double* host_soa);
-int e2d_set_state_device(E2DHandle h, const double* dev_soa);
-int e2d_get_state_device(E2DHandle h, double* dev_soa);
+E2D_API int e2d_set_state(E2DHandle h, const double* host_soa);
+E2D_API int e2d_get_state(E2DHandle h, double* host_soa);
+E2D_API int e2d_set_state_device(E2DHandle h, const double* dev_soa);
+E2D_API int e2d_get_state_device(E2DHandle h, double* dev_soa);
 
 /* ---- time integration ---------------------------------------------------------- */
 /* Butcher rows of ExplicitRungeKutta (pyhype/time_marching/explicit_runge_kutta.py:
    91-274): nstages rows, row s holds a[s][0..s]; row-major nstages x nstages.     */
-int e2d_set_tableau(E2DHandle h, int32_t nstages, const double* a);
+E2D_API int e2d_set_tableau(E2DHandle h, int32_t nstages, const double* a);
 /* Solver.get_dt without the t_final clamp: CFL * min over all cells of all blocks
    (pyhype/solvers/base.py:114-136, pyhype/blocks/quad_block.py:423-436).
    Batched problems write one value per instance.                                  */
-int e2d_compute_dt(E2DHandle h, double* dt_host);
+E2D_API int e2d_compute_dt(E2DHandle h, double* dt_host);
 /* One ExplicitRungeKutta.integrate(dt) including the ghost/BC refresh after every
    stage; t is the solver time at the start of the step (moving BCs).              */
-int e2d_step(E2DHandle h, double dt, double t);
+E2D_API int e2d_step(E2DHandle h, double dt, double t);
 /* The Euler2D._solve loop (pyhype/solvers/Euler2D.py:361-376): dt -> clamp to
    t_final - t -> step -> realizability, until t >= t_final or max_steps.  Time is
    non-dimensional (t_final already multiplied by a_inf).  *t_inout is updated.
    Returns E2D_ERR_UNREALIZABLE (with *real filled) if a step produced rho<=0 or
    E<=0.                                                                            */
-int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps,
+E2D_API int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps,
             int32_t* steps_done, E2DRealizability* real);
-int e2d_check_realizable(E2DHandle h, E2DRealizability* out);
+E2D_API int e2d_check_realizable(E2DHandle h, E2DRealizability* out);
 
 /* ---- per-operator entry points (parity testing) ---------------------------------- */
 /* dUdt of the current state (FiniteVolumeMethod.dUdt, pyhype/fvm/base.py:108-139)
    into a caller device buffer of 4 cell planes; optional intermediates in dbg.    */
-int e2d_residual(E2DHandle h, double* dudt_dev, const E2DDebug* dbg);
+E2D_API int e2d_residual(E2DHandle h, double* dudt_dev, const E2DDebug* dbg);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,612 @@
+// e2d_api.cu - the C ABI declared in include/euler2d.h.
+//
+// A handle owns, in one GPU's memory: the block table, the geometry planes, the
+// tile tables that map CTAs to (block, tile), the state buffers of the RK stage
+// program, the face-indexed L/R state and flux arrays, and the per-instance time
+// state.  Host calls enqueue work on the handle's stream; a time loop can be
+// replayed from a captured CUDA graph because dt and t live on the device.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "e2d_kernels.cuh"
+#include "../../include/euler2d_bench.h"
+
+using namespace e2d;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) return fail(E2D_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+__global__ void k_reset_min(InstanceState* inst, int n) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) inst[q].min_bits = 0x7ff0000000000000ULL;
+}
+
+__global__ void k_reset_real(RealizState* r) {
+  r->first = ~0ULL;
+  r->nbad = 0;
+}
+
+}  // namespace
+
+struct E2DSolver {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  E2DConfig cfg{};
+  std::vector<E2DBlock> hblocks;
+  Params P{};
+  E2DBlock* dblocks = nullptr;
+  std::vector<void*> allocs;
+  double* geo = nullptr;
+  int4* cell_tiles = nullptr;
+  int ncell_tiles = 0;
+  int4* face_tiles = nullptr;
+  int nface_tiles = 0;
+  FaceArrays F{};
+  StateBuffers S{};
+  int nbuf = 0;
+  InstanceState* inst = nullptr;
+  std::vector<InstanceState> hinst;
+  RealizState* real = nullptr;
+  int nstages = 0;
+  std::vector<StageProgram> prog;
+  std::vector<int> stage_input;
+  // captured step graphs, keyed by the number of steps they replay
+  std::vector<std::pair<int, cudaGraphExec_t>> graphs;
+  int64_t ncell = 0, nvface = 0, nhface = 0;
+
+  void drop_graphs() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    graphs.clear();
+  }
+  ~E2DSolver() {
+    drop_graphs();
+    for (void* p : allocs) cudaFree(p);
+    if (own) cudaStreamDestroy(own);
+  }
+  template <typename T>
+  int alloc(T** p, size_t count) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) return fail(E2D_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", sizeof(T) * count, cudaGetErrorString(e));
+    allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return 0;
+  }
+};
+
+// Stage program of a Butcher tableau (rows = stages; row s uses k_0..k_s).  Buffer 0
+// holds U^n and, after the last stage, U^{n+1}; buffer r+1 holds row r's partial sum
+// for r < S-1; buffer S holds the last row's partial sum until the last stage.  Each
+// stage adds dt*a[r][s]*k_s to every row r >= s with a nonzero coefficient, in
+// increasing s, which is the reference's summation order
+// (explicit_runge_kutta.py:63-80).
+static int build_program(E2DSolver* h, int S, const double* a) {
+  if (S < 1 || S > MAX_STAGES) return fail(E2D_ERR_INVALID, "nstages must be in [1, %d]", MAX_STAGES);
+  h->prog.assign(S, StageProgram{});
+  h->stage_input.assign(S, 0);
+  auto row_buf = [&](int r) { return r == S - 1 ? S : r + 1; };
+  std::vector<int> started(S, 0);
+  for (int s = 0; s < S; ++s) {
+    // input of stage s: row s-1's buffer if it has any term, else U^n
+    if (s > 0) {
+      bool any = false;
+      for (int j = 0; j < s; ++j) any = any || a[(s - 1) * S + j] != 0.0;
+      h->stage_input[s] = any ? row_buf(s - 1) : 0;
+    }
+    StageProgram& p = h->prog[s];
+    p.nupd = 0;
+    p.final_stage = (s == S - 1);
+    for (int r = s; r < S; ++r) {
+      double c = a[r * S + s];
+      if (c == 0.0) continue;
+      StageUpdate u;
+      u.a = c;
+      u.src = started[r] ? row_buf(r) : 0;
+      u.dst = (r == S - 1 && s == S - 1) ? 0 : row_buf(r);
+      started[r] = 1;
+      p.upd[p.nupd++] = u;
+    }
+    if (s == S - 1) {
+      // the final row's last term may sit in an earlier column: then U^{n+1} is the
+      // finished partial sum (or U^n itself if the row is all zeros)
+      bool wrote0 = false;
+      for (int u = 0; u < p.nupd; ++u) wrote0 = wrote0 || p.upd[u].dst == 0;
+      if (!wrote0 && started[S - 1]) {
+        if (p.nupd >= MAX_STAGES) return fail(E2D_ERR_INVALID, "stage program overflow");
+        StageUpdate u;
+        u.a = 0.0;
+        u.src = row_buf(S - 1);
+        u.dst = 0;
+        p.upd[p.nupd++] = u;  // dta = 0: exact copy for finite k
+      }
+    }
+  }
+  h->nstages = S;
+  return 0;
+}
+
+static int ensure_buffers(E2DSolver* h) {
+  int need = h->nstages + 1;
+  for (int b = h->nbuf; b < need; ++b) {
+    if (int e = h->alloc(&h->S.buf[b], 4 * (size_t)h->ncell)) return e;
+    if (b > 0) CK(cudaMemsetAsync(h->S.buf[b], 0, sizeof(double) * 4 * h->ncell, h->stream));
+  }
+  if (need > h->nbuf) h->nbuf = need;
+  h->drop_graphs();
+  return 0;
+}
+
+extern "C" {
+
+int e2d_abi_version(void) { return E2D_ABI_VERSION; }
+const char* e2d_last_error(void) { return g_err.c_str(); }
+
+int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* geo, E2DHandle* out) {
+  if (!cfg || !blocks || !geo || !out) return fail(E2D_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (cfg->nblocks < 1) return fail(E2D_ERR_INVALID, "nblocks must be >= 1");
+  if (cfg->precision != E2D_FP64) return fail(E2D_ERR_UNSUPPORTED, "this entry point builds the FP64 path");
+  if (cfg->flux < 0 || cfg->flux > 2 || cfg->limiter < 0 || cfg->limiter > 3 || cfg->recon < 0 || cfg->recon > 1)
+    return fail(E2D_ERR_INVALID, "unknown flux/limiter/reconstruction code");
+  const int ninst = cfg->ninstances > 0 ? cfg->ninstances : 1;
+  // validate the block table before anything touches the device
+  int64_t ncell = 0, nv = 0, nh = 0;
+  for (int b = 0; b < cfg->nblocks; ++b) {
+    const E2DBlock& B = blocks[b];
+    if (B.nx < 2 || B.ny < 2) return fail(E2D_ERR_INVALID, "block %d: nx, ny must be >= 2", b);
+    if (B.instance < 0 || B.instance >= ninst) return fail(E2D_ERR_INVALID, "block %d: bad instance id", b);
+    if (B.cell_offset < 0 || B.vface_offset < 0 || B.hface_offset < 0)
+      return fail(E2D_ERR_INVALID, "block %d: negative offset", b);
+    for (int s = 0; s < 4; ++s) {
+      int k = B.side_kind[s];
+      if (k < E2D_SIDE_NEIGHBOR || k > E2D_SIDE_MIXED) return fail(E2D_ERR_INVALID, "block %d side %d: bad kind", b, s);
+      if (k == E2D_SIDE_NEIGHBOR) {
+        int n = B.neighbor[s];
+        if (n < 0 || n >= cfg->nblocks) return fail(E2D_ERR_INVALID, "block %d side %d: neighbour %d out of range", b, s, n);
+        const E2DBlock& N = blocks[n];
+        if ((s <= E2D_W && N.ny != B.ny) || (s >= E2D_N && N.nx != B.nx))
+          return fail(E2D_ERR_INVALID, "block %d side %d: neighbour size mismatch", b, s);
+        if (N.instance != B.instance) return fail(E2D_ERR_INVALID, "block %d side %d: neighbour in another instance", b, s);
+      }
+      if (k == E2D_SIDE_MIXED) {
+        const E2DMixedSide& m = B.mixed[s];
+        if (!B.side_coord[s]) return fail(E2D_ERR_INVALID, "block %d side %d: MIXED side without coordinates", b, s);
+        for (int kk : {m.kind_below, m.kind_above})
+          if (kk != E2D_SIDE_REFLECT && kk != E2D_SIDE_DIRICHLET)
+            return fail(E2D_ERR_INVALID, "block %d side %d: MIXED sub-kind must be REFLECT or DIRICHLET", b, s);
+      }
+    }
+    int64_t e1 = B.cell_offset + (int64_t)B.nx * B.ny;
+    int64_t e2 = B.vface_offset + (int64_t)B.ny * (B.nx + 1);
+    int64_t e3 = B.hface_offset + (int64_t)(B.ny + 1) * B.nx;
+    ncell = e1 > ncell ? e1 : ncell;
+    nv = e2 > nv ? e2 : nv;
+    nh = e3 > nh ? e3 : nh;
+  }
+  for (int p = 0; p < E2D_G_NCELL; ++p)
+    if (!geo->cell[p]) return fail(E2D_ERR_INVALID, "geometry cell plane %d missing", p);
+  for (int p = 0; p < E2D_F_NFACE; ++p)
+    if (!geo->vface[p] || !geo->hface[p]) return fail(E2D_ERR_INVALID, "geometry face plane %d missing", p);
+
+  E2DSolver* h = new E2DSolver();
+  auto bail = [&](int code) {
+    delete h;
+    return code;
+  };
+  cudaError_t ce = cudaGetDevice(&h->device);
+  if (ce != cudaSuccess) return bail(fail(E2D_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(ce)));
+  ce = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) return bail(fail(E2D_ERR_CUDA, "stream: %s", cudaGetErrorString(ce)));
+  h->stream = h->own;
+  h->cfg = *cfg;
+  h->ncell = ncell;
+  h->nvface = nv;
+  h->nhface = nh;
+  h->hblocks.assign(blocks, blocks + cfg->nblocks);
+
+  // geometry planes: one allocation, planes back to back
+  const size_t ngeo = (size_t)E2D_G_NCELL * ncell + (size_t)E2D_F_NFACE * (nv + nh);
+  if (int e = h->alloc(&h->geo, ngeo)) return bail(e);
+  {
+    double* p = h->geo;
+    for (int k = 0; k < E2D_G_NCELL; ++k, p += ncell) {
+      if ((ce = cudaMemcpy(p, geo->cell[k], sizeof(double) * ncell, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail(fail(E2D_ERR_CUDA, "geometry copy: %s", cudaGetErrorString(ce)));
+      h->P.geo.cell[k] = p;
+    }
+    for (int k = 0; k < E2D_F_NFACE; ++k, p += nv) {
+      if ((ce = cudaMemcpy(p, geo->vface[k], sizeof(double) * nv, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail(fail(E2D_ERR_CUDA, "geometry copy: %s", cudaGetErrorString(ce)));
+      h->P.geo.vface[k] = p;
+    }
+    for (int k = 0; k < E2D_F_NFACE; ++k, p += nh) {
+      if ((ce = cudaMemcpy(p, geo->hface[k], sizeof(double) * nh, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail(fail(E2D_ERR_CUDA, "geometry copy: %s", cudaGetErrorString(ce)));
+      h->P.geo.hface[k] = p;
+    }
+  }
+  // block table with MIXED side coordinates moved to the device
+  std::vector<E2DBlock> dev_blocks = h->hblocks;
+  for (int b = 0; b < cfg->nblocks; ++b)
+    for (int s = 0; s < 4; ++s) {
+      if (dev_blocks[b].side_kind[s] != E2D_SIDE_MIXED) {
+        dev_blocks[b].side_coord[s] = nullptr;
+        continue;
+      }
+      const int len = s <= E2D_W ? dev_blocks[b].ny : dev_blocks[b].nx;
+      double* d = nullptr;
+      if (int e = h->alloc(&d, len)) return bail(e);
+      if ((ce = cudaMemcpy(d, blocks[b].side_coord[s], sizeof(double) * len, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail(fail(E2D_ERR_CUDA, "coord copy: %s", cudaGetErrorString(ce)));
+      dev_blocks[b].side_coord[s] = d;
+    }
+  if (int e = h->alloc(&h->dblocks, cfg->nblocks)) return bail(e);
+  if ((ce = cudaMemcpy(h->dblocks, dev_blocks.data(), sizeof(E2DBlock) * cfg->nblocks, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return bail(fail(E2D_ERR_CUDA, "block table copy: %s", cudaGetErrorString(ce)));
+
+  // tile tables: cells (ny x nx) and face nodes ((ny+1) x (nx+1)) per block
+  std::vector<int4> ct, ft;
+  for (int b = 0; b < cfg->nblocks; ++b) {
+    const E2DBlock& B = h->hblocks[b];
+    for (int i0 = 0; i0 < B.ny; i0 += TY)
+      for (int j0 = 0; j0 < B.nx; j0 += TX) ct.push_back(make_int4(b, i0, j0, 0));
+    for (int i0 = 0; i0 <= B.ny; i0 += TY)
+      for (int j0 = 0; j0 <= B.nx; j0 += TX) ft.push_back(make_int4(b, i0, j0, 0));
+  }
+  h->ncell_tiles = (int)ct.size();
+  h->nface_tiles = (int)ft.size();
+  if (int e = h->alloc(&h->cell_tiles, ct.size())) return bail(e);
+  if (int e = h->alloc(&h->face_tiles, ft.size())) return bail(e);
+  if ((ce = cudaMemcpy(h->cell_tiles, ct.data(), sizeof(int4) * ct.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (ce = cudaMemcpy(h->face_tiles, ft.data(), sizeof(int4) * ft.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return bail(fail(E2D_ERR_CUDA, "tile copy: %s", cudaGetErrorString(ce)));
+
+  // face arrays
+  if (int e = h->alloc(&h->F.vL, 4 * (size_t)nv)) return bail(e);
+  if (int e = h->alloc(&h->F.vR, 4 * (size_t)nv)) return bail(e);
+  if (int e = h->alloc(&h->F.vI, 4 * (size_t)nv)) return bail(e);
+  if (int e = h->alloc(&h->F.hL, 4 * (size_t)nh)) return bail(e);
+  if (int e = h->alloc(&h->F.hR, 4 * (size_t)nh)) return bail(e);
+  if (int e = h->alloc(&h->F.hI, 4 * (size_t)nh)) return bail(e);
+
+  // instance time state and realizability counters
+  h->hinst.assign(ninst, InstanceState{});
+  for (auto& I : h->hinst) {
+    I.min_bits = 0x7ff0000000000000ULL;
+    I.t_final = INFINITY;
+    I.max_steps = 0x7fffffff;
+  }
+  if (int e = h->alloc(&h->inst, ninst)) return bail(e);
+  if ((ce = cudaMemcpy(h->inst, h->hinst.data(), sizeof(InstanceState) * ninst, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return bail(fail(E2D_ERR_CUDA, "instance copy: %s", cudaGetErrorString(ce)));
+  if (int e = h->alloc(&h->real, 1)) return bail(e);
+  k_reset_real<<<1, 1, 0, h->stream>>>(h->real);
+
+  h->P.blocks = h->dblocks;
+  h->P.nblocks = cfg->nblocks;
+  h->P.ncell = ncell;
+  h->P.nvface = nv;
+  h->P.nhface = nh;
+  h->P.gamma = cfg->gamma;
+  h->P.gm1 = cfg->gm1;
+  h->P.gm = cfg->gamma / (cfg->gamma - 1.0);
+  h->P.k = 1.0 / (cfg->gamma - 1.0);
+  h->P.cfl = cfg->cfl;
+  h->P.flux = cfg->flux;
+  h->P.limiter = cfg->limiter;
+  h->P.recon = cfg->recon;
+
+  // default integrator: the classical RK4 rows (explicit_runge_kutta.py:212-224)
+  const double rk4[16] = {0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1, 0, 1.0 / 6, 1.0 / 3, 1.0 / 3, 1.0 / 6};
+  if (int e = build_program(h, 4, rk4)) return bail(e);
+  if (int e = ensure_buffers(h)) return bail(e);
+  if ((ce = cudaStreamSynchronize(h->stream)) != cudaSuccess)
+    return bail(fail(E2D_ERR_CUDA, "create: %s", cudaGetErrorString(ce)));
+  *out = h;
+  return 0;
+}
+
+int e2d_destroy(E2DHandle h) {
+  if (!h) return 0;
+  cudaStreamSynchronize(h->stream);
+  delete h;
+  return 0;
+}
+
+int e2d_set_stream(E2DHandle h, void* stream) {
+  if (!h) return fail(E2D_ERR_INVALID, "null handle");
+  h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own;
+  h->drop_graphs();
+  return 0;
+}
+
+int64_t e2d_num_cells(E2DHandle h) { return h ? h->ncell : -1; }
+
+int e2d_set_state(E2DHandle h, const double* host_soa) {
+  if (!h || !host_soa) return fail(E2D_ERR_INVALID, "null argument");
+  CK(cudaMemcpyAsync(h->S.buf[0], host_soa, sizeof(double) * 4 * h->ncell, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int e2d_get_state(E2DHandle h, double* host_soa) {
+  if (!h || !host_soa) return fail(E2D_ERR_INVALID, "null argument");
+  CK(cudaMemcpyAsync(host_soa, h->S.buf[0], sizeof(double) * 4 * h->ncell, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int e2d_set_state_device(E2DHandle h, const double* dev_soa) {
+  if (!h || !dev_soa) return fail(E2D_ERR_INVALID, "null argument");
+  CK(cudaMemcpyAsync(h->S.buf[0], dev_soa, sizeof(double) * 4 * h->ncell, cudaMemcpyDeviceToDevice, h->stream));
+  return 0;
+}
+
+int e2d_get_state_device(E2DHandle h, double* dev_soa) {
+  if (!h || !dev_soa) return fail(E2D_ERR_INVALID, "null argument");
+  CK(cudaMemcpyAsync(dev_soa, h->S.buf[0], sizeof(double) * 4 * h->ncell, cudaMemcpyDeviceToDevice, h->stream));
+  return 0;
+}
+
+int e2d_set_tableau(E2DHandle h, int32_t nstages, const double* a) {
+  if (!h || !a) return fail(E2D_ERR_INVALID, "null argument");
+  for (int r = 0; r < nstages; ++r)
+    for (int c = r + 1; c < nstages; ++c)
+      if (a[r * nstages + c] != 0.0) return fail(E2D_ERR_INVALID, "tableau must be lower triangular (explicit)");
+  if (int e = build_program(h, nstages, a)) return e;
+  return ensure_buffers(h);
+}
+
+static int enqueue_stages(E2DHandle h, double* dudt_out, const DebugOut* dbg) {
+  for (int s = 0; s < h->nstages; ++s) {
+    const double* in = h->S.buf[h->stage_input[s]];
+    CK(launch_reconstruct(h->P, h->cell_tiles, h->ncell_tiles, in, h->inst, h->F, dbg, h->stream));
+    CK(launch_flux(h->P, h->face_tiles, h->nface_tiles, h->inst, h->F, dbg, h->stream));
+    CK(launch_update(h->P, h->cell_tiles, h->ncell_tiles, h->F, h->S, h->prog[s], h->inst, h->real, dudt_out,
+                     h->stream));
+  }
+  return 0;
+}
+
+static int enqueue_run_step(E2DHandle h) {
+  const int ninst = (int)h->hinst.size();
+  CK(launch_dt(h->P, h->cell_tiles, h->ncell_tiles, h->S.buf[0], h->inst, h->stream));
+  CK(launch_begin_step(h->inst, ninst, h->P.cfl, 1, h->stream));
+  if (int e = enqueue_stages(h, nullptr, nullptr)) return e;
+  CK(launch_end_step(h->inst, ninst, h->real, h->stream));
+  return 0;
+}
+
+int e2d_compute_dt(E2DHandle h, double* dt_host) {
+  if (!h || !dt_host) return fail(E2D_ERR_INVALID, "null argument");
+  const int ninst = (int)h->hinst.size();
+  k_reset_min<<<(ninst + 127) / 128, 128, 0, h->stream>>>(h->inst, ninst);
+  CK(cudaGetLastError());
+  CK(launch_dt(h->P, h->cell_tiles, h->ncell_tiles, h->S.buf[0], h->inst, h->stream));
+  CK(cudaMemcpyAsync(h->hinst.data(), h->inst, sizeof(InstanceState) * ninst, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int q = 0; q < ninst; ++q) {
+    double m;
+    unsigned long long b = h->hinst[q].min_bits;
+    std::memcpy(&m, &b, sizeof m);
+    dt_host[q] = h->P.cfl * m;
+  }
+  return 0;
+}
+
+int e2d_step(E2DHandle h, double dt, double t) {
+  if (!h) return fail(E2D_ERR_INVALID, "null handle");
+  const int ninst = (int)h->hinst.size();
+  CK(launch_set_time(h->inst, ninst, t, dt, h->stream));
+  if (int e = enqueue_stages(h, nullptr, nullptr)) return e;
+  CK(launch_end_step(h->inst, ninst, h->real, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int e2d_residual(E2DHandle h, double* dudt_dev, const E2DDebug* d) {
+  if (!h || !dudt_dev) return fail(E2D_ERR_INVALID, "null argument");
+  const int ninst = (int)h->hinst.size();
+  double t = h->hinst.empty() ? 0.0 : h->hinst[0].t;
+  CK(launch_set_time(h->inst, ninst, t, 0.0, h->stream));
+  DebugOut dbg{};
+  const DebugOut* pd = nullptr;
+  if (d) {
+    dbg.gx = d->gx; dbg.gy = d->gy; dbg.phi = d->phi;
+    dbg.vflux_raw = d->vflux_raw; dbg.hflux_raw = d->hflux_raw;
+    dbg.vflux = d->vflux; dbg.hflux = d->hflux;
+    pd = &dbg;
+  }
+  StageProgram none{};
+  none.nupd = 0;
+  none.final_stage = 0;
+  CK(launch_reconstruct(h->P, h->cell_tiles, h->ncell_tiles, h->S.buf[0], h->inst, h->F, pd, h->stream));
+  CK(launch_flux(h->P, h->face_tiles, h->nface_tiles, h->inst, h->F, pd, h->stream));
+  CK(launch_update(h->P, h->cell_tiles, h->ncell_tiles, h->F, h->S, none, h->inst, h->real, dudt_dev, h->stream));
+  if (d) {
+    const size_t bv = sizeof(double) * 4 * h->nvface, bh = sizeof(double) * 4 * h->nhface;
+    if (d->vL) CK(cudaMemcpyAsync(d->vL, h->F.vL, bv, cudaMemcpyDeviceToDevice, h->stream));
+    if (d->vR) CK(cudaMemcpyAsync(d->vR, h->F.vR, bv, cudaMemcpyDeviceToDevice, h->stream));
+    if (d->hL) CK(cudaMemcpyAsync(d->hL, h->F.hL, bh, cudaMemcpyDeviceToDevice, h->stream));
+    if (d->hR) CK(cudaMemcpyAsync(d->hR, h->F.hR, bh, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  CK(launch_end_step(h->inst, ninst, h->real, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int e2d_check_realizable(E2DHandle h, E2DRealizability* out) {
+  if (!h || !out) return fail(E2D_ERR_INVALID, "null argument");
+  k_reset_real<<<1, 1, 0, h->stream>>>(h->real);
+  CK(cudaGetLastError());
+  CK(launch_realizable(h->P, h->cell_tiles, h->ncell_tiles, h->S.buf[0], h->real, h->stream));
+  RealizState r;
+  CK(cudaMemcpyAsync(&r, h->real, sizeof r, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  out->ok = r.nbad == 0;
+  out->nbad = (int64_t)r.nbad;
+  out->block = r.nbad ? (int32_t)(r.first >> 40) : -1;
+  out->cell = r.nbad ? (int64_t)(r.first & ((1ULL << 40) - 1)) : -1;
+  return out->ok ? 0 : fail(E2D_ERR_UNREALIZABLE, "unrealizable state in block %d cell %lld", out->block, (long long)out->cell);
+}
+
+// Capture `steps` run-steps into one graph (replayed until the instances stop).
+static int get_graph(E2DHandle h, int steps, cudaGraphExec_t* out) {
+  for (auto& g : h->graphs)
+    if (g.first == steps) {
+      *out = g.second;
+      return 0;
+    }
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int err = 0;
+  for (int k = 0; k < steps && !err; ++k) err = enqueue_run_step(h);
+  cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+  if (err) {
+    if (g) cudaGraphDestroy(g);
+    return err;
+  }
+  if (ce != cudaSuccess) return fail(E2D_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+  cudaGraphExec_t ex = nullptr;
+  ce = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) return fail(E2D_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+  h->graphs.emplace_back(steps, ex);
+  *out = ex;
+  return 0;
+}
+
+int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps, int32_t* steps_done,
+            E2DRealizability* realo) {
+  if (!h || !t_inout) return fail(E2D_ERR_INVALID, "null argument");
+  const int ninst = (int)h->hinst.size();
+  for (auto& I : h->hinst) {
+    I.t = *t_inout;
+    I.t_final = t_final;
+    I.max_steps = max_steps;
+    I.steps = 0;
+    I.halted = 0;
+    I.active = 0;
+    I.min_bits = 0x7ff0000000000000ULL;
+  }
+  CK(cudaMemcpyAsync(h->inst, h->hinst.data(), sizeof(InstanceState) * ninst, cudaMemcpyHostToDevice, h->stream));
+  k_reset_real<<<1, 1, 0, h->stream>>>(h->real);
+  CK(cudaGetLastError());
+  // steps per host check: enough to amortise the launch of a graph, few enough that
+  // the inactive tail after t_final is cheap
+  const int chunk = max_steps < 8 ? (max_steps > 0 ? max_steps : 1) : 8;
+  cudaGraphExec_t gx = nullptr;
+  if (int e = get_graph(h, chunk, &gx)) return e;
+  for (;;) {
+    CK(cudaGraphLaunch(gx, h->stream));
+    CK(cudaMemcpyAsync(h->hinst.data(), h->inst, sizeof(InstanceState) * ninst, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    bool any = false, halted = false;
+    for (auto& I : h->hinst) {
+      halted = halted || I.halted;
+      any = any || (!I.halted && I.t < I.t_final && I.steps < I.max_steps);
+    }
+    if (!any || halted) break;
+  }
+  *t_inout = h->hinst[0].t;
+  if (steps_done) *steps_done = h->hinst[0].steps;
+  RealizState r;
+  CK(cudaMemcpyAsync(&r, h->real, sizeof r, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (realo) {
+    realo->ok = r.nbad == 0;
+    realo->nbad = (int64_t)r.nbad;
+    realo->block = r.nbad ? (int32_t)(r.first >> 40) : -1;
+    realo->cell = r.nbad ? (int64_t)(r.first & ((1ULL << 40) - 1)) : -1;
+  }
+  if (r.nbad) return fail(E2D_ERR_UNREALIZABLE, "unrealizable state after step %d", h->hinst[0].steps);
+  return 0;
+}
+
+
+// Per-kernel CUDA-event timing of `steps` device-loop steps (euler2d_bench.h).
+int e2d_bench_kernels(E2DHandle h, int32_t steps, double* ms, int64_t* launches) {
+  if (!h || !ms || steps < 1) return fail(E2D_ERR_INVALID, "bad argument");
+  const int ninst = (int)h->hinst.size();
+  for (auto& I : h->hinst) {
+    I.t_final = INFINITY;
+    I.max_steps = 0x7fffffff;
+    I.steps = 0;
+    I.halted = 0;
+    I.min_bits = 0x7ff0000000000000ULL;
+  }
+  CK(cudaMemcpyAsync(h->inst, h->hinst.data(), sizeof(InstanceState) * ninst, cudaMemcpyHostToDevice, h->stream));
+  k_reset_real<<<1, 1, 0, h->stream>>>(h->real);
+  const int per_step = 3 + 3 * h->nstages;
+  std::vector<cudaEvent_t> ev(2 * per_step * steps);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  std::vector<int> cls;
+  int k = 0;
+  auto rec = [&](int c) { cls.push_back(c); return cudaEventRecord(ev[k++], h->stream); };
+  auto fin = [&]() { return cudaEventRecord(ev[k++], h->stream); };
+  for (int st = 0; st < steps; ++st) {
+    CK(rec(0));
+    CK(launch_dt(h->P, h->cell_tiles, h->ncell_tiles, h->S.buf[0], h->inst, h->stream));
+    CK(fin());
+    CK(rec(4));
+    CK(launch_begin_step(h->inst, ninst, h->P.cfl, 1, h->stream));
+    CK(fin());
+    for (int s = 0; s < h->nstages; ++s) {
+      const double* in = h->S.buf[h->stage_input[s]];
+      CK(rec(1));
+      CK(launch_reconstruct(h->P, h->cell_tiles, h->ncell_tiles, in, h->inst, h->F, nullptr, h->stream));
+      CK(fin());
+      CK(rec(2));
+      CK(launch_flux(h->P, h->face_tiles, h->nface_tiles, h->inst, h->F, nullptr, h->stream));
+      CK(fin());
+      CK(rec(3));
+      CK(launch_update(h->P, h->cell_tiles, h->ncell_tiles, h->F, h->S, h->prog[s], h->inst, h->real, nullptr,
+                       h->stream));
+      CK(fin());
+    }
+    CK(rec(4));
+    CK(launch_end_step(h->inst, ninst, h->real, h->stream));
+    CK(fin());
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  double tot[E2D_BENCH_NK] = {0, 0, 0, 0, 0};
+  int64_t cnt[E2D_BENCH_NK] = {0, 0, 0, 0, 0};
+  for (size_t q = 0; q < cls.size(); ++q) {
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, ev[2 * q], ev[2 * q + 1]));
+    tot[cls[q]] += t;
+    cnt[cls[q]] += 1;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  for (int c = 0; c < E2D_BENCH_NK; ++c) {
+    ms[c] = cnt[c] ? tot[c] / cnt[c] : 0.0;
+    if (launches) launches[c] = cnt[c];
+  }
+  CK(cudaMemcpyAsync(h->hinst.data(), h->inst, sizeof(InstanceState) * ninst, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+}  // extern "C"

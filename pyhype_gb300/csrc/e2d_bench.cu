@@ -1,0 +1,65 @@
+// e2d_bench.cu - FP64 instruction-throughput probe (see include/euler2d_bench.h).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+
+#include "../../include/euler2d_bench.h"
+
+namespace {
+
+template <int OP>
+__global__ void k_fp64_chain(double* out, int iters, double seed) {
+  double a0 = seed + threadIdx.x, a1 = a0 + 1.0, a2 = a0 + 2.0, a3 = a0 + 3.0;
+  double a4 = a0 + 4.0, a5 = a0 + 5.0, a6 = a0 + 6.0, a7 = a0 + 7.0;
+  const double m = 1.0000000001, c = 1e-9;
+  for (int i = 0; i < iters; ++i) {
+    if (OP == 0) {
+      a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+      a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+    } else if (OP == 1) {
+      a0 = a0 + c; a1 = a1 + c; a2 = a2 + c; a3 = a3 + c;
+      a4 = a4 + c; a5 = a5 + c; a6 = a6 + c; a7 = a7 + c;
+    } else {
+      a0 = a0 * m; a1 = a1 * m; a2 = a2 * m; a3 = a3 * m;
+      a4 = a4 * m; a5 = a5 * m; a6 = a6 * m; a7 = a7 * m;
+    }
+  }
+  double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (s == 12345.678) out[blockIdx.x] = s;  // keeps the chains live, never true in practice
+}
+
+}  // namespace
+
+extern "C" int e2d_bench_fp64_peak(int32_t op, double* tflops) {
+  if (!tflops || op < 0 || op > 2) return E2D_ERR_INVALID;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return E2D_ERR_CUDA;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  double* out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * 65536) != cudaSuccess) return E2D_ERR_NOMEM;
+  const int blocks = sms * 8, threads = 256, iters = 2048;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 0.0;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(e0);
+    if (op == 0) k_fp64_chain<0><<<blocks, threads>>>(out, iters, 1.0);
+    else if (op == 1) k_fp64_chain<1><<<blocks, threads>>>(out, iters, 1.0);
+    else k_fp64_chain<2><<<blocks, threads>>>(out, iters, 1.0);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double inst = (double)blocks * threads * iters * 8.0;
+    const double fl = inst * (op == 0 ? 2.0 : 1.0) / (ms * 1e-3) / 1e12;
+    if (rep > 0 && fl > best) best = fl;  // first launch is warm-up
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return E2D_ERR_CUDA;
+  *tflops = best;
+  return 0;
+}

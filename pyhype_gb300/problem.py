@@ -206,12 +206,15 @@ def build_problem(
     precision: int = 0,
     instance_of: Optional[Dict[int, int]] = None,
     sizes: Optional[Dict[int, tuple]] = None,
+    geometries: Optional[Dict[int, BlockGeometry]] = None,
 ) -> Problem:
     """Assemble the block table and the geometry planes.
 
     ``sizes`` optionally gives per-block ``(nx, ny)`` (independent batched instances);
     otherwise every block uses ``nx, ny`` as the reference does
-    (``pyhype/solvers/base.py:472-482``).
+    (``pyhype/solvers/base.py:472-482``).  ``geometries`` optionally supplies
+    precomputed block geometry (e.g. arrays recorded from another platform, whose
+    libm may round arctan/cos differently in the last bit).
     """
     if flux not in FLUX:
         raise ValueError(f"Flux function type {flux} is not available.")
@@ -226,7 +229,10 @@ def build_problem(
     for blk in ids:
         d = mesh_dict[blk]
         bnx, bny = (sizes[blk] if sizes is not None else (nx, ny))
-        g = build_block_geometry({k: d[k] for k in ("NE", "NW", "SE", "SW")}, bnx, bny)
+        if geometries is not None and blk in geometries:
+            g = geometries[blk]
+        else:
+            g = build_block_geometry({k: d[k] for k in ("NE", "NW", "SE", "SW")}, bnx, bny)
         geos.append(g)
         dims.append((bnx, bny))
         sides = []

@@ -1,0 +1,57 @@
+"""Algorithmic work per launch of each FP64 stage kernel, for the roofline.
+
+Counts are +, -, *, /, sqrt = 1 flop each (min/max/compare/abs/negation = 0), read
+off the kernel code on its dominant path: Roe flux, Venkatakrishnan limiter,
+conservative reconstruction, Cartesian block, interior cell, no Harten correction
+triggered.  Divisions and square roots are listed separately because each costs the
+FP64 pipe several instruction slots (a reciprocal seed plus Newton steps).
+
+k_reconstruct, per cell (4 variables):
+  interface averages        4 x (add + mul)                         =  8 / var
+  Green-Gauss gx, gy        2 x (4 mul + 3 add + 1 mul)             = 16 / var
+  dmax, dmin                2 sub                                    =  2 / var
+  per side (4): high-order term 3, davg 2, slope 1 div,
+                Venkatakrishnan 5 + 1 div                           = 48 / var
+  limited face states       4 x (mul + add)                         =  8 / var
+                                                          -> 82 x 4 = 328
+  4 face states to primitive (2 div + 7)                              =  36
+  total 364 flops, 40 of them divisions
+k_flux, per face (Roe):
+  Roe average 18 (1 div, 3 sqrt), 3 sound speeds 9 (3 div, 3 sqrt), speeds 6,
+  Harten 4, H/ua/1/a/r2a/h 13 (2 div), dW 4, Lp dW 8, |L| 4, Rc 22,
+  F(WL)+F(WR) 26, flux combine 16, 2 L F 8                             = 138
+  (6 divisions, 6 square roots); a cell owns 2 faces
+k_update, per cell-stage: divergence 5 / var = 20, RK4 stage program on average
+  1.75 updates x (1 + 4 x 2)                                           = 35.75
+k_dt, per cell (once per step): conversion 9 (2 div), sound 3 (1 div, 1 sqrt),
+  2 x (add + div)                                                      = 16
+"""
+from __future__ import annotations
+
+FLOPS_PER_CELL_RECONSTRUCT = 364
+FLOPS_PER_FACE_ROE = 138
+FLOPS_PER_CELL_UPDATE_RK4 = 35.75
+FLOPS_PER_CELL_DT = 16
+DIV_PER_CELL_RECONSTRUCT = 40
+DIV_PER_FACE_ROE = 6
+SQRT_PER_FACE_ROE = 6
+
+# Algorithmic HBM bytes per cell-stage of the whole stage (state reads/writes and
+# geometry of the cell and its two owned faces), FP64, RK4 low-storage average:
+# U_s 32 + U^n 32 + accumulator read+write 64 + U_{s+1} 32 + geometry 64 (A, 1/A and
+# 8 quadrature offsets ... counted once per cell).  Face-array traffic between the
+# three kernels and halo re-reads are implementation overhead, not counted.
+BYTES_PER_CELL_STAGE_FP64 = 224
+
+
+def kernel_flops(kind: str, ncell: int, nvface: int, nhface: int) -> float:
+    """Algorithmic flops of one launch of a kernel class over the whole problem."""
+    if kind == "reconstruct":
+        return FLOPS_PER_CELL_RECONSTRUCT * ncell
+    if kind == "flux":
+        return FLOPS_PER_FACE_ROE * (nvface + nhface)
+    if kind == "update":
+        return FLOPS_PER_CELL_UPDATE_RK4 * ncell
+    if kind == "dt":
+        return FLOPS_PER_CELL_DT * ncell
+    return 0.0

@@ -38,15 +38,45 @@ def mesh_dict(z) -> dict:
     return out
 
 
-def problem(z, precision: int = 0):
+def geometry(z, b: int):
+    """BlockGeometry assembled from the reference's recorded mesh arrays of block b.
+
+    The transcendental functions behind the face angles and areas (numpy arctan,
+    arccos, cos, sin) may round differently on another platform; parity with the
+    reference's run is judged on the reference's own geometry."""
+    from pyhype_gb300.mesh.quad_mesh import BlockGeometry
+
+    p = f"geo{b}_"
+    g = {k[len(p):]: z[k] for k in z.files if k.startswith(p)}
+    v = lambda w, e: np.ascontiguousarray(np.concatenate([w[:, :1], e], axis=1))  # noqa: E731
+    h = lambda s, n: np.ascontiguousarray(np.concatenate([s[:1, :], n], axis=0))  # noqa: E731
+    ny, nx = g["A"].shape
+    return BlockGeometry(
+        nx=nx, ny=ny, nodes_x=g["nodes_x"], nodes_y=g["nodes_y"], xc=g["xc"], yc=g["yc"], A=g["A"],
+        dx=g["dx"], dy=g["dy"],
+        v_L=v(g["LW"], g["LE"]), v_theta=v(g["thW"], g["thE"]),
+        v_cos=v(g["cos_scalarW"], g["cos_scalarE"]), v_sin=v(g["sin_scalarW"], g["sin_scalarE"]),
+        v_mid_x=None, v_mid_y=None,
+        h_L=h(g["LS"], g["LN"]), h_theta=h(g["thS"], g["thN"]),
+        h_cos=h(g["cos_scalarS"], g["cos_scalarN"]), h_sin=h(g["sin_scalarS"], g["sin_scalarN"]),
+        h_mid_x=None, h_mid_y=None,
+        qE_x=g["qxE"], qE_y=g["qyE"], qW_x=g["qxW"], qW_y=g["qyW"],
+        qN_x=g["qxN"], qN_y=g["qyN"], qS_x=g["qxS"], qS_y=g["qyS"],
+        is_cartesian=bool(g["is_cartesian"]),
+    )
+
+
+def problem(z, precision: int = 0, reference_geometry: bool = True):
     from pyhype_gb300.fluids import Air
     from pyhype_gb300.problem import build_problem
 
     air = Air(a_inf=343.0, rho_inf=1.0)
+    geos = {int(b): geometry(z, int(b)) for b in z["blk_ids"]} if reference_geometry else None
     return build_problem(
         mesh_dict(z), int(z["nx"]), int(z["ny"]),
         flux=str(z["flux"]), limiter=str(z["limiter"]), recon=str(z["recon"]),
         gamma=air.gamma(), gm1=air.gamma() - 1, cfl=float(z["cfl"]), fluid=air, precision=precision,
+        geometries=geos,
     )
 
 

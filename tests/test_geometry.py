@@ -36,3 +36,23 @@ def test_rectangular_generator_corners():
     nbr = np.array([[-1 if m.dict[b]["Neighbor" + s] is None else m.dict[b]["Neighbor" + s] for s in "EWNS"]
                     for b in sorted(m.dict)])
     assert np.array_equal(nbr, z["neighbors"])
+
+
+@pytest.mark.parametrize("name", ["m2x4_40", "dmr_example", "p100"])
+def test_problem_planes_from_own_geometry_equal_reference_geometry(name):
+    """On this platform the geometry planes built from the product's own mesh code are
+    the ones built from the reference's recorded arrays."""
+    z = G.load(name)
+    a = G.problem(z, reference_geometry=True)
+    b = G.problem(z, reference_geometry=False)
+    import ctypes
+    import numpy as np
+    for k in range(12):
+        pa = np.ctypeslib.as_array(a.geometry.cell[k], shape=(a.ncell,))
+        pb = np.ctypeslib.as_array(b.geometry.cell[k], shape=(b.ncell,))
+        assert np.array_equal(pa, pb), k
+    for k in range(5):
+        assert np.array_equal(np.ctypeslib.as_array(a.geometry.vface[k], shape=(a.nvface,)),
+                              np.ctypeslib.as_array(b.geometry.vface[k], shape=(b.nvface,)))
+        assert np.array_equal(np.ctypeslib.as_array(a.geometry.hface[k], shape=(a.nhface,)),
+                              np.ctypeslib.as_array(b.geometry.hface[k], shape=(b.nhface,)))

@@ -1,0 +1,90 @@
+"""CUDA path (through the C ABI) against the CPU oracle and the reference fixtures.
+
+The bar is value equality (bit-exact up to the sign of zero) for every per-operator
+intermediate, the dt of every step and the state after every step."""
+import numpy as np
+import pytest
+
+import _golden as G
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+CASES = G.cases()
+OPS_CASES = [c for c in CASES if "ops_state" in G.load(c).files]
+
+
+def _solver(z):
+    from pyhype_gb300._native import DeviceSolver
+
+    P = G.problem(z)
+    return P, DeviceSolver(P, tableau=z["tableau"])
+
+
+def _eq(a, b):
+    return a.shape == b.shape and np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", OPS_CASES)
+def test_residual_intermediates_vs_oracle(name):
+    z = G.load(name)
+    P, S = _solver(z)
+    U = P.to_soa(list(z["ops_state"]))
+    S.set_state(U)
+    dudt, dbg = S.residual(debug=True)
+    ref, rdbg = Oracle(P).residual(U, debug=True)
+    for key in ("gx", "gy", "phi", "vL", "vR", "hL", "hR", "vflux_raw", "hflux_raw", "vflux", "hflux"):
+        assert _eq(dbg[key], rdbg[key]), f"{key}: max diff {np.max(np.abs(dbg[key] - rdbg[key]))}"
+    assert _eq(dudt, ref), f"dUdt: max diff {np.max(np.abs(dudt - ref))}"
+    # and against the reference's own dUdt
+    for b in range(P.nblocks):
+        assert _eq(P.from_soa(dudt)[b], z[f"ops{int(z['blk_ids'][b])}_dUdt"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_steps_vs_reference(name):
+    """Per-step: dt equal, state fingerprint equal to the reference's."""
+    z = G.load(name)
+    P, S = _solver(z)
+    S.set_state(P.to_soa(list(z["ic"])))
+    t, tf = 0.0, G.t_final(z)
+    for step in range(1, int(z["steps"]) + 1):
+        dt = float(S.compute_dt()[0])
+        if tf - t < dt:
+            dt = tf - t
+        assert dt == z["dts"][step - 1], f"step {step}: dt {dt!r} vs {z['dts'][step - 1]!r}"
+        S.step(dt, t)
+        t += dt
+        blocks = P.from_soa(S.get_state())
+        if f"state_{step}" in z.files:
+            ref = z[f"state_{step}"]
+            assert np.array_equal(np.stack(blocks), ref), f"step {step}: max diff {np.max(np.abs(np.stack(blocks) - ref))}"
+        assert G.fingerprint(blocks) == str(z["fingerprints"][step - 1]), f"fingerprint after step {step}"
+
+
+@pytest.mark.parametrize("name", ["p100", "m2x4_40", "dmr_example", "ti_DormandPrince5", "bc_mixed"])
+def test_device_loop_vs_reference(name):
+    """The device-resident time loop (dt, clamp, stages, t += dt on the GPU, replayed
+    from a CUDA graph) reproduces the reference's whole run."""
+    z = G.load(name)
+    P, S = _solver(z)
+    S.set_state(P.to_soa(list(z["ic"])))
+    n = int(z["steps"])
+    t, steps = S.run(0.0, G.t_final(z), max_steps=n)
+    assert steps == n
+    assert t == z["ts"][n - 1]
+    assert G.fingerprint(P.from_soa(S.get_state())) == str(z["fingerprints"][n - 1])
+
+
+def test_run_stops_at_t_final():
+    """t_final clamp: the last step is shortened so t lands exactly on t_final."""
+    z = G.load("ops_explosion_cons")
+    P, S = _solver(z)
+    U0 = P.to_soa(list(z["ic"]))
+    S.set_state(U0)
+    tf = 0.5 * float(z["ts"][2])
+    t, steps = S.run(0.0, tf, max_steps=1000)
+    Ut, t_or, dts = Oracle(P).run(U0, z["tableau"], 0.0, tf, 1000)
+    assert t == tf == t_or
+    assert steps == len(dts)
+    assert np.array_equal(S.get_state(), Ut)
