@@ -230,8 +230,9 @@ E2D_API int e2d_check_realizable(E2DHandle h, E2DRealizability* out);
 
 /* ---- per-operator entry points (parity testing) ---------------------------------- */
 /* dUdt of the current state (FiniteVolumeMethod.dUdt, pyhype/fvm/base.py:108-139)
-   into a caller device buffer of 4 cell planes; optional intermediates in dbg.    */
-E2D_API int e2d_residual(E2DHandle h, double* dudt_dev, const E2DDebug* dbg);
+   at solver time t (time-dependent sides) into a caller device buffer of 4 cell
+   planes; optional intermediates in dbg.                                           */
+E2D_API int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* dbg);
 
 #ifdef __cplusplus
 }

@@ -75,7 +75,7 @@ def load(path: Optional[str] = None):
     L.e2d_run.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_int32,
                           ctypes.POINTER(ctypes.c_int32), vp]
     L.e2d_check_realizable.argtypes = [vp, vp]
-    L.e2d_residual.argtypes = [vp, vp, vp]
+    L.e2d_residual.argtypes = [vp, ctypes.c_double, vp, vp]
     if L.e2d_abi_version() != 1:
         raise RuntimeError("libeuler2d.so ABI version mismatch")
     _lib = L
@@ -164,7 +164,7 @@ class DeviceSolver:
             _check(code)
         return r
 
-    def residual(self, debug: bool = False):
+    def residual(self, debug: bool = False, t: float = 0.0):
         """dUdt of the current state (host copy), optionally with the intermediates."""
         import torch  # device buffers for the per-operator outputs
 
@@ -179,12 +179,12 @@ class DeviceSolver:
                       "vflux": P.nvface, "hflux": P.nhface}
             dbg_t = {k: torch.zeros((4, n), dtype=torch.float64, device=dev) for k, n in shapes.items()}
             d = E2DDebug()
-            for k, t in dbg_t.items():
-                setattr(d, k, ctypes.cast(t.data_ptr(), c_double_p))
+            for k, buf in dbg_t.items():
+                setattr(d, k, ctypes.cast(buf.data_ptr(), c_double_p))
             self._dbg = d
             dptr = ctypes.addressof(d)
         torch.cuda.synchronize()
-        _check(self.L.e2d_residual(self.h, ctypes.c_void_p(dudt.data_ptr()), dptr))
+        _check(self.L.e2d_residual(self.h, float(t), ctypes.c_void_p(dudt.data_ptr()), dptr))
         out = dudt.cpu().numpy()
         if debug:
             return out, {k: v.cpu().numpy() for k, v in dbg_t.items()}

@@ -426,10 +426,9 @@ int e2d_step(E2DHandle h, double dt, double t) {
   return 0;
 }
 
-int e2d_residual(E2DHandle h, double* dudt_dev, const E2DDebug* d) {
+int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* d) {
   if (!h || !dudt_dev) return fail(E2D_ERR_INVALID, "null argument");
   const int ninst = (int)h->hinst.size();
-  double t = h->hinst.empty() ? 0.0 : h->hinst[0].t;
   CK(launch_set_time(h->inst, ninst, t, 0.0, h->stream));
   DebugOut dbg{};
   const DebugOut* pd = nullptr;

@@ -20,6 +20,19 @@ def fingerprint(arrays) -> str:
     return h.hexdigest()[:32]
 
 
+def _device_bc(name: str, side: str):
+    """Device boundary condition for the fixtures' custom reference BC objects (the
+    double-Mach setup of make_golden.py)."""
+    from pyhype_gb300.configs import double_mach_bcs
+
+    west, south, north = double_mach_bcs()
+    if name == "Dirichlet":
+        return west()
+    if name == "Switch":
+        return {"S": south, "N": north}[side]()
+    return None if name == "None" else name
+
+
 def mesh_dict(z) -> dict:
     out = {}
     for k, b in enumerate(z["blk_ids"]):
@@ -29,8 +42,7 @@ def mesh_dict(z) -> dict:
         for s, side in enumerate("EWNS"):
             nb = int(z["neighbors"][k, s])
             d["Neighbor" + side] = None if nb < 0 else nb
-            bc = str(z["bc"][k, s])
-            d["BCType" + side] = None if bc == "None" else bc
+            d["BCType" + side] = _device_bc(str(z["bc"][k, s]), side)
         for corner in ("NE", "NW", "SE", "SW"):
             d["Neighbor" + corner] = None
             d["BCType" + corner] = None
@@ -70,7 +82,8 @@ def problem(z, precision: int = 0, reference_geometry: bool = True):
     from pyhype_gb300.fluids import Air
     from pyhype_gb300.problem import build_problem
 
-    air = Air(a_inf=343.0, rho_inf=1.0)
+    a_inf = float(z["a_inf"]) if "a_inf" in z.files else 343.0
+    air = Air(a_inf=a_inf, rho_inf=1.0)
     geos = {int(b): geometry(z, int(b)) for b in z["blk_ids"]} if reference_geometry else None
     return build_problem(
         mesh_dict(z), int(z["nx"]), int(z["ny"]),
@@ -81,7 +94,8 @@ def problem(z, precision: int = 0, reference_geometry: bool = True):
 
 
 def t_final(z) -> float:
-    return float(z["t_final"]) * 343.0
+    a_inf = float(z["a_inf"]) if "a_inf" in z.files else 343.0
+    return float(z["t_final"]) * a_inf
 
 
 def cases():

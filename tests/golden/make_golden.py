@@ -101,6 +101,104 @@ class DMRExampleIC(InitialCondition):
         block.state.make_non_dimensional()
 
 
+# ---- double-Mach-reflection boundary conditions as reference BoundaryCondition objects ----
+from pyhype.boundary_conditions.base import BoundaryCondition  # noqa: E402
+from pyhype.boundary_conditions.funcs import BoundaryConditionFunctions  # noqa: E402
+
+HARNESS_CLOCK = [0.0]  # solver time at the start of the step the BC values are for
+
+
+def clock_ghost_fills(solver, num_stages):
+    """Ghost cells are filled at the end of every stage; the fill after a step's last
+    stage serves the next step.  Set the clock so that every boundary evaluation made
+    for step n (ghosts and boundary face states) sees t at the start of step n."""
+    blocks = solver._blocks
+    orig = blocks.apply_boundary_condition
+    state = {"stage": 0, "t": 0.0, "dt": 0.0}
+
+    def wrapped():
+        state["stage"] += 1
+        HARNESS_CLOCK[0] = state["t"] + state["dt"] if state["stage"] == num_stages else state["t"]
+        orig()
+
+    blocks.apply_boundary_condition = wrapped
+    return state
+
+
+def _prim_as(state, W):
+    """A fixed primitive state converted to the type of ``state`` (same converter the
+    reference's PrimitiveDirichletBC would use, at the ghost's shape)."""
+    arr = np.broadcast_to(np.asarray(W, dtype=float).reshape(1, 1, 4), state.data.shape).copy()
+    return PrimitiveState(fluid=state.fluid, array=arr).to_type(type(state)).data
+
+
+class DirichletBC(BoundaryCondition):
+    def __init__(self, W):
+        self.W = W
+
+    def _apply_boundary_condition(self, state, *args, **kwargs):
+        state.data = _prim_as(state, self.W)
+
+
+class SwitchBC(BoundaryCondition):
+    """Per boundary cell: ``below`` where the centroid coordinate along the side is
+    < x0 + speed * t, else ``above``; each is a primitive state or "Reflection"."""
+
+    def __init__(self, x0, speed, below, above):
+        self.x0, self.speed, self.below, self.above = x0, speed, below, above
+        self.coord = self.angle = None
+
+    def bind(self, block, side):
+        m = block.mesh
+        if side in ("N", "S"):
+            row = -1 if side == "N" else 0
+            self.coord = m.x[row, :, 0][None, :, None]
+        else:
+            col = -1 if side == "E" else 0
+            self.coord = m.y[:, col, 0][:, None, None]
+        d = {"E": Direction.east, "W": Direction.west, "N": Direction.north, "S": Direction.south}[side]
+        self.angle = m.boundary_angle(direction=d)
+
+    def _part(self, spec, state):
+        if isinstance(spec, str):
+            tmp = type(state)(fluid=state.fluid, array=state.data.copy())
+            BoundaryConditionFunctions.reflection(tmp, self.angle)
+            return tmp.data
+        return _prim_as(state, spec)
+
+    def _apply_boundary_condition(self, state, *args, **kwargs):
+        mask = self.coord < self.x0 + self.speed * HARNESS_CLOCK[0]
+        state.data = np.where(mask, self._part(self.below, state), self._part(self.above, state))
+
+
+DMR_PRE = [1.4, 0.0, 0.0, 1.0]
+DMR_POST = [8.0, 8.25 * np.cos(np.pi / 6), -8.25 * np.sin(np.pi / 6), 116.5]
+
+
+class DMRIC(InitialCondition):
+    """Mach-10 shock at 60 degrees through (1/6, 0): post-shock for x < 1/6 + y/sqrt(3)."""
+
+    def apply_to_block(self, block):
+        post = PrimitiveState(fluid=block.config.fluid, array=np.array(DMR_POST).reshape((1, 1, 4))).to_type(ConservativeState)
+        pre = PrimitiveState(fluid=block.config.fluid, array=np.array(DMR_PRE).reshape((1, 1, 4))).to_type(ConservativeState)
+        block.state.data = np.where(block.mesh.x < 1 / 6 + block.mesh.y / np.sqrt(3), post.data, pre.data)
+        block.state.make_non_dimensional()
+
+
+def dmr_mesh(nblk=5):
+    """[0,4]x[0,1] as nblk blocks in a row: post-shock inflow on the west side and on
+    the south side for x < 1/6, reflecting wall for x >= 1/6, the exact moving-shock
+    state on the north side, outflow east."""
+    from pyhype.mesh.base import QuadMeshGenerator
+
+    south = [SwitchBC(1 / 6, 0.0, DMR_POST, "Reflection") for _ in range(nblk)]
+    north = [SwitchBC(1 / 6 + 1 / np.sqrt(3), 20 / np.sqrt(3), DMR_POST, DMR_PRE) for _ in range(nblk)]
+    gen = QuadMeshGenerator(nx_blk=nblk, ny_blk=1, BCE=["OutletDirichlet"], BCW=[DirichletBC(DMR_POST)],
+                            BCN=north, BCS=south, SW=(0.0, 0.0), SE=(4.0, 0.0), NW=(0.0, 1.0), NE=(4.0, 1.0))
+    gen._switch = {"N": north, "S": south}
+    return gen
+
+
 def single_block(x0, x1, y0, y1, bce="Reflection", bcw="Reflection", bcn="Reflection", bcs="Reflection"):
     return {
         0: {
@@ -163,6 +261,7 @@ def rect_mesh(nbx, nby, east, north, bc="Reflection"):
 
 
 AIR = Air(a_inf=343.0, rho_inf=1.0)
+AIR_UNIT = Air(a_inf=1.0, rho_inf=1.0)
 
 BASE = dict(
     fvm_type="MUSCL",
@@ -199,6 +298,8 @@ CASES = {
     "dmr_example": (dict(nx=12, ny=12, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState, time_integrator="RK2", CFL=0.4), dmr_example_mesh, lambda: DMRExampleIC(), 5, "all", 2, None),
     "ssprk2_hlll": (dict(nx=20, ny=16, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState, CFL=0.4), lambda: single_block(0, 10, 0, 8), lambda: ExplosionIC(**MOVING), 4, "all", None, [[1], [0.5, 0.5]]),
 }
+CASES["dmr5"] = (dict(nx=16, ny=20, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState, CFL=0.4,
+                     t_final=0.2, fluid=AIR_UNIT), lambda: dmr_mesh(5), lambda: DMRIC(), 8, "all", 3, [[1], [0.5, 0.5]])
 for _ti in ("ExplicitEuler1", "RK2", "Ralston2", "RK3", "RK3SSP", "Ralston3", "Ralston4", "DormandPrince5"):
     CASES["ti_" + _ti] = (dict(nx=16, ny=16, time_integrator=_ti, CFL=0.4), lambda: single_block(0, 10, 0, 10), lambda: ExplosionIC(**MOVING), 3, "all", None, None)
 
@@ -222,7 +323,12 @@ def encode_mesh(mesh_cfg, out):
             v = d["Neighbor" + side]
             nbr[k, s] = -1 if v is None else v
             b = d["BCType" + side]
-            bc[k, s] = "None" if b is None else str(b)
+            if isinstance(b, SwitchBC):
+                bc[k, s] = "Switch"
+            elif isinstance(b, DirichletBC):
+                bc[k, s] = "Dirichlet"
+            else:
+                bc[k, s] = "None" if b is None else str(b)
     out["corners"] = corners
     out["neighbors"] = nbr
     out["bc"] = bc
@@ -309,9 +415,17 @@ def run_case(name):
     overrides, mesh_f, ic_f, steps, snaps, ops_step, tableau = CASES[name]
     cfg_kwargs = dict(BASE)
     cfg_kwargs.update(overrides)
-    cfg = SolverConfig(initial_condition=ic_f(), fluid=AIR, **cfg_kwargs)
+    fluid = cfg_kwargs.pop("fluid", AIR)
+    cfg = SolverConfig(initial_condition=ic_f(), fluid=fluid, **cfg_kwargs)
     mesh = mesh_f()
     solver = Euler2D(config=cfg, mesh_config=mesh)
+    # bind position-dependent BCs to the blocks that own them
+    for bnum, blk in solver._blocks.blocks.items():
+        d = mesh_dict_of(mesh)[bnum]
+        for side in "EWNS":
+            bc = d["BCType" + side]
+            if isinstance(bc, SwitchBC):
+                bc.bind(blk, side)
     if tableau is not None:
         solver._time_integrator = ExplicitRungeKutta(cfg, a=tableau)
     out = {}
@@ -320,6 +434,7 @@ def run_case(name):
     out["ny"] = np.array(cfg.ny)
     out["cfl"] = np.array(cfg.CFL)
     out["t_final"] = np.array(cfg.t_final)
+    out["a_inf"] = np.array(cfg.fluid.far_field.a)
     out["flux"] = np.array(cfg.fvm_flux_function_type)
     out["limiter"] = np.array(cfg.fvm_slope_limiter_type)
     out["recon"] = np.array(cfg.reconstruction_type.__name__)
@@ -330,6 +445,8 @@ def run_case(name):
         tab[i, : len(row)] = row
     out["tableau"] = tab
     record_geometry(solver, out)
+    HARNESS_CLOCK[0] = 0.0
+    clock = clock_ghost_fills(solver, solver._time_integrator.num_stages)
     solver._pre_process_solve()
     bnums = sorted(solver._blocks.blocks.keys())
     out["ic"] = np.stack([solver._blocks[b].state.data.copy() for b in bnums])
@@ -337,9 +454,13 @@ def run_case(name):
     t0 = time.time()
     for step in range(1, steps + 1):
         if ops_step is not None and step == ops_step:
+            HARNESS_CLOCK[0] = solver.t
+            out["ops_t"] = np.array(solver.t)
             capture_ops(solver, out, "ops")
             out["ops_state"] = np.stack([solver._blocks[b].state.data.copy() for b in bnums])
         dt = solver.get_dt()
+        HARNESS_CLOCK[0] = solver.t
+        clock.update(stage=0, t=solver.t, dt=dt)
         solver._update_solution_blocks(dt)
         solver._realizability_check()
         solver.t += dt

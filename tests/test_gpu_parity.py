@@ -31,8 +31,9 @@ def test_residual_intermediates_vs_oracle(name):
     P, S = _solver(z)
     U = P.to_soa(list(z["ops_state"]))
     S.set_state(U)
-    dudt, dbg = S.residual(debug=True)
-    ref, rdbg = Oracle(P).residual(U, debug=True)
+    t = float(z["ops_t"]) if "ops_t" in z.files else 0.0
+    dudt, dbg = S.residual(debug=True, t=t)
+    ref, rdbg = Oracle(P).residual(U, t=t, debug=True)
     for key in ("gx", "gy", "phi", "vL", "vR", "hL", "hR", "vflux_raw", "hflux_raw", "vflux", "hflux"):
         assert _eq(dbg[key], rdbg[key]), f"{key}: max diff {np.max(np.abs(dbg[key] - rdbg[key]))}"
     assert _eq(dudt, ref), f"dUdt: max diff {np.max(np.abs(dudt - ref))}"
@@ -62,7 +63,7 @@ def test_steps_vs_reference(name):
         assert G.fingerprint(blocks) == str(z["fingerprints"][step - 1]), f"fingerprint after step {step}"
 
 
-@pytest.mark.parametrize("name", ["p100", "m2x4_40", "dmr_example", "ti_DormandPrince5", "bc_mixed"])
+@pytest.mark.parametrize("name", ["p100", "m2x4_40", "dmr_example", "dmr5", "ti_DormandPrince5", "bc_mixed"])
 def test_device_loop_vs_reference(name):
     """The device-resident time loop (dt, clamp, stages, t += dt on the GPU, replayed
     from a CUDA graph) reproduces the reference's whole run."""

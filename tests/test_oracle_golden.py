@@ -17,7 +17,8 @@ OPS_CASES = [c for c in CASES if "ops_state" in G.load(c).files]
 def test_operator_intermediates(name):
     z = G.load(name)
     P = G.problem(z)
-    dudt, dbg = Oracle(P).residual(P.to_soa(list(z["ops_state"])), debug=True)
+    t = float(z["ops_t"]) if "ops_t" in z.files else 0.0
+    dudt, dbg = Oracle(P).residual(P.to_soa(list(z["ops_state"])), t=t, debug=True)
     for b in range(P.nblocks):
         p = f"ops{int(z['blk_ids'][b])}_"
         vf = P.vface_block(dbg["vflux"], b)
