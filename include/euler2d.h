@@ -234,6 +234,27 @@ E2D_API int e2d_check_realizable(E2DHandle h, E2DRealizability* out);
    planes; optional intermediates in dbg.                                           */
 E2D_API int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* dbg);
 
+/* ---- allocation-free CFL time step ----------------------------------------------
+   No counterpart in the reference.  For callers that may not allocate device
+   memory: an application that hands all of its GPU memory to its own pool
+   allocator and forbids cudaMalloc/cudaFree once it is running (an allocation
+   synchronizes the device and fragments the pool), so it cannot create a handle.
+   From caller-owned device buffers - the SoA state (4 planes of ncell doubles) and
+   the CFL_DX / CFL_DY geometry planes - it computes what e2d_compute_dt computes
+   for a single-instance problem: *dt_host = cfl * min over cells of
+   min(dx/(|u|+a), dy/(|v|+a)), bit for bit.  Its scratch is a file-scope device
+   array of E2D_NOALLOC_MAX_CELLS/256 + 1 eight-byte words (512 KiB) that every GPU
+   loading the library keeps until the process exits; ncell above
+   E2D_NOALLOC_MAX_CELLS returns E2D_ERR_INVALID.  The first call on a device looks
+   up that array's device address, so make it before any stream capture.  All calls
+   share the array and each overwrites the part it uses: calls that overlap on the
+   GPU (different streams or threads) race.  Runs on `stream` (NULL = legacy default
+   stream) and blocks until the result is on the host.                            */
+#define E2D_NOALLOC_MAX_CELLS 16777216
+E2D_API int e2d_compute_dt_noalloc(const double* dev_state, int64_t ncell, const double* dev_cfl_dx,
+                                   const double* dev_cfl_dy, double gamma, double gm1, double cfl,
+                                   void* stream, double* dt_host);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,6 +23,7 @@ UNITS = {
     "e2d_fp64.cu": ["-fmad=false"],
     "e2d_api.cu": ["-fmad=false"],
     "e2d_bench.cu": [],
+    "e2d_noalloc.cu": ["-fmad=false"],
 }
 
 

@@ -49,6 +49,14 @@ __global__ void k_reset_real(RealizState* r) {
 
 }  // namespace
 
+namespace e2d {
+// records the thread-local message returned by e2d_last_error (used by other units)
+int set_error(int code, const char* msg) {
+  g_err = msg;
+  return code;
+}
+}  // namespace e2d
+
 struct E2DSolver {
   int device = 0;
   cudaStream_t own = nullptr;
