@@ -37,7 +37,9 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = "multiblock explosion 2x4 blocks x 1024x1024 cells, Roe/Venkatakrishnan/Green-Gauss/RK4, CFL 0.8"
+WORKLOAD = ("multiblock explosion 2x4 blocks x 1024x1024 cells, Roe/Venkatakrishnan/Green-Gauss/RK4, CFL 0.8, "
+            "explosion IC with seeded cell noise (seed 0)")
+SEED = 0
 METRIC = "cell-stage updates/s (FP64 plain, multiblock explosion 2x4x1024^2, RK4)"
 
 
@@ -49,7 +51,27 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=1024, help="cells per block side")
     ap.add_argument("--cpu-steps", type=int, default=1, help="RK4 steps in the CPU-baseline sample")
+    ap.add_argument("--skip-cpu-baseline", action="store_true", help="omit the CPU baseline (profiling runs)")
     return ap.parse_args()
+
+
+def seeded_state(block, seed: int):
+    """Explosion state with seeded per-cell noise on every primitive variable (density
+    and pressure +-2 %, velocities +-0.01 of the far-field sound speed), so no region
+    of the synthetic input is uniform."""
+    import numpy as np
+
+    from pyhype_gb300.states import ConservativeState, PrimitiveState
+
+    fl = block.config.fluid
+    W = ConservativeState(fl, array=block.state.data.copy()).to_type(PrimitiveState).data
+    rng = np.random.default_rng(seed * 1000003 + block.global_block_num)
+    n = W.shape[:2]
+    W[:, :, 0] *= 1 + rng.uniform(-0.02, 0.02, n)
+    W[:, :, 3] *= 1 + rng.uniform(-0.02, 0.02, n)
+    W[:, :, 1] += rng.uniform(-0.01, 0.01, n)
+    W[:, :, 2] += rng.uniform(-0.01, 0.01, n)
+    block.state.data = PrimitiveState(fl, array=W).to_type(ConservativeState).data
 
 
 def make_solver(n: int, device_solver: bool = True):
@@ -75,6 +97,8 @@ def make_solver(n: int, device_solver: bool = True):
 
         s = Euler2D(config=cfg, mesh_config=mesh)
         s.apply_initial_condition()
+        for b in s.blocks:
+            seeded_state(b, SEED)
         return s, cfg
     # host-only: problem + initial state for the CPU arm
     from pyhype_gb300.problem import problem_from_config
@@ -86,6 +110,7 @@ def make_solver(n: int, device_solver: bool = True):
         d = mesh.dict[blk]
         hb = HostBlock(cfg, blk, P.block_geometry[k], {c: d[c] for c in ("NE", "NW", "SE", "SW")}, {}, {})
         cfg.initial_condition.apply_to_block(hb)
+        seeded_state(hb, SEED)
         blocks.append(hb.state.data)
     return (P, P.to_soa(blocks)), cfg
 
@@ -362,7 +387,7 @@ def main():
         "gpu_launches": int(args.steps * (3 + 3 * stages)),
         "clocks": clocks,
     }
-    if rank == 0 and ws == 1:
+    if rank == 0 and ws == 1 and not args.skip_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(args.n, args.cpu_steps)
         except Exception as exc:  # the GPU number stands without it
