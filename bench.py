@@ -352,6 +352,41 @@ def main():
     step_ms = ms / args.steps
     hbm_achieved = P.ncell * stages * BYTES_PER_CELL_STAGE_FP64 / (step_ms * 1e-3) / 1e9
 
+    # FP32 form on the same workload and seeded state (same warm-up + timed steps)
+    fp32 = None
+    try:
+        S32 = _native.DeviceSolver(P.with_precision(1), tableau=solver._time_integrator.tableau())
+        S32.set_stream(stream.cuda_stream)
+        S32.set_state(P.to_soa([b.state.data for b in solver.blocks]))
+        t32, _ = S32.run(0.0, t_final, max_steps=args.warmup)
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        t32, _ = S32.run(t32, t_final, max_steps=args.steps)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        ms32 = max_over_ranks(g0.elapsed_time(g1), ws)
+        k32 = np.zeros(5)
+        c32 = np.zeros(5, dtype=np.int64)
+        L.e2d_bench_kernels(S32.h, 2, k32.ctypes.data, c32.ctypes.data)
+        U64 = dev.get_state()
+        # the FP64 solver has taken e2e steps more; rerun FP64 to the same step count
+        S64b = _native.DeviceSolver(P, tableau=solver._time_integrator.tableau())
+        S64b.set_stream(stream.cuda_stream)
+        S64b.set_state(P.to_soa([b.state.data for b in solver.blocks]))
+        S64b.run(0.0, t_final, max_steps=args.warmup + args.steps)
+        U64 = S64b.get_state()
+        S32.run(t32, t_final, max_steps=0)
+        U32 = S32.get_state()
+        l1 = float(np.sum(np.abs(U32[0] - U64[0])) / np.sum(np.abs(U64[0])))
+        fp32 = {"value": ws * P.ncell * stages * args.steps / (ms32 * 1e-3), "unit": "cell-stage updates/s",
+                "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": ms / ms32,
+                "l1_density_rel_vs_fp64": l1, "l1_after_steps": args.warmup + args.steps,
+                "kernel_ms": {n: float(x) for n, x in zip(names, k32)}}
+        S32.close()
+        S64b.close()
+    except Exception as exc:
+        fp32 = {"error": str(exc)}
+
     clocks = clk.summary()
     line = {
         "metric": METRIC,
@@ -384,6 +419,7 @@ def main():
                     "frac": hbm_achieved / hbm_peak, "bytes_per_cell_stage": BYTES_PER_CELL_STAGE_FP64,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"},
         },
+        "fp32": fp32,
         "gpu_launches": int(args.steps * (3 + 3 * stages)),
         "clocks": clocks,
     }

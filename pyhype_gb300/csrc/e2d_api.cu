@@ -57,22 +57,32 @@ int set_error(int code, const char* msg) {
 }
 }  // namespace e2d
 
+// Everything that has the arithmetic type of a path: parameters (with the geometry
+// plane pointers), face arrays and state buffers.
+template <typename T>
+struct PathT {
+  ParamsT<T> P{};
+  T* geo = nullptr;
+  FaceArraysT<T> F{};
+  StateBuffersT<T> S{};
+  T* dudt_tmp = nullptr;  // FP32 residual staging for the FP64 caller buffer
+};
+
 struct E2DSolver {
   int device = 0;
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
   E2DConfig cfg{};
+  int prec = E2D_FP64;
   std::vector<E2DBlock> hblocks;
-  Params P{};
+  PathT<double> pd;
+  PathT<float> pf;
   E2DBlock* dblocks = nullptr;
   std::vector<void*> allocs;
-  double* geo = nullptr;
   int4* cell_tiles = nullptr;
   int ncell_tiles = 0;
   int4* face_tiles = nullptr;
   int nface_tiles = 0;
-  FaceArrays F{};
-  StateBuffers S{};
   int nbuf = 0;
   InstanceState* inst = nullptr;
   std::vector<InstanceState> hinst;
@@ -104,13 +114,26 @@ struct E2DSolver {
   }
 };
 
+template <typename T>
+PathT<T>& path(E2DSolver* h);
+template <>
+PathT<double>& path<double>(E2DSolver* h) { return h->pd; }
+template <>
+PathT<float>& path<float>(E2DSolver* h) { return h->pf; }
+
+// Run f<T>(h) for the handle's precision.
+#define E2D_DISPATCH(h, f, ...) ((h)->prec == E2D_FP32 ? f<float>(h, ##__VA_ARGS__) : f<double>(h, ##__VA_ARGS__))
+
 // Stage program of a Butcher tableau (rows = stages; row s uses k_0..k_s).  Buffer 0
 // holds U^n and, after the last stage, U^{n+1}; buffer r+1 holds row r's partial sum
 // for r < S-1; buffer S holds the last row's partial sum until the last stage.  Each
 // stage adds dt*a[r][s]*k_s to every row r >= s with a nonzero coefficient, in
 // increasing s, which is the reference's summation order
 // (explicit_runge_kutta.py:63-80).
+// On the FP32 path the last row is formed as an increment (from zero) that the last
+// stage adds to U^n with Kahan compensation, instead of as U^n + terms.
 static int build_program(E2DSolver* h, int S, const double* a) {
+  const bool kahan = h->prec == E2D_FP32;
   if (S < 1 || S > MAX_STAGES) return fail(E2D_ERR_INVALID, "nstages must be in [1, %d]", MAX_STAGES);
   h->prog.assign(S, StageProgram{});
   h->stage_input.assign(S, 0);
@@ -129,10 +152,15 @@ static int build_program(E2DSolver* h, int S, const double* a) {
     for (int r = s; r < S; ++r) {
       double c = a[r * S + s];
       if (c == 0.0) continue;
-      StageUpdate u;
+      StageUpdate u{};
       u.a = c;
       u.src = started[r] ? row_buf(r) : 0;
       u.dst = (r == S - 1 && s == S - 1) ? 0 : row_buf(r);
+      if (kahan && r == S - 1) {
+        u.src_zero = !started[r];
+        u.kahan = (s == S - 1);
+        u.dst = row_buf(r);
+      }
       started[r] = 1;
       p.upd[p.nupd++] = u;
     }
@@ -140,13 +168,14 @@ static int build_program(E2DSolver* h, int S, const double* a) {
       // the final row's last term may sit in an earlier column: then U^{n+1} is the
       // finished partial sum (or U^n itself if the row is all zeros)
       bool wrote0 = false;
-      for (int u = 0; u < p.nupd; ++u) wrote0 = wrote0 || p.upd[u].dst == 0;
+      for (int u = 0; u < p.nupd; ++u) wrote0 = wrote0 || p.upd[u].dst == 0 || p.upd[u].kahan;
       if (!wrote0 && started[S - 1]) {
         if (p.nupd >= MAX_STAGES) return fail(E2D_ERR_INVALID, "stage program overflow");
-        StageUpdate u;
+        StageUpdate u{};
         u.a = 0.0;
         u.src = row_buf(S - 1);
-        u.dst = 0;
+        u.dst = kahan ? row_buf(S - 1) : 0;
+        u.kahan = kahan;
         p.upd[p.nupd++] = u;  // dta = 0: exact copy for finite k
       }
     }
@@ -155,16 +184,152 @@ static int build_program(E2DSolver* h, int S, const double* a) {
   return 0;
 }
 
-static int ensure_buffers(E2DSolver* h) {
+template <typename T>
+static int ensure_buffers_t(E2DSolver* h) {
+  PathT<T>& p = path<T>(h);
   int need = h->nstages + 1;
   for (int b = h->nbuf; b < need; ++b) {
-    if (int e = h->alloc(&h->S.buf[b], 4 * (size_t)h->ncell)) return e;
-    if (b > 0) CK(cudaMemsetAsync(h->S.buf[b], 0, sizeof(double) * 4 * h->ncell, h->stream));
+    if (int e = h->alloc(&p.S.buf[b], 4 * (size_t)h->ncell)) return e;
+    if (b > 0) CK(cudaMemsetAsync(p.S.buf[b], 0, sizeof(T) * 4 * h->ncell, h->stream));
   }
   if (need > h->nbuf) h->nbuf = need;
   h->drop_graphs();
   return 0;
 }
+
+static int ensure_buffers(E2DSolver* h) { return E2D_DISPATCH(h, ensure_buffers_t); }
+
+// Geometry planes in the path's type: one allocation, planes back to back.  The FP32
+// path rounds the FP64 host planes once.
+template <typename T>
+static int upload_geometry(E2DSolver* h, const E2DGeometry* geo) {
+  PathT<T>& p = path<T>(h);
+  const int64_t ncell = h->ncell, nv = h->nvface, nh = h->nhface;
+  const size_t ngeo = (size_t)E2D_G_NCELL * ncell + (size_t)E2D_F_NFACE * (nv + nh);
+  if (int e = h->alloc(&p.geo, ngeo)) return e;
+  std::vector<T> tmp;
+  auto put = [&](T* dst, const double* src, int64_t n) -> int {
+    const void* from = src;
+    if (sizeof(T) != sizeof(double)) {
+      tmp.resize(n);
+      for (int64_t i = 0; i < n; ++i) tmp[i] = (T)src[i];
+      from = tmp.data();
+    }
+    CK(cudaMemcpy(dst, from, sizeof(T) * n, cudaMemcpyHostToDevice));
+    return 0;
+  };
+  T* q = p.geo;
+  for (int k = 0; k < E2D_G_NCELL; ++k, q += ncell) {
+    if (int e = put(q, geo->cell[k], ncell)) return e;
+    p.P.geo.cell[k] = q;
+  }
+  for (int k = 0; k < E2D_F_NFACE; ++k, q += nv) {
+    if (int e = put(q, geo->vface[k], nv)) return e;
+    p.P.geo.vface[k] = q;
+  }
+  for (int k = 0; k < E2D_F_NFACE; ++k, q += nh) {
+    if (int e = put(q, geo->hface[k], nh)) return e;
+    p.P.geo.hface[k] = q;
+  }
+  return 0;
+}
+
+// Face arrays, the Kahan compensation (FP32) and the scalar parameters of a path.
+template <typename T>
+static int init_path(E2DSolver* h) {
+  PathT<T>& p = path<T>(h);
+  const int64_t nv = h->nvface, nh = h->nhface;
+  if (int e = h->alloc(&p.F.vL, 4 * (size_t)nv)) return e;
+  if (int e = h->alloc(&p.F.vR, 4 * (size_t)nv)) return e;
+  if (int e = h->alloc(&p.F.vI, 4 * (size_t)nv)) return e;
+  if (int e = h->alloc(&p.F.hL, 4 * (size_t)nh)) return e;
+  if (int e = h->alloc(&p.F.hR, 4 * (size_t)nh)) return e;
+  if (int e = h->alloc(&p.F.hI, 4 * (size_t)nh)) return e;
+  p.S.comp = nullptr;
+  if (h->prec == E2D_FP32) {
+    if (int e = h->alloc(&p.S.comp, 4 * (size_t)h->ncell)) return e;
+    CK(cudaMemsetAsync(p.S.comp, 0, sizeof(T) * 4 * h->ncell, h->stream));
+  }
+  const E2DConfig* cfg = &h->cfg;
+  p.P.blocks = h->dblocks;
+  p.P.nblocks = cfg->nblocks;
+  p.P.ncell = h->ncell;
+  p.P.nvface = nv;
+  p.P.nhface = nh;
+  p.P.gamma = cfg->gamma;
+  p.P.gm1 = cfg->gm1;
+  p.P.gm = cfg->gamma / (cfg->gamma - 1.0);
+  p.P.k = 1.0 / (cfg->gamma - 1.0);
+  p.P.cfl = cfg->cfl;
+  p.P.flux = cfg->flux;
+  p.P.limiter = cfg->limiter;
+  p.P.recon = cfg->recon;
+  return 0;
+}
+
+template <typename T>
+static int bench_kernels_t(E2DHandle h, int32_t steps, double* ms, int64_t* launches) {
+  PathT<T>& p = path<T>(h);
+  const int ninst = (int)h->hinst.size();
+  for (auto& I : h->hinst) {
+    I.t_final = INFINITY;
+    I.max_steps = 0x7fffffff;
+    I.steps = 0;
+    I.halted = 0;
+    I.min_bits = 0x7ff0000000000000ULL;
+  }
+  CK(cudaMemcpyAsync(h->inst, h->hinst.data(), sizeof(InstanceState) * ninst, cudaMemcpyHostToDevice, h->stream));
+  k_reset_real<<<1, 1, 0, h->stream>>>(h->real);
+  const int per_step = 3 + 3 * h->nstages;
+  std::vector<cudaEvent_t> ev(2 * per_step * steps);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  std::vector<int> cls;
+  int k = 0;
+  auto rec = [&](int c) { cls.push_back(c); return cudaEventRecord(ev[k++], h->stream); };
+  auto fin = [&]() { return cudaEventRecord(ev[k++], h->stream); };
+  for (int st = 0; st < steps; ++st) {
+    CK(rec(0));
+    CK(launch_dt<T>(p.P, h->cell_tiles, h->ncell_tiles, p.S.buf[0], h->inst, h->stream));
+    CK(fin());
+    CK(rec(4));
+    CK(launch_begin_step(h->inst, ninst, p.P.cfl, 1, h->stream));
+    CK(fin());
+    for (int s = 0; s < h->nstages; ++s) {
+      const T* in = p.S.buf[h->stage_input[s]];
+      CK(rec(1));
+      CK(launch_reconstruct<T>(p.P, h->cell_tiles, h->ncell_tiles, in, h->inst, p.F, nullptr, h->stream));
+      CK(fin());
+      CK(rec(2));
+      CK(launch_flux<T>(p.P, h->face_tiles, h->nface_tiles, h->inst, p.F, nullptr, h->stream));
+      CK(fin());
+      CK(rec(3));
+      CK(launch_update<T>(p.P, h->cell_tiles, h->ncell_tiles, p.F, p.S, h->prog[s], h->inst, h->real, nullptr,
+                          h->stream));
+      CK(fin());
+    }
+    CK(rec(4));
+    CK(launch_end_step(h->inst, ninst, h->real, h->stream));
+    CK(fin());
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  double tot[E2D_BENCH_NK] = {0, 0, 0, 0, 0};
+  int64_t cnt[E2D_BENCH_NK] = {0, 0, 0, 0, 0};
+  for (size_t q = 0; q < cls.size(); ++q) {
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, ev[2 * q], ev[2 * q + 1]));
+    tot[cls[q]] += t;
+    cnt[cls[q]] += 1;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  for (int c = 0; c < E2D_BENCH_NK; ++c) {
+    ms[c] = cnt[c] ? tot[c] / cnt[c] : 0.0;
+    if (launches) launches[c] = cnt[c];
+  }
+  CK(cudaMemcpyAsync(h->hinst.data(), h->inst, sizeof(InstanceState) * ninst, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
 
 extern "C" {
 
@@ -175,7 +340,7 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
   if (!cfg || !blocks || !geo || !out) return fail(E2D_ERR_INVALID, "null argument");
   *out = nullptr;
   if (cfg->nblocks < 1) return fail(E2D_ERR_INVALID, "nblocks must be >= 1");
-  if (cfg->precision != E2D_FP64) return fail(E2D_ERR_UNSUPPORTED, "this entry point builds the FP64 path");
+  if (cfg->precision != E2D_FP64 && cfg->precision != E2D_FP32) return fail(E2D_ERR_INVALID, "unknown precision");
   if (cfg->flux < 0 || cfg->flux > 2 || cfg->limiter < 0 || cfg->limiter > 3 || cfg->recon < 0 || cfg->recon > 1)
     return fail(E2D_ERR_INVALID, "unknown flux/limiter/reconstruction code");
   const int ninst = cfg->ninstances > 0 ? cfg->ninstances : 1;
@@ -234,27 +399,9 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
   h->nhface = nh;
   h->hblocks.assign(blocks, blocks + cfg->nblocks);
 
-  // geometry planes: one allocation, planes back to back
-  const size_t ngeo = (size_t)E2D_G_NCELL * ncell + (size_t)E2D_F_NFACE * (nv + nh);
-  if (int e = h->alloc(&h->geo, ngeo)) return bail(e);
-  {
-    double* p = h->geo;
-    for (int k = 0; k < E2D_G_NCELL; ++k, p += ncell) {
-      if ((ce = cudaMemcpy(p, geo->cell[k], sizeof(double) * ncell, cudaMemcpyHostToDevice)) != cudaSuccess)
-        return bail(fail(E2D_ERR_CUDA, "geometry copy: %s", cudaGetErrorString(ce)));
-      h->P.geo.cell[k] = p;
-    }
-    for (int k = 0; k < E2D_F_NFACE; ++k, p += nv) {
-      if ((ce = cudaMemcpy(p, geo->vface[k], sizeof(double) * nv, cudaMemcpyHostToDevice)) != cudaSuccess)
-        return bail(fail(E2D_ERR_CUDA, "geometry copy: %s", cudaGetErrorString(ce)));
-      h->P.geo.vface[k] = p;
-    }
-    for (int k = 0; k < E2D_F_NFACE; ++k, p += nh) {
-      if ((ce = cudaMemcpy(p, geo->hface[k], sizeof(double) * nh, cudaMemcpyHostToDevice)) != cudaSuccess)
-        return bail(fail(E2D_ERR_CUDA, "geometry copy: %s", cudaGetErrorString(ce)));
-      h->P.geo.hface[k] = p;
-    }
-  }
+  h->prec = cfg->precision;
+  if (int e = (h->prec == E2D_FP32 ? upload_geometry<float>(h, geo) : upload_geometry<double>(h, geo)))
+    return bail(e);
   // block table with MIXED side coordinates moved to the device
   std::vector<E2DBlock> dev_blocks = h->hblocks;
   for (int b = 0; b < cfg->nblocks; ++b)
@@ -291,14 +438,6 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
       (ce = cudaMemcpy(h->face_tiles, ft.data(), sizeof(int4) * ft.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
     return bail(fail(E2D_ERR_CUDA, "tile copy: %s", cudaGetErrorString(ce)));
 
-  // face arrays
-  if (int e = h->alloc(&h->F.vL, 4 * (size_t)nv)) return bail(e);
-  if (int e = h->alloc(&h->F.vR, 4 * (size_t)nv)) return bail(e);
-  if (int e = h->alloc(&h->F.vI, 4 * (size_t)nv)) return bail(e);
-  if (int e = h->alloc(&h->F.hL, 4 * (size_t)nh)) return bail(e);
-  if (int e = h->alloc(&h->F.hR, 4 * (size_t)nh)) return bail(e);
-  if (int e = h->alloc(&h->F.hI, 4 * (size_t)nh)) return bail(e);
-
   // instance time state and realizability counters
   h->hinst.assign(ninst, InstanceState{});
   for (auto& I : h->hinst) {
@@ -312,19 +451,7 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
   if (int e = h->alloc(&h->real, 1)) return bail(e);
   k_reset_real<<<1, 1, 0, h->stream>>>(h->real);
 
-  h->P.blocks = h->dblocks;
-  h->P.nblocks = cfg->nblocks;
-  h->P.ncell = ncell;
-  h->P.nvface = nv;
-  h->P.nhface = nh;
-  h->P.gamma = cfg->gamma;
-  h->P.gm1 = cfg->gm1;
-  h->P.gm = cfg->gamma / (cfg->gamma - 1.0);
-  h->P.k = 1.0 / (cfg->gamma - 1.0);
-  h->P.cfl = cfg->cfl;
-  h->P.flux = cfg->flux;
-  h->P.limiter = cfg->limiter;
-  h->P.recon = cfg->recon;
+  if (int e = E2D_DISPATCH(h, init_path)) return bail(e);
 
   // default integrator: the classical RK4 rows (explicit_runge_kutta.py:212-224)
   const double rk4[16] = {0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1, 0, 1.0 / 6, 1.0 / 3, 1.0 / 3, 1.0 / 6};
@@ -354,27 +481,55 @@ int64_t e2d_num_cells(E2DHandle h) { return h ? h->ncell : -1; }
 
 int e2d_set_state(E2DHandle h, const double* host_soa) {
   if (!h || !host_soa) return fail(E2D_ERR_INVALID, "null argument");
-  CK(cudaMemcpyAsync(h->S.buf[0], host_soa, sizeof(double) * 4 * h->ncell, cudaMemcpyHostToDevice, h->stream));
+  const size_t n = 4 * (size_t)h->ncell;
+  if (h->prec == E2D_FP32) {
+    std::vector<float> tmp(n);
+    for (size_t i = 0; i < n; ++i) tmp[i] = (float)host_soa[i];
+    CK(cudaMemcpyAsync(h->pf.S.buf[0], tmp.data(), sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->pf.S.comp, 0, sizeof(float) * n, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+  }
+  CK(cudaMemcpyAsync(h->pd.S.buf[0], host_soa, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return 0;
 }
 
 int e2d_get_state(E2DHandle h, double* host_soa) {
   if (!h || !host_soa) return fail(E2D_ERR_INVALID, "null argument");
-  CK(cudaMemcpyAsync(host_soa, h->S.buf[0], sizeof(double) * 4 * h->ncell, cudaMemcpyDeviceToHost, h->stream));
+  const size_t n = 4 * (size_t)h->ncell;
+  if (h->prec == E2D_FP32) {
+    std::vector<float> tmp(n);
+    CK(cudaMemcpyAsync(tmp.data(), h->pf.S.buf[0], sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i < n; ++i) host_soa[i] = (double)tmp[i];
+    return 0;
+  }
+  CK(cudaMemcpyAsync(host_soa, h->pd.S.buf[0], sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return 0;
 }
 
 int e2d_set_state_device(E2DHandle h, const double* dev_soa) {
   if (!h || !dev_soa) return fail(E2D_ERR_INVALID, "null argument");
-  CK(cudaMemcpyAsync(h->S.buf[0], dev_soa, sizeof(double) * 4 * h->ncell, cudaMemcpyDeviceToDevice, h->stream));
+  const int64_t n = 4 * h->ncell;
+  if (h->prec == E2D_FP32) {
+    CK(launch_convert(dev_soa, h->pf.S.buf[0], n, h->stream));
+    CK(cudaMemsetAsync(h->pf.S.comp, 0, sizeof(float) * n, h->stream));
+    return 0;
+  }
+  CK(cudaMemcpyAsync(h->pd.S.buf[0], dev_soa, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
   return 0;
 }
 
 int e2d_get_state_device(E2DHandle h, double* dev_soa) {
   if (!h || !dev_soa) return fail(E2D_ERR_INVALID, "null argument");
-  CK(cudaMemcpyAsync(dev_soa, h->S.buf[0], sizeof(double) * 4 * h->ncell, cudaMemcpyDeviceToDevice, h->stream));
+  const int64_t n = 4 * h->ncell;
+  if (h->prec == E2D_FP32) {
+    CK(launch_convert(h->pf.S.buf[0], dev_soa, n, h->stream));
+    return 0;
+  }
+  CK(cudaMemcpyAsync(dev_soa, h->pd.S.buf[0], sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
   return 0;
 }
 
@@ -387,39 +542,64 @@ int e2d_set_tableau(E2DHandle h, int32_t nstages, const double* a) {
   return ensure_buffers(h);
 }
 
-static int enqueue_stages(E2DHandle h, double* dudt_out, const DebugOut* dbg) {
+}  // extern "C"
+
+template <typename T>
+static int enqueue_stages(E2DHandle h, T* dudt_out, const DebugOutT<T>* dbg) {
+  PathT<T>& p = path<T>(h);
   for (int s = 0; s < h->nstages; ++s) {
-    const double* in = h->S.buf[h->stage_input[s]];
-    CK(launch_reconstruct(h->P, h->cell_tiles, h->ncell_tiles, in, h->inst, h->F, dbg, h->stream));
-    CK(launch_flux(h->P, h->face_tiles, h->nface_tiles, h->inst, h->F, dbg, h->stream));
-    CK(launch_update(h->P, h->cell_tiles, h->ncell_tiles, h->F, h->S, h->prog[s], h->inst, h->real, dudt_out,
-                     h->stream));
+    const T* in = p.S.buf[h->stage_input[s]];
+    CK(launch_reconstruct<T>(p.P, h->cell_tiles, h->ncell_tiles, in, h->inst, p.F, dbg, h->stream));
+    CK(launch_flux<T>(p.P, h->face_tiles, h->nface_tiles, h->inst, p.F, dbg, h->stream));
+    CK(launch_update<T>(p.P, h->cell_tiles, h->ncell_tiles, p.F, p.S, h->prog[s], h->inst, h->real, dudt_out,
+                        h->stream));
   }
   return 0;
 }
 
-static int enqueue_run_step(E2DHandle h) {
+extern "C" {
+
+}  // extern "C"
+
+template <typename T>
+static int enqueue_run_step_t(E2DHandle h) {
+  PathT<T>& p = path<T>(h);
   const int ninst = (int)h->hinst.size();
-  CK(launch_dt(h->P, h->cell_tiles, h->ncell_tiles, h->S.buf[0], h->inst, h->stream));
-  CK(launch_begin_step(h->inst, ninst, h->P.cfl, 1, h->stream));
-  if (int e = enqueue_stages(h, nullptr, nullptr)) return e;
+  CK(launch_dt<T>(p.P, h->cell_tiles, h->ncell_tiles, p.S.buf[0], h->inst, h->stream));
+  CK(launch_begin_step(h->inst, ninst, p.P.cfl, 1, h->stream));
+  if (int e = enqueue_stages<T>(h, nullptr, nullptr)) return e;
   CK(launch_end_step(h->inst, ninst, h->real, h->stream));
   return 0;
 }
+
+extern "C" {
+
+static int enqueue_run_step(E2DHandle h) { return E2D_DISPATCH(h, enqueue_run_step_t); }
+
+}  // extern "C"
+
+template <typename T>
+static int launch_dt_path(E2DHandle h) {
+  PathT<T>& p = path<T>(h);
+  CK(launch_dt<T>(p.P, h->cell_tiles, h->ncell_tiles, p.S.buf[0], h->inst, h->stream));
+  return 0;
+}
+
+extern "C" {
 
 int e2d_compute_dt(E2DHandle h, double* dt_host) {
   if (!h || !dt_host) return fail(E2D_ERR_INVALID, "null argument");
   const int ninst = (int)h->hinst.size();
   k_reset_min<<<(ninst + 127) / 128, 128, 0, h->stream>>>(h->inst, ninst);
   CK(cudaGetLastError());
-  CK(launch_dt(h->P, h->cell_tiles, h->ncell_tiles, h->S.buf[0], h->inst, h->stream));
+  if (int e = E2D_DISPATCH(h, launch_dt_path)) return e;
   CK(cudaMemcpyAsync(h->hinst.data(), h->inst, sizeof(InstanceState) * ninst, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   for (int q = 0; q < ninst; ++q) {
     double m;
     unsigned long long b = h->hinst[q].min_bits;
     std::memcpy(&m, &b, sizeof m);
-    dt_host[q] = h->P.cfl * m;
+    dt_host[q] = h->cfg.cfl * m;
   }
   return 0;
 }
@@ -428,7 +608,9 @@ int e2d_step(E2DHandle h, double dt, double t) {
   if (!h) return fail(E2D_ERR_INVALID, "null handle");
   const int ninst = (int)h->hinst.size();
   CK(launch_set_time(h->inst, ninst, t, dt, h->stream));
-  if (int e = enqueue_stages(h, nullptr, nullptr)) return e;
+  if (int e = (h->prec == E2D_FP32 ? enqueue_stages<float>(h, nullptr, nullptr)
+                                   : enqueue_stages<double>(h, nullptr, nullptr)))
+    return e;
   CK(launch_end_step(h->inst, ninst, h->real, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return 0;
@@ -438,26 +620,40 @@ int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* d) {
   if (!h || !dudt_dev) return fail(E2D_ERR_INVALID, "null argument");
   const int ninst = (int)h->hinst.size();
   CK(launch_set_time(h->inst, ninst, t, 0.0, h->stream));
-  DebugOut dbg{};
-  const DebugOut* pd = nullptr;
-  if (d) {
-    dbg.gx = d->gx; dbg.gy = d->gy; dbg.phi = d->phi;
-    dbg.vflux_raw = d->vflux_raw; dbg.hflux_raw = d->hflux_raw;
-    dbg.vflux = d->vflux; dbg.hflux = d->hflux;
-    pd = &dbg;
-  }
   StageProgram none{};
   none.nupd = 0;
   none.final_stage = 0;
-  CK(launch_reconstruct(h->P, h->cell_tiles, h->ncell_tiles, h->S.buf[0], h->inst, h->F, pd, h->stream));
-  CK(launch_flux(h->P, h->face_tiles, h->nface_tiles, h->inst, h->F, pd, h->stream));
-  CK(launch_update(h->P, h->cell_tiles, h->ncell_tiles, h->F, h->S, none, h->inst, h->real, dudt_dev, h->stream));
-  if (d) {
-    const size_t bv = sizeof(double) * 4 * h->nvface, bh = sizeof(double) * 4 * h->nhface;
-    if (d->vL) CK(cudaMemcpyAsync(d->vL, h->F.vL, bv, cudaMemcpyDeviceToDevice, h->stream));
-    if (d->vR) CK(cudaMemcpyAsync(d->vR, h->F.vR, bv, cudaMemcpyDeviceToDevice, h->stream));
-    if (d->hL) CK(cudaMemcpyAsync(d->hL, h->F.hL, bh, cudaMemcpyDeviceToDevice, h->stream));
-    if (d->hR) CK(cudaMemcpyAsync(d->hR, h->F.hR, bh, cudaMemcpyDeviceToDevice, h->stream));
+  if (h->prec == E2D_FP32) {
+    if (d) return fail(E2D_ERR_UNSUPPORTED, "per-operator intermediates are produced by the FP64 path only");
+    PathT<float>& p = h->pf;
+    if (!p.dudt_tmp)
+      if (int e = h->alloc(&p.dudt_tmp, 4 * (size_t)h->ncell)) return e;
+    CK(launch_reconstruct<float>(p.P, h->cell_tiles, h->ncell_tiles, p.S.buf[0], h->inst, p.F, nullptr, h->stream));
+    CK(launch_flux<float>(p.P, h->face_tiles, h->nface_tiles, h->inst, p.F, nullptr, h->stream));
+    CK(launch_update<float>(p.P, h->cell_tiles, h->ncell_tiles, p.F, p.S, none, h->inst, h->real, p.dudt_tmp,
+                            h->stream));
+    CK(launch_convert(p.dudt_tmp, dudt_dev, 4 * h->ncell, h->stream));
+  } else {
+    PathT<double>& p = h->pd;
+    DebugOut dbg{};
+    const DebugOut* pdb = nullptr;
+    if (d) {
+      dbg.gx = d->gx; dbg.gy = d->gy; dbg.phi = d->phi;
+      dbg.vflux_raw = d->vflux_raw; dbg.hflux_raw = d->hflux_raw;
+      dbg.vflux = d->vflux; dbg.hflux = d->hflux;
+      pdb = &dbg;
+    }
+    CK(launch_reconstruct<double>(p.P, h->cell_tiles, h->ncell_tiles, p.S.buf[0], h->inst, p.F, pdb, h->stream));
+    CK(launch_flux<double>(p.P, h->face_tiles, h->nface_tiles, h->inst, p.F, pdb, h->stream));
+    CK(launch_update<double>(p.P, h->cell_tiles, h->ncell_tiles, p.F, p.S, none, h->inst, h->real, dudt_dev,
+                             h->stream));
+    if (d) {
+      const size_t bv = sizeof(double) * 4 * h->nvface, bh = sizeof(double) * 4 * h->nhface;
+      if (d->vL) CK(cudaMemcpyAsync(d->vL, p.F.vL, bv, cudaMemcpyDeviceToDevice, h->stream));
+      if (d->vR) CK(cudaMemcpyAsync(d->vR, p.F.vR, bv, cudaMemcpyDeviceToDevice, h->stream));
+      if (d->hL) CK(cudaMemcpyAsync(d->hL, p.F.hL, bh, cudaMemcpyDeviceToDevice, h->stream));
+      if (d->hR) CK(cudaMemcpyAsync(d->hR, p.F.hR, bh, cudaMemcpyDeviceToDevice, h->stream));
+    }
   }
   CK(launch_end_step(h->inst, ninst, h->real, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -468,7 +664,10 @@ int e2d_check_realizable(E2DHandle h, E2DRealizability* out) {
   if (!h || !out) return fail(E2D_ERR_INVALID, "null argument");
   k_reset_real<<<1, 1, 0, h->stream>>>(h->real);
   CK(cudaGetLastError());
-  CK(launch_realizable(h->P, h->cell_tiles, h->ncell_tiles, h->S.buf[0], h->real, h->stream));
+  if (h->prec == E2D_FP32)
+    CK(launch_realizable<float>(h->pf.P, h->cell_tiles, h->ncell_tiles, h->pf.S.buf[0], h->real, h->stream));
+  else
+    CK(launch_realizable<double>(h->pd.P, h->cell_tiles, h->ncell_tiles, h->pd.S.buf[0], h->real, h->stream));
   RealizState r;
   CK(cudaMemcpyAsync(&r, h->real, sizeof r, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -556,64 +755,7 @@ int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps, int
 // Per-kernel CUDA-event timing of `steps` device-loop steps (euler2d_bench.h).
 int e2d_bench_kernels(E2DHandle h, int32_t steps, double* ms, int64_t* launches) {
   if (!h || !ms || steps < 1) return fail(E2D_ERR_INVALID, "bad argument");
-  const int ninst = (int)h->hinst.size();
-  for (auto& I : h->hinst) {
-    I.t_final = INFINITY;
-    I.max_steps = 0x7fffffff;
-    I.steps = 0;
-    I.halted = 0;
-    I.min_bits = 0x7ff0000000000000ULL;
-  }
-  CK(cudaMemcpyAsync(h->inst, h->hinst.data(), sizeof(InstanceState) * ninst, cudaMemcpyHostToDevice, h->stream));
-  k_reset_real<<<1, 1, 0, h->stream>>>(h->real);
-  const int per_step = 3 + 3 * h->nstages;
-  std::vector<cudaEvent_t> ev(2 * per_step * steps);
-  for (auto& e : ev) CK(cudaEventCreate(&e));
-  std::vector<int> cls;
-  int k = 0;
-  auto rec = [&](int c) { cls.push_back(c); return cudaEventRecord(ev[k++], h->stream); };
-  auto fin = [&]() { return cudaEventRecord(ev[k++], h->stream); };
-  for (int st = 0; st < steps; ++st) {
-    CK(rec(0));
-    CK(launch_dt(h->P, h->cell_tiles, h->ncell_tiles, h->S.buf[0], h->inst, h->stream));
-    CK(fin());
-    CK(rec(4));
-    CK(launch_begin_step(h->inst, ninst, h->P.cfl, 1, h->stream));
-    CK(fin());
-    for (int s = 0; s < h->nstages; ++s) {
-      const double* in = h->S.buf[h->stage_input[s]];
-      CK(rec(1));
-      CK(launch_reconstruct(h->P, h->cell_tiles, h->ncell_tiles, in, h->inst, h->F, nullptr, h->stream));
-      CK(fin());
-      CK(rec(2));
-      CK(launch_flux(h->P, h->face_tiles, h->nface_tiles, h->inst, h->F, nullptr, h->stream));
-      CK(fin());
-      CK(rec(3));
-      CK(launch_update(h->P, h->cell_tiles, h->ncell_tiles, h->F, h->S, h->prog[s], h->inst, h->real, nullptr,
-                       h->stream));
-      CK(fin());
-    }
-    CK(rec(4));
-    CK(launch_end_step(h->inst, ninst, h->real, h->stream));
-    CK(fin());
-  }
-  CK(cudaStreamSynchronize(h->stream));
-  double tot[E2D_BENCH_NK] = {0, 0, 0, 0, 0};
-  int64_t cnt[E2D_BENCH_NK] = {0, 0, 0, 0, 0};
-  for (size_t q = 0; q < cls.size(); ++q) {
-    float t = 0.f;
-    CK(cudaEventElapsedTime(&t, ev[2 * q], ev[2 * q + 1]));
-    tot[cls[q]] += t;
-    cnt[cls[q]] += 1;
-  }
-  for (auto& e : ev) cudaEventDestroy(e);
-  for (int c = 0; c < E2D_BENCH_NK; ++c) {
-    ms[c] = cnt[c] ? tot[c] / cnt[c] : 0.0;
-    if (launches) launches[c] = cnt[c];
-  }
-  CK(cudaMemcpyAsync(h->hinst.data(), h->inst, sizeof(InstanceState) * ninst, cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaStreamSynchronize(h->stream));
-  return 0;
+  return E2D_DISPATCH(h, bench_kernels_t, steps, ms, launches);
 }
 
 }  // extern "C"

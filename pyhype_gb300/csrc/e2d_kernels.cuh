@@ -1,5 +1,5 @@
 // e2d_kernels.cuh - launch interface between the C ABI (e2d_api.cu) and the stage
-// kernels (e2d_fp64.cu).  Internal to the library.
+// kernels (e2d_stage.cuh, instantiated by e2d_fp64.cu and e2d_fp32.cu).  Internal.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -12,31 +12,34 @@ constexpr int TX = 32;        // cell tile width  (one warp along x)
 constexpr int TY = 8;         // cell tile height
 constexpr int MAX_STAGES = 8;
 
-// Device view of the geometry planes.
-struct DevGeometry {
-  const double* cell[E2D_G_NCELL];
-  const double* vface[E2D_F_NFACE];
-  const double* hface[E2D_F_NFACE];
+// Device view of the geometry planes (in the arithmetic type of the path).
+template <typename T>
+struct DevGeometryT {
+  const T* cell[E2D_G_NCELL];
+  const T* vface[E2D_F_NFACE];
+  const T* hface[E2D_F_NFACE];
 };
 
 // Face-indexed left/right states (primitive, rotated into the face frame) and the
 // integrated face fluxes L*(2F), 4 planes each.
-struct FaceArrays {
-  double* vL;
-  double* vR;
-  double* hL;
-  double* hR;
-  double* vI;
-  double* hI;
+template <typename T>
+struct FaceArraysT {
+  T* vL;
+  T* vR;
+  T* hL;
+  T* hR;
+  T* vI;
+  T* hI;
 };
 
 // Per-instance time state, device resident so a whole step can be replayed from a
-// CUDA graph.  One instance for a plain solver; one per problem in a batch.
+// CUDA graph.  One instance for a plain solver; one per problem in a batch.  Time,
+// dt and the CFL minimum are FP64 on every path.
 struct InstanceState {
   double t;            // solver (non-dimensional) time at the start of the step
   double dt;           // current step
   double t_final;
-  unsigned long long min_bits;  // min over cells of min(tx, ty) as IEEE bits (>= 0)
+  unsigned long long min_bits;  // min over cells of min(tx, ty) as FP64 IEEE bits (>= 0)
   int32_t active;      // 1 while this instance still steps
   int32_t steps;       // steps taken
   int32_t max_steps;
@@ -48,20 +51,26 @@ struct RealizState {
   unsigned long long nbad;
 };
 
-struct Params {
+template <typename T>
+struct ParamsT {
   const E2DBlock* blocks;   // device copy, side_coord patched to device pointers
   int nblocks;
   int64_t ncell, nvface, nhface;
-  DevGeometry geo;
+  DevGeometryT<T> geo;
   double gamma, gm1, gm, k, cfl;
   int flux, limiter, recon;
 };
 
 // One update of the RK stage program: dst = src + (dt * a) * k (buffers by id).
+// src_zero: the partial sum starts here (src value 0, used for increments).
+// kahan: the result is an increment added into buffer 0 with compensated (Kahan)
+// summation; dst is unused.
 struct StageUpdate {
   int dst;
   int src;
   double a;
+  int src_zero;
+  int kahan;
 };
 struct StageProgram {
   int nupd;
@@ -69,35 +78,52 @@ struct StageProgram {
   int final_stage;   // 1 on the last stage (realizability + step bookkeeping)
 };
 
-struct StateBuffers {
-  double* buf[MAX_STAGES + 1];   // 0 = U^n, 1.. = row partial sums
+template <typename T>
+struct StateBuffersT {
+  T* buf[MAX_STAGES + 1];   // 0 = U^n, 1.. = row partial sums
+  T* comp;                  // Kahan compensation of U^n (FP32 path), else null
 };
 
-struct DebugOut {
-  double* gx;
-  double* gy;
-  double* phi;
-  double* vflux_raw;
-  double* hflux_raw;
-  double* vflux;
-  double* hflux;
+template <typename T>
+struct DebugOutT {
+  T* gx;
+  T* gy;
+  T* phi;
+  T* vflux_raw;
+  T* hflux_raw;
+  T* vflux;
+  T* hflux;
 };
 
-// launchers (e2d_fp64.cu)
-cudaError_t launch_reconstruct(const Params& P, const int4* cell_tiles, int ntiles, const double* U,
-                               const InstanceState* inst, FaceArrays F, const DebugOut* dbg,
+using DevGeometry = DevGeometryT<double>;
+using FaceArrays = FaceArraysT<double>;
+using Params = ParamsT<double>;
+using StateBuffers = StateBuffersT<double>;
+using DebugOut = DebugOutT<double>;
+
+// launchers, instantiated for double (e2d_fp64.cu) and float (e2d_fp32.cu)
+template <typename T>
+cudaError_t launch_reconstruct(const ParamsT<T>& P, const int4* cell_tiles, int ntiles, const T* U,
+                               const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>* dbg,
                                cudaStream_t st);
-cudaError_t launch_flux(const Params& P, const int4* face_tiles, int ntiles, const InstanceState* inst,
-                        FaceArrays F, const DebugOut* dbg, cudaStream_t st);
-cudaError_t launch_update(const Params& P, const int4* cell_tiles, int ntiles, FaceArrays F,
-                          StateBuffers S, const StageProgram& prog, InstanceState* inst,
-                          RealizState* real, double* dudt_out, cudaStream_t st);
-cudaError_t launch_dt(const Params& P, const int4* cell_tiles, int ntiles, const double* U,
+template <typename T>
+cudaError_t launch_flux(const ParamsT<T>& P, const int4* face_tiles, int ntiles, const InstanceState* inst,
+                        FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st);
+template <typename T>
+cudaError_t launch_update(const ParamsT<T>& P, const int4* cell_tiles, int ntiles, FaceArraysT<T> F,
+                          StateBuffersT<T> S, const StageProgram& prog, InstanceState* inst,
+                          RealizState* real, T* dudt_out, cudaStream_t st);
+template <typename T>
+cudaError_t launch_dt(const ParamsT<T>& P, const int4* cell_tiles, int ntiles, const T* U,
                       InstanceState* inst, cudaStream_t st);
+template <typename T>
+cudaError_t launch_realizable(const ParamsT<T>& P, const int4* cell_tiles, int ntiles, const T* U,
+                              RealizState* real, cudaStream_t st);
 cudaError_t launch_begin_step(InstanceState* inst, int ninst, double cfl, int use_min, cudaStream_t st);
 cudaError_t launch_end_step(InstanceState* inst, int ninst, const RealizState* real, cudaStream_t st);
 cudaError_t launch_set_time(InstanceState* inst, int ninst, double t, double dt, cudaStream_t st);
-cudaError_t launch_realizable(const Params& P, const int4* cell_tiles, int ntiles, const double* U,
-                              RealizState* real, cudaStream_t st);
+// precision conversions between caller FP64 buffers and an FP32 state
+cudaError_t launch_convert(const double* src, float* dst, int64_t n, cudaStream_t st);
+cudaError_t launch_convert(const float* src, double* dst, int64_t n, cudaStream_t st);
 
 }  // namespace e2d

@@ -1,0 +1,572 @@
+// e2d_stage.cuh - the stage kernels of the 2D Euler MUSCL scheme, templated on the
+// arithmetic type.  Included by e2d_fp64.cu (T = double, -fmad=false: the
+// bit-exact path) and e2d_fp32.cu (T = float, contraction allowed, Kahan-compensated
+// step accumulation).
+//
+// One RK stage is three launches over every block of the problem at once (a tile
+// table maps CTAs to (block, tile) pairs):
+//
+//   k_reconstruct  per cell: reconstruction-type state of the cell and its four
+//                  neighbours (ghost cells formed on the fly at block edges), interface
+//                  averages, Green-Gauss gradient, limiter, limited face states; each
+//                  face state is rotated into its face frame, converted to primitive
+//                  and written to the face-indexed L/R arrays, block-boundary cells
+//                  also write the outside state of their boundary face.
+//   k_flux         per face, exactly once: Riemann flux of (L, R), rotated back,
+//                  times 2*L (one-point rule, weight 2).
+//   k_update       per cell: dUdt = 0.5*(((I_W - I_E) + I_S) - I_N)/A and the RK stage
+//                  program (every partial Butcher sum this stage contributes to);
+//                  on the last stage also the positivity check.
+//
+// GB300's FP64 pipe is the binding resource of this scheme in FP64 (about 1000 FP64
+// pipe operations per cell-stage against ~250 bytes of HBM traffic), so the split
+// avoids every recomputation a fused halo-tile kernel would do (gradients and
+// limiter of the halo ring, fluxes of tile-edge faces); the extra face-array traffic
+// costs HBM bandwidth that is otherwise idle.
+#pragma once
+#include <cstdio>
+
+#include "e2d_device.cuh"
+#include "e2d_kernels.cuh"
+
+namespace e2d {
+
+
+__device__ __forceinline__ int64_t cell_at(const E2DBlock* B, int i, int j) {
+  return B->cell_offset + (int64_t)i * B->nx + j;
+}
+__device__ __forceinline__ int64_t vf_at(const E2DBlock* B, int i, int j) {
+  return B->vface_offset + (int64_t)i * (B->nx + 1) + j;
+}
+__device__ __forceinline__ int64_t hf_at(const E2DBlock* B, int i, int j) {
+  return B->hface_offset + (int64_t)i * B->nx + j;
+}
+
+// Side kind at position k along a side, resolving MIXED sides; gd/fd point at the
+// Dirichlet ghost (conservative) and face (reconstruction variables) vectors.
+__device__ __forceinline__ int side_kind_at(const E2DBlock* B, int side, int k, double t,
+                                            const double*& gd, const double*& fd) {
+  int kind = B->side_kind[side];
+  gd = B->dirichlet_ghost[side];
+  fd = B->dirichlet_face[side];
+  if (kind == E2D_SIDE_MIXED) {
+    const E2DMixedSide* m = &B->mixed[side];
+    double coord = B->side_coord[side][k];
+    if (coord < m->x0 + m->speed * t) {
+      kind = m->kind_below; gd = m->ghost_below; fd = m->face_below;
+    } else {
+      kind = m->kind_above; gd = m->ghost_above; fd = m->face_above;
+    }
+  }
+  return kind;
+}
+
+template <typename T>
+__device__ __forceinline__ void boundary_cs(const ParamsT<T>& P, const E2DBlock* B, int side, int k, T& c, T& s) {
+  int64_t f;
+  if (side == E2D_E) { f = vf_at(B, k, B->nx); c = P.geo.vface[E2D_F_COS][f]; s = P.geo.vface[E2D_F_SIN][f]; }
+  else if (side == E2D_W) { f = vf_at(B, k, 0); c = P.geo.vface[E2D_F_COS][f]; s = P.geo.vface[E2D_F_SIN][f]; }
+  else if (side == E2D_N) { f = hf_at(B, B->ny, k); c = P.geo.hface[E2D_F_COS][f]; s = P.geo.hface[E2D_F_SIN][f]; }
+  else { f = hf_at(B, 0, k); c = P.geo.hface[E2D_F_COS][f]; s = P.geo.hface[E2D_F_SIN][f]; }
+}
+
+template <typename T>
+__device__ __forceinline__ void load_cell(const T* __restrict__ U, int64_t ncell, int64_t c, T* q) {
+  q[0] = U[c];
+  q[1] = U[ncell + c];
+  q[2] = U[2 * ncell + c];
+  q[3] = U[3 * ncell + c];
+}
+
+// Ghost cell (conservative variables) at position k along a side: neighbour cell,
+// own boundary cell (copy / outlet), its reflection, or a Dirichlet state
+// (pyhype/blocks/ghost.py:149-158,187-216).
+template <typename T>
+__device__ void ghost_cons(const ParamsT<T>& P, const E2DBlock* B, int side, int k, const T* __restrict__ U,
+                           double t, T* g) {
+  const double *gd, *fd;
+  int kind = side_kind_at(B, side, k, t, gd, fd);
+  if (kind == E2D_SIDE_NEIGHBOR) {
+    const E2DBlock* N = P.blocks + B->neighbor[side];
+    int64_t c;
+    if (side == E2D_E) c = cell_at(N, k, 0);
+    else if (side == E2D_W) c = cell_at(N, k, N->nx - 1);
+    else if (side == E2D_N) c = cell_at(N, 0, k);
+    else c = cell_at(N, N->ny - 1, k);
+    load_cell(U, P.ncell, c, g);
+    return;
+  }
+  if (kind == E2D_SIDE_DIRICHLET) {
+    g[0] = T(gd[0]); g[1] = T(gd[1]); g[2] = T(gd[2]); g[3] = T(gd[3]);
+    return;
+  }
+  int64_t c;
+  if (side == E2D_E) c = cell_at(B, k, B->nx - 1);
+  else if (side == E2D_W) c = cell_at(B, k, 0);
+  else if (side == E2D_N) c = cell_at(B, B->ny - 1, k);
+  else c = cell_at(B, 0, k);
+  load_cell(U, P.ncell, c, g);
+  if (kind == E2D_SIDE_REFLECT) {
+    T cs, sn;
+    boundary_cs(P, B, side, k, cs, sn);
+    reflect(g, cs, sn);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void store4(T* __restrict__ base, int64_t stride, int64_t f, const T* q) {
+  base[f] = q[0];
+  base[stride + f] = q[1];
+  base[2 * stride + f] = q[2];
+  base[3 * stride + f] = q[3];
+}
+
+// Outside state (reconstruction variables) of the boundary face at position k of
+// side `side`: ghost average for inter-block/copy sides, else the block's own
+// limited face state with the side's BC applied (pyhype/fvm/base.py:305-325 and the
+// apply_boundary_condition_to_state calls of fvm/base.py:353-363,419-429).
+template <typename T>
+__device__ __forceinline__ void outside_state(const ParamsT<T>& P, const E2DBlock* B, int side, int k, double t,
+                                              const T* ghost_recon, const T* own_face, T* o) {
+  const double *gd, *fd;
+  int kind = side_kind_at(B, side, k, t, gd, fd);
+  if (kind == E2D_SIDE_NEIGHBOR || kind == E2D_SIDE_COPY) {
+    o[0] = ghost_recon[0]; o[1] = ghost_recon[1]; o[2] = ghost_recon[2]; o[3] = ghost_recon[3];
+  } else if (kind == E2D_SIDE_DIRICHLET) {
+    o[0] = T(fd[0]); o[1] = T(fd[1]); o[2] = T(fd[2]); o[3] = T(fd[3]);
+  } else {
+    o[0] = own_face[0]; o[1] = own_face[1]; o[2] = own_face[2]; o[3] = own_face[3];
+    if (kind == E2D_SIDE_REFLECT) {
+      T c, s;
+      boundary_cs(P, B, side, k, c, s);
+      reflect(o, c, s);
+    }
+  }
+}
+
+// --------------------------------------------------------------------------------------
+// K1: reconstruction
+// --------------------------------------------------------------------------------------
+template <typename T, int LIM, int RECON, bool DBG>
+__global__ void __launch_bounds__(TX * TY) k_reconstruct(ParamsT<T> P, const int4* __restrict__ tiles,
+                                                         const T* __restrict__ U,
+                                                         const InstanceState* __restrict__ inst,
+                                                         FaceArraysT<T> F, DebugOutT<T> dbg) {
+  const int4 tl = tiles[blockIdx.x];
+  const E2DBlock* B = P.blocks + tl.x;
+  const InstanceState* I = inst + B->instance;
+  if (!I->active) return;
+  const double t = I->t;
+  const int nx = B->nx, ny = B->ny;
+  const int i0 = tl.y, j0 = tl.z;
+  const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
+
+  __shared__ T sW[4][TY + 2][TX + 2];
+  for (int p = threadIdx.x; p < (TY + 2) * (TX + 2); p += TX * TY) {
+    const int ly = p / (TX + 2), lx = p - ly * (TX + 2);
+    const int gi = i0 + ly - 1, gj = j0 + lx - 1;
+    const bool in_i = gi >= 0 && gi < ny, in_j = gj >= 0 && gj < nx;
+    T q[4], r[4] = {T(0), T(0), T(0), T(0)};
+    bool ok = true;
+    if (in_i && in_j) load_cell(U, P.ncell, cell_at(B, gi, gj), q);
+    else if (in_i && gj == -1) ghost_cons(P, B, E2D_W, gi, U, t, q);
+    else if (in_i && gj == nx) ghost_cons(P, B, E2D_E, gi, U, t, q);
+    else if (in_j && gi == -1) ghost_cons(P, B, E2D_S, gj, U, t, q);
+    else if (in_j && gi == ny) ghost_cons(P, B, E2D_N, gj, U, t, q);
+    else ok = false;
+    if (ok) to_recon<RECON>(q, G, r);
+    sW[0][ly][lx] = r[0];
+    sW[1][ly][lx] = r[1];
+    sW[2][ly][lx] = r[2];
+    sW[3][ly][lx] = r[3];
+  }
+  __syncthreads();
+
+  const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
+  const int i = i0 + ty, j = j0 + tx;
+  if (i >= ny || j >= nx) return;
+  const int64_t c = cell_at(B, i, j);
+  const int64_t fE = vf_at(B, i, j + 1), fW = vf_at(B, i, j);
+  const int64_t fN = hf_at(B, i + 1, j), fS = hf_at(B, i, j);
+  const T LcE = P.geo.vface[E2D_F_LC][fE], LsE = P.geo.vface[E2D_F_LS][fE];
+  const T LcW = P.geo.vface[E2D_F_LC][fW], LsW = P.geo.vface[E2D_F_LS][fW];
+  const T LcN = P.geo.hface[E2D_F_LC][fN], LsN = P.geo.hface[E2D_F_LS][fN];
+  const T LcS = P.geo.hface[E2D_F_LC][fS], LsS = P.geo.hface[E2D_F_LS][fS];
+  const T ia = P.geo.cell[E2D_G_INV_A][c];
+  T hx[4], hy[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    hx[s] = P.geo.cell[E2D_G_HX_E + s][c];
+    hy[s] = P.geo.cell[E2D_G_HY_E + s][c];
+  }
+
+  T face[4][4];  // [side][var] limited face states, reconstruction variables
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    const T w0 = sW[v][ty + 1][tx + 1];
+    const T we = sW[v][ty + 1][tx];
+    const T ea = sW[v][ty + 1][tx + 2];
+    const T so = sW[v][ty][tx + 1];
+    const T no = sW[v][ty + 2][tx + 1];
+    // interface averages (quad_block.py:181-218) and Green-Gauss (greengauss.py:137-155)
+    const T ie = T(0.5) * (w0 + ea), iw = T(0.5) * (we + w0);
+    const T in = T(0.5) * (w0 + no), is = T(0.5) * (so + w0);
+    const T gx = (ie * LcE + iw * (-LcW) + in * LcN + is * (-LcS)) * ia;
+    const T gy = (ie * LsE + iw * (-LsW) + in * LsN + is * (-LsS)) * ia;
+    // limiter (limiters/base.py:47-221)
+    const T dmax = vmax(vmax(vmax(vmax(w0, we), ea), so), no) - w0;
+    const T dmin = vmin(vmin(vmin(vmin(w0, we), ea), so), no) - w0;
+    T hot[4];
+    T ph = T(0);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      hot[s] = gx * hx[s] + gy * hy[s];
+      const T davg = (w0 + hot[s]) - w0;
+      // slope dmax/davg (davg > 0), dmin/davg (davg < 0), 1 (davg == 0), with a single
+      // division so lanes of different signs share one division sequence
+      const bool pos = is_pos(davg), neg = is_neg(davg);
+      const T q = (pos ? dmax : dmin) / ((pos || neg) ? davg : T(1));
+      const T sl = (pos || neg) ? q : T(1);
+      const T p = psi<LIM>(sl);
+      ph = (s == 0) ? p : vmin(ph, p);
+    }
+    ph = is_neg(ph) ? T(0) : ph;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) face[s][v] = w0 + ph * hot[s];
+    if (DBG) {
+      if (dbg.gx) dbg.gx[v * P.ncell + c] = gx;
+      if (dbg.gy) dbg.gy[v * P.ncell + c] = gy;
+      if (dbg.phi) dbg.phi[v * P.ncell + c] = ph;
+    }
+  }
+
+  const bool cart = B->is_cartesian != 0;
+  // east face of this cell = left state of vertical face j+1
+  {
+    T q[4] = {face[E2D_E][0], face[E2D_E][1], face[E2D_E][2], face[E2D_E][3]}, w[4];
+    if (!cart) rotate(q, P.geo.vface[E2D_F_COS][fE], P.geo.vface[E2D_F_SIN][fE]);
+    recon_to_prim<RECON>(q, G, w);
+    store4(F.vL, P.nvface, fE, w);
+  }
+  // west face = right state of vertical face j
+  {
+    T q[4] = {face[E2D_W][0], face[E2D_W][1], face[E2D_W][2], face[E2D_W][3]}, w[4];
+    if (!cart) rotate(q, P.geo.vface[E2D_F_COS][fW], P.geo.vface[E2D_F_SIN][fW]);
+    recon_to_prim<RECON>(q, G, w);
+    store4(F.vR, P.nvface, fW, w);
+  }
+  // north face = left state of horizontal face i+1 (y sweep in the x frame)
+  {
+    T q[4] = {face[E2D_N][0], face[E2D_N][1], face[E2D_N][2], face[E2D_N][3]}, w[4];
+    if (cart) rotate90(q);
+    else rotate(q, P.geo.hface[E2D_F_COS][fN], P.geo.hface[E2D_F_SIN][fN]);
+    recon_to_prim<RECON>(q, G, w);
+    store4(F.hL, P.nhface, fN, w);
+  }
+  // south face = right state of horizontal face i
+  {
+    T q[4] = {face[E2D_S][0], face[E2D_S][1], face[E2D_S][2], face[E2D_S][3]}, w[4];
+    if (cart) rotate90(q);
+    else rotate(q, P.geo.hface[E2D_F_COS][fS], P.geo.hface[E2D_F_SIN][fS]);
+    recon_to_prim<RECON>(q, G, w);
+    store4(F.hR, P.nhface, fS, w);
+  }
+  // outside states of block-boundary faces
+  if (j == 0) {
+    const T gr[4] = {sW[0][ty + 1][tx], sW[1][ty + 1][tx], sW[2][ty + 1][tx], sW[3][ty + 1][tx]};
+    T o[4], w[4];
+    outside_state(P, B, E2D_W, i, t, gr, face[E2D_W], o);
+    if (!cart) rotate(o, P.geo.vface[E2D_F_COS][fW], P.geo.vface[E2D_F_SIN][fW]);
+    recon_to_prim<RECON>(o, G, w);
+    store4(F.vL, P.nvface, fW, w);
+  }
+  if (j == nx - 1) {
+    const T gr[4] = {sW[0][ty + 1][tx + 2], sW[1][ty + 1][tx + 2], sW[2][ty + 1][tx + 2], sW[3][ty + 1][tx + 2]};
+    T o[4], w[4];
+    outside_state(P, B, E2D_E, i, t, gr, face[E2D_E], o);
+    if (!cart) rotate(o, P.geo.vface[E2D_F_COS][fE], P.geo.vface[E2D_F_SIN][fE]);
+    recon_to_prim<RECON>(o, G, w);
+    store4(F.vR, P.nvface, fE, w);
+  }
+  if (i == 0) {
+    const T gr[4] = {sW[0][ty][tx + 1], sW[1][ty][tx + 1], sW[2][ty][tx + 1], sW[3][ty][tx + 1]};
+    T o[4], w[4];
+    outside_state(P, B, E2D_S, j, t, gr, face[E2D_S], o);
+    if (cart) rotate90(o);
+    else rotate(o, P.geo.hface[E2D_F_COS][fS], P.geo.hface[E2D_F_SIN][fS]);
+    recon_to_prim<RECON>(o, G, w);
+    store4(F.hL, P.nhface, fS, w);
+  }
+  if (i == ny - 1) {
+    const T gr[4] = {sW[0][ty + 2][tx + 1], sW[1][ty + 2][tx + 1], sW[2][ty + 2][tx + 1], sW[3][ty + 2][tx + 1]};
+    T o[4], w[4];
+    outside_state(P, B, E2D_N, j, t, gr, face[E2D_N], o);
+    if (cart) rotate90(o);
+    else rotate(o, P.geo.hface[E2D_F_COS][fN], P.geo.hface[E2D_F_SIN][fN]);
+    recon_to_prim<RECON>(o, G, w);
+    store4(F.hR, P.nhface, fN, w);
+  }
+}
+
+// --------------------------------------------------------------------------------------
+// K2: one Riemann flux per face
+// --------------------------------------------------------------------------------------
+template <typename T, int FLUX, bool DBG>
+__global__ void __launch_bounds__(TX * TY) k_flux(ParamsT<T> P, const int4* __restrict__ tiles,
+                                                  const InstanceState* __restrict__ inst, FaceArraysT<T> F,
+                                                  DebugOutT<T> dbg) {
+  const int4 tl = tiles[blockIdx.x];
+  const E2DBlock* B = P.blocks + tl.x;
+  if (!inst[B->instance].active) return;
+  const int nx = B->nx, ny = B->ny;
+  const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
+  const int i = tl.y + ty, j = tl.z + tx;
+  if (i > ny || j > nx) return;
+  const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
+  const bool cart = B->is_cartesian != 0;
+  if (i < ny) {
+    const int64_t f = vf_at(B, i, j);
+    T L[4] = {F.vL[f], F.vL[P.nvface + f], F.vL[2 * P.nvface + f], F.vL[3 * P.nvface + f]};
+    T R[4] = {F.vR[f], F.vR[P.nvface + f], F.vR[2 * P.nvface + f], F.vR[3 * P.nvface + f]};
+    T Fx[4];
+    riemann<FLUX>(L, R, G, Fx);
+    if (DBG && dbg.vflux_raw) store4(dbg.vflux_raw, P.nvface, f, Fx);
+    if (!cart) unrotate(Fx, P.geo.vface[E2D_F_COS][f], P.geo.vface[E2D_F_SIN][f]);
+    if (DBG && dbg.vflux) store4(dbg.vflux, P.nvface, f, Fx);
+    const T len = P.geo.vface[E2D_F_L][f];
+    T I[4] = {len * (T(2) * Fx[0]), len * (T(2) * Fx[1]), len * (T(2) * Fx[2]), len * (T(2) * Fx[3])};
+    store4(F.vI, P.nvface, f, I);
+  }
+  if (j < nx) {
+    const int64_t f = hf_at(B, i, j);
+    T L[4] = {F.hL[f], F.hL[P.nhface + f], F.hL[2 * P.nhface + f], F.hL[3 * P.nhface + f]};
+    T R[4] = {F.hR[f], F.hR[P.nhface + f], F.hR[2 * P.nhface + f], F.hR[3 * P.nhface + f]};
+    T Fy[4];
+    riemann<FLUX>(L, R, G, Fy);
+    if (DBG && dbg.hflux_raw) store4(dbg.hflux_raw, P.nhface, f, Fy);
+    if (cart) unrotate90(Fy);
+    else unrotate(Fy, P.geo.hface[E2D_F_COS][f], P.geo.hface[E2D_F_SIN][f]);
+    if (DBG && dbg.hflux) store4(dbg.hflux, P.nhface, f, Fy);
+    const T len = P.geo.hface[E2D_F_L][f];
+    T I[4] = {len * (T(2) * Fy[0]), len * (T(2) * Fy[1]), len * (T(2) * Fy[2]), len * (T(2) * Fy[3])};
+    store4(F.hI, P.nhface, f, I);
+  }
+}
+
+// --------------------------------------------------------------------------------------
+// K3: divergence + RK stage program (+ positivity on the last stage)
+// --------------------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(TX * TY) k_update(ParamsT<T> P, const int4* __restrict__ tiles, FaceArraysT<T> F,
+                                                    StateBuffersT<T> S, StageProgram prog,
+                                                    InstanceState* __restrict__ inst,
+                                                    RealizState* __restrict__ real, T* __restrict__ dudt_out) {
+  const int4 tl = tiles[blockIdx.x];
+  const E2DBlock* B = P.blocks + tl.x;
+  const InstanceState* I = inst + B->instance;
+  if (!I->active) return;
+  const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
+  const int i = tl.y + ty, j = tl.z + tx;
+  const bool live = i < B->ny && j < B->nx;
+  bool bad = false;
+  int64_t c = 0;
+  if (live) {
+    c = cell_at(B, i, j);
+    const int64_t fW = vf_at(B, i, j), fE = fW + 1;
+    const int64_t fS = hf_at(B, i, j), fN = fS + B->nx;
+    const T A = P.geo.cell[E2D_G_A][c];
+    T k[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const T IW = F.vI[v * P.nvface + fW], IE = F.vI[v * P.nvface + fE];
+      const T IS = F.hI[v * P.nhface + fS], IN = F.hI[v * P.nhface + fN];
+      k[v] = T(0.5) * (IW - IE + IS - IN) / A;
+    }
+    if (dudt_out) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) dudt_out[v * P.ncell + c] = k[v];
+    }
+    const double dt = I->dt;
+    for (int u = 0; u < prog.nupd; ++u) {
+      const StageUpdate up = prog.upd[u];
+      const T* src = S.buf[up.src];
+      const T dta = T(dt * up.a);
+      if (!up.kahan) {
+        T* dst = S.buf[up.dst];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const T base = up.src_zero ? T(0) : src[v * P.ncell + c];
+          dst[v * P.ncell + c] = base + dta * k[v];
+        }
+      } else {
+        // U^{n+1} = U^n + increment with Kahan compensation carried across steps
+        T* U0 = S.buf[0];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const T inc = (up.src_zero ? T(0) : src[v * P.ncell + c]) + dta * k[v];
+          const T y = inc - S.comp[v * P.ncell + c];
+          const T u0 = U0[v * P.ncell + c];
+          const T tt = u0 + y;
+          S.comp[v * P.ncell + c] = (tt - u0) - y;
+          U0[v * P.ncell + c] = tt;
+        }
+      }
+    }
+    if (prog.final_stage) {
+      const T rho = S.buf[0][c], E = S.buf[0][3 * P.ncell + c];
+      bad = !(rho > T(0)) || !(E > T(0));
+      if (bad) atomicMin(&real->first, ((unsigned long long)tl.x << 40) | (unsigned long long)(c - B->cell_offset));
+    }
+  }
+  if (prog.final_stage) {
+    const int nb = __syncthreads_count(bad);
+    if (threadIdx.x == 0 && nb) atomicAdd(&real->nbad, (unsigned long long)nb);
+  }
+}
+
+// --------------------------------------------------------------------------------------
+// CFL time step: min over cells of min(dx/(|u|+a), dy/(|v|+a)) per instance
+// (quad_block.py:423-436)
+// --------------------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(TX * TY) k_dt(ParamsT<T> P, const int4* __restrict__ tiles,
+                                                const T* __restrict__ U, InstanceState* __restrict__ inst) {
+  const int4 tl = tiles[blockIdx.x];
+  const E2DBlock* B = P.blocks + tl.x;
+  InstanceState* I = inst + B->instance;
+  const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
+  const int i = tl.y + ty, j = tl.z + tx;
+  double m = __longlong_as_double(0x7ff0000000000000LL);
+  if (i < B->ny && j < B->nx) {
+    const int64_t c = cell_at(B, i, j);
+    T q[4], w[4];
+    load_cell(U, P.ncell, c, q);
+    const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
+    cons_to_prim(q, G, w);
+    const T a = sqrt(T(P.gamma) * w[3] / w[0]);
+    const T tx_ = P.geo.cell[E2D_G_CFL_DX][c] / (fabs(w[1]) + a);
+    const T ty_ = P.geo.cell[E2D_G_CFL_DY][c] / (fabs(w[2]) + a);
+    m = double(vmin(tx_, ty_));  // the reduction itself is FP64 on every path
+  }
+  unsigned long long bits = (unsigned long long)__double_as_longlong(m);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long other = __shfl_xor_sync(0xffffffffu, bits, o);
+    bits = other < bits ? other : bits;
+  }
+  __shared__ unsigned long long wmin[TX * TY / 32];
+  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = bits;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long b = wmin[0];
+    for (int w = 1; w < TX * TY / 32; ++w) b = wmin[w] < b ? wmin[w] : b;
+    atomicMin(&I->min_bits, b);
+  }
+}
+
+template <typename T>
+__global__ void k_realizable(ParamsT<T> P, const int4* __restrict__ tiles, const T* __restrict__ U,
+                             RealizState* __restrict__ real) {
+  const int4 tl = tiles[blockIdx.x];
+  const E2DBlock* B = P.blocks + tl.x;
+  const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
+  const int i = tl.y + ty, j = tl.z + tx;
+  bool bad = false;
+  if (i < B->ny && j < B->nx) {
+    const int64_t c = cell_at(B, i, j);
+    bad = !(U[c] > T(0)) || !(U[3 * P.ncell + c] > T(0));
+    if (bad) atomicMin(&real->first, ((unsigned long long)tl.x << 40) | (unsigned long long)(c - B->cell_offset));
+  }
+  const int nb = __syncthreads_count(bad);
+  if (threadIdx.x == 0 && nb) atomicAdd(&real->nbad, (unsigned long long)nb);
+}
+
+
+}  // namespace e2d
+
+namespace e2d {
+// ---- launchers ------------------------------------------------------------------------
+template <typename T, int LIM, int RECON>
+static cudaError_t recon_lim_recon(const ParamsT<T>& P, const int4* tiles, int n, const T* U,
+                                   const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>* dbg,
+                                   cudaStream_t st) {
+  if (dbg) k_reconstruct<T, LIM, RECON, true><<<n, TX * TY, 0, st>>>(P, tiles, U, inst, F, *dbg);
+  else k_reconstruct<T, LIM, RECON, false><<<n, TX * TY, 0, st>>>(P, tiles, U, inst, F, DebugOutT<T>{});
+  return cudaGetLastError();
+}
+
+template <typename T, int LIM>
+static cudaError_t recon_lim(const ParamsT<T>& P, const int4* tiles, int n, const T* U, const InstanceState* inst,
+                             FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st) {
+  if (P.recon == E2D_RECON_PRIMITIVE)
+    return recon_lim_recon<T, LIM, E2D_RECON_PRIMITIVE>(P, tiles, n, U, inst, F, dbg, st);
+  return recon_lim_recon<T, LIM, E2D_RECON_CONSERVATIVE>(P, tiles, n, U, inst, F, dbg, st);
+}
+
+template <typename T>
+cudaError_t launch_reconstruct(const ParamsT<T>& P, const int4* tiles, int n, const T* U, const InstanceState* inst,
+                               FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  switch (P.limiter) {
+    case E2D_LIM_BARTH_JESPERSEN: return recon_lim<T, E2D_LIM_BARTH_JESPERSEN>(P, tiles, n, U, inst, F, dbg, st);
+    case E2D_LIM_VAN_ALBADA: return recon_lim<T, E2D_LIM_VAN_ALBADA>(P, tiles, n, U, inst, F, dbg, st);
+    case E2D_LIM_VAN_LEER: return recon_lim<T, E2D_LIM_VAN_LEER>(P, tiles, n, U, inst, F, dbg, st);
+    default: return recon_lim<T, E2D_LIM_VENKATAKRISHNAN>(P, tiles, n, U, inst, F, dbg, st);
+  }
+}
+
+template <typename T, int FLUX>
+static cudaError_t flux_t(const ParamsT<T>& P, const int4* tiles, int n, const InstanceState* inst,
+                          FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st) {
+  if (dbg) k_flux<T, FLUX, true><<<n, TX * TY, 0, st>>>(P, tiles, inst, F, *dbg);
+  else k_flux<T, FLUX, false><<<n, TX * TY, 0, st>>>(P, tiles, inst, F, DebugOutT<T>{});
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_flux(const ParamsT<T>& P, const int4* tiles, int n, const InstanceState* inst, FaceArraysT<T> F,
+                        const DebugOutT<T>* dbg, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  switch (P.flux) {
+    case E2D_FLUX_HLLL: return flux_t<T, E2D_FLUX_HLLL>(P, tiles, n, inst, F, dbg, st);
+    case E2D_FLUX_HLLE: return flux_t<T, E2D_FLUX_HLLE>(P, tiles, n, inst, F, dbg, st);
+    default: return flux_t<T, E2D_FLUX_ROE>(P, tiles, n, inst, F, dbg, st);
+  }
+}
+
+template <typename T>
+cudaError_t launch_update(const ParamsT<T>& P, const int4* tiles, int n, FaceArraysT<T> F, StateBuffersT<T> S,
+                          const StageProgram& prog, InstanceState* inst, RealizState* real, T* dudt_out,
+                          cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_update<T><<<n, TX * TY, 0, st>>>(P, tiles, F, S, prog, inst, real, dudt_out);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_dt(const ParamsT<T>& P, const int4* tiles, int n, const T* U, InstanceState* inst,
+                      cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_dt<T><<<n, TX * TY, 0, st>>>(P, tiles, U, inst);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_realizable(const ParamsT<T>& P, const int4* tiles, int n, const T* U, RealizState* real,
+                              cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_realizable<T><<<n, TX * TY, 0, st>>>(P, tiles, U, real);
+  return cudaGetLastError();
+}
+
+#define E2D_INSTANTIATE_STAGE_LAUNCHERS(T)                                                                       \
+  template cudaError_t launch_reconstruct<T>(const ParamsT<T>&, const int4*, int, const T*, const InstanceState*, \
+                                             FaceArraysT<T>, const DebugOutT<T>*, cudaStream_t);                 \
+  template cudaError_t launch_flux<T>(const ParamsT<T>&, const int4*, int, const InstanceState*, FaceArraysT<T>,  \
+                                      const DebugOutT<T>*, cudaStream_t);                                        \
+  template cudaError_t launch_update<T>(const ParamsT<T>&, const int4*, int, FaceArraysT<T>, StateBuffersT<T>,    \
+                                        const StageProgram&, InstanceState*, RealizState*, T*, cudaStream_t);    \
+  template cudaError_t launch_dt<T>(const ParamsT<T>&, const int4*, int, const T*, InstanceState*, cudaStream_t); \
+  template cudaError_t launch_realizable<T>(const ParamsT<T>&, const int4*, int, const T*, RealizState*, cudaStream_t);
+
+}  // namespace e2d

@@ -136,6 +136,16 @@ class Problem:
     def nblocks(self) -> int:
         return len(self.block_ids)
 
+    def with_precision(self, precision: int) -> "Problem":
+        """The same block table and geometry with another arithmetic precision
+        (0 = FP64, 1 = FP32); arrays are shared, not copied."""
+        cfg = E2DConfig()
+        ctypes.pointer(cfg)[0] = self.cfg
+        cfg.precision = precision
+        return Problem(cfg=cfg, blocks=self.blocks, geometry=self.geometry, block_geometry=self.block_geometry,
+                       block_ids=self.block_ids, cell_offsets=self.cell_offsets, ncell=self.ncell,
+                       nvface=self.nvface, nhface=self.nhface, _keep=self._keep)
+
     # ---- layout helpers: (nblocks, ny, nx, 4) <-> SoA planes ----------------------
     def to_soa(self, per_block: List[np.ndarray]) -> np.ndarray:
         out = np.empty((4, self.ncell), dtype=np.float64)

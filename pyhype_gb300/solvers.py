@@ -57,12 +57,18 @@ class HostBlock:
 
 
 class Euler2D:
-    def __init__(self, config, mesh_config: Union[MeshGenerator, dict]) -> None:
+    def __init__(self, config, mesh_config: Union[MeshGenerator, dict], precision: str = "fp64") -> None:
+        """``precision="fp32"`` selects the FP32 form (FP32 state and flux arithmetic,
+        Kahan-compensated step accumulation, FP64 dt reduction); the default is the
+        FP64 path, equal to the reference value for value."""
+        if precision not in ("fp64", "fp32"):
+            raise ValueError(f"precision must be 'fp64' or 'fp32', not {precision!r}")
+        self.precision = precision
         self.config = config
         self.fluid = config.fluid
         info = mesh_config.dict if isinstance(mesh_config, MeshGenerator) else mesh_config
         self.mesh_config: Dict[int, dict] = info
-        self.problem = problem_from_config(config, info)
+        self.problem = problem_from_config(config, info, precision=0 if precision == "fp64" else 1)
         self._blocks: Dict[int, HostBlock] = {}
         for k, blk in enumerate(self.problem.block_ids):
             d = info[blk]

@@ -1,0 +1,55 @@
+"""The FP32 form (FP32 state, geometry and flux arithmetic; Kahan-compensated step
+accumulation; FP64 dt reduction) against the FP64 path on the same problems.
+
+Stated results, not bit-exactness: the L1 density error relative to the FP64 path
+stays below the bound written in each test."""
+import numpy as np
+import pytest
+
+import _golden as G
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(z, tableau=None):
+    from pyhype_gb300._native import DeviceSolver
+
+    P64 = G.problem(z, precision=0)
+    P32 = G.problem(z, precision=1)
+    a = z["tableau"] if tableau is None else tableau
+    return P64, DeviceSolver(P64, tableau=a), DeviceSolver(P32, tableau=a)
+
+
+def _l1_rel(a, b):
+    return float(np.sum(np.abs(a - b)) / np.sum(np.abs(b)))
+
+
+@pytest.mark.parametrize("name,steps,bound", [("p100", 100, 1e-5), ("m2x4_40", 12, 1e-5), ("dmr5", 8, 1e-5),
+                                              ("hlll_prim", 5, 1e-5), ("lim_vl", 5, 1e-5)])
+def test_fp32_density_l1_vs_fp64(name, steps, bound):
+    z = G.load(name)
+    P, S64, S32 = _pair(z)
+    U0 = P.to_soa(list(z["ic"]))
+    S64.set_state(U0)
+    S32.set_state(U0)
+    tf = G.t_final(z)
+    t64, n64 = S64.run(0.0, tf, max_steps=steps)
+    t32, n32 = S32.run(0.0, tf, max_steps=steps)
+    assert n64 == n32 == steps
+    assert abs(t32 - t64) <= 1e-5 * t64  # dt from FP32 states, reduced in FP64
+    U64, U32 = S64.get_state(), S32.get_state()
+    err = _l1_rel(U32[0], U64[0])
+    assert err < bound, f"L1 density error {err:.3e}"
+    assert S32.check_realizable().ok == 1
+
+
+def test_fp32_residual_close_to_fp64():
+    z = G.load("ops_explosion_cons")
+    P, S64, S32 = _pair(z)
+    U = P.to_soa(list(z["ops_state"]))
+    S64.set_state(U)
+    S32.set_state(U)
+    d64 = S64.residual()
+    d32 = S32.residual()
+    scale = np.max(np.abs(d64), axis=1, keepdims=True)
+    assert np.max(np.abs(d32 - d64) / scale) < 1e-3
