@@ -227,6 +227,9 @@ E2D_API int e2d_step(E2DHandle h, double dt, double t);
 E2D_API int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps,
             int32_t* steps_done, E2DRealizability* real);
 E2D_API int e2d_check_realizable(E2DHandle h, E2DRealizability* out);
+/* Solver time and steps taken of every instance (batched problems advance each
+   instance with its own CFL dt); arrays of E2DConfig.ninstances entries.        */
+E2D_API int e2d_instance_times(E2DHandle h, double* t_out, int32_t* steps_out);
 
 /* ---- per-operator entry points (parity testing) ---------------------------------- */
 /* dUdt of the current state (FiniteVolumeMethod.dUdt, pyhype/fvm/base.py:108-139)

@@ -29,7 +29,7 @@ E2D_ERR_NOMEM = -6
 EXPORTS = (
     "e2d_abi_version", "e2d_last_error", "e2d_create", "e2d_destroy", "e2d_set_stream", "e2d_num_cells",
     "e2d_set_state", "e2d_get_state", "e2d_set_state_device", "e2d_get_state_device", "e2d_set_tableau",
-    "e2d_compute_dt", "e2d_step", "e2d_run", "e2d_check_realizable", "e2d_residual",
+    "e2d_compute_dt", "e2d_step", "e2d_run", "e2d_check_realizable", "e2d_residual", "e2d_instance_times",
 )
 
 
@@ -75,6 +75,7 @@ def load(path: Optional[str] = None):
     L.e2d_run.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_int32,
                           ctypes.POINTER(ctypes.c_int32), vp]
     L.e2d_check_realizable.argtypes = [vp, vp]
+    L.e2d_instance_times.argtypes = [vp, vp, vp]
     L.e2d_residual.argtypes = [vp, ctypes.c_double, vp, vp]
     if L.e2d_abi_version() != 1:
         raise RuntimeError("libeuler2d.so ABI version mismatch")
@@ -156,6 +157,13 @@ class DeviceSolver:
             raise RealizabilityError(code, self.L.e2d_last_error().decode(), r)
         _check(code)
         return tt.value, steps.value
+
+    def instance_times(self):
+        n = max(1, self.problem.cfg.ninstances)
+        t = np.zeros(n)
+        steps = np.zeros(n, dtype=np.int32)
+        _check(self.L.e2d_instance_times(self.h, t.ctypes.data, steps.ctypes.data))
+        return t, steps
 
     def check_realizable(self) -> E2DRealizability:
         r = E2DRealizability()

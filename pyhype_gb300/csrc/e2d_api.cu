@@ -660,6 +660,18 @@ int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* d) {
   return 0;
 }
 
+int e2d_instance_times(E2DHandle h, double* t_out, int32_t* steps_out) {
+  if (!h) return fail(E2D_ERR_INVALID, "null handle");
+  const int ninst = (int)h->hinst.size();
+  CK(cudaMemcpyAsync(h->hinst.data(), h->inst, sizeof(InstanceState) * ninst, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int q = 0; q < ninst; ++q) {
+    if (t_out) t_out[q] = h->hinst[q].t;
+    if (steps_out) steps_out[q] = h->hinst[q].steps;
+  }
+  return 0;
+}
+
 int e2d_check_realizable(E2DHandle h, E2DRealizability* out) {
   if (!h || !out) return fail(E2D_ERR_INVALID, "null argument");
   k_reset_real<<<1, 1, 0, h->stream>>>(h->real);
