@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--n", type=int, default=1024, help="cells per block side")
     ap.add_argument("--cpu-steps", type=int, default=1, help="RK4 steps in the CPU-baseline sample")
     ap.add_argument("--skip-cpu-baseline", action="store_true", help="omit the CPU baseline (profiling runs)")
+    ap.add_argument("--skip-ensemble", action="store_true", help="omit the batched-ensemble section")
+    ap.add_argument("--workload", default="multiblock", choices=["multiblock", "ensemble"],
+                    help="'ensemble' runs the full 512-instance, 200-step batched comparison instead")
     return ap.parse_args()
 
 
@@ -224,6 +227,69 @@ def cpu_baseline(n: int, steps: int):
     }
 
 
+def ensemble_section(stream, full: bool = False, autotune: bool = True):
+    """512 seeded explosion instances of uneven sizes (64..512 per side), Roe/Venkat,
+    SSP-RK2, CFL 0.5, per-instance dt: FP32 batched vs FP64 batched vs FP64 instances
+    solved one after another, and the FP32 L1 density difference at equal steps."""
+    import numpy as np
+    import torch
+
+    from pyhype_gb300.batch import EnsembleSolver, ensemble_problem, explosion_ensemble
+
+    inst = explosion_ensemble(512, seed=0)
+    P = ensemble_problem(inst, precision=0, cfl=0.5)
+    cells = P.ncell
+    stages = 2
+    k32, w = (200, 3) if full else (20, 3)
+    k64 = 200 if full else 10
+    out = {"workload": "512 instances, nx,ny in {64..512} (seed 0), explosion IC, Roe/Venkatakrishnan, SSP-RK2, "
+                       "CFL 0.5, per-instance dt", "cells": cells}
+
+    def timed(solver, steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        solver.device.run(0.0, float("inf"), max_steps=steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    E32 = EnsembleSolver(inst, precision=1, problem=P)
+    E32.device.set_stream(stream.cuda_stream)
+    if autotune:
+        out["fp32_autotune"] = E32.device.autotune(reps=2)
+    E32.device.run(0.0, float("inf"), max_steps=w)
+    ms32 = timed(E32, k32)
+    out["fp32_batched"] = {"value": cells * stages * k32 / (ms32 * 1e-3), "unit": "cell-stage updates/s",
+                           "steps": k32, "ms_per_step": ms32 / k32}
+    E64 = EnsembleSolver(inst, precision=0, problem=P)
+    E64.device.set_stream(stream.cuda_stream)
+    E64.device.run(0.0, float("inf"), max_steps=w)
+    ms64 = timed(E64, k64)
+    out["fp64_batched"] = {"value": cells * stages * k64 / (ms64 * 1e-3), "unit": "cell-stage updates/s",
+                           "steps": k64, "ms_per_step": ms64 / k64}
+    if w + k64 < w + k32:
+        E64.device.run(0.0, float("inf"), max_steps=k32 - k64)
+    a, b = E64.states(), E32.states()
+    l1 = [float(np.sum(np.abs(y[:, :, 0] - x[:, :, 0])) / np.sum(np.abs(x[:, :, 0]))) for x, y in zip(a, b)]
+    out["fp32_l1_density_rel_vs_fp64"] = {"after_steps": w + k32, "mean": float(np.mean(l1)), "max": float(np.max(l1))}
+    # FP64 instances one after another (each its own device problem)
+    nseq = 512 if full else 16
+    seq_ms, seq_cells = 0.0, 0
+    for one in inst[:nseq]:
+        S = EnsembleSolver([one], precision=0)
+        S.device.set_stream(stream.cuda_stream)
+        S.device.run(0.0, float("inf"), max_steps=1)
+        seq_ms += timed(S, k64)
+        seq_cells += S.problem.ncell
+        S.device.close()
+    out["fp64_sequential"] = {"value": seq_cells * stages * k64 / (seq_ms * 1e-3), "unit": "cell-stage updates/s",
+                              "instances_timed": nseq, "steps": k64}
+    out["fp32_batched_over_fp64_sequential"] = out["fp32_batched"]["value"] / out["fp64_sequential"]["value"]
+    E32.device.close()
+    E64.device.close()
+    return out
+
+
 def run_reference(args, ws, rank):
     """--impl reference: the reference algorithm's CPU implementation (C restatement,
     all host threads) on the same workload; rank 0 only."""
@@ -268,6 +334,15 @@ def main():
         return
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
+    if args.workload == "ensemble":
+        import torch
+
+        torch.cuda.set_device(local)
+        st = torch.cuda.Stream()
+        res = ensemble_section(st, full=True)
+        if rank == 0:
+            print(json.dumps({"metric": "cell-stage updates/s, batched ensemble", "ensemble": res}), flush=True)
+        return
     import ctypes
 
     import numpy as np
@@ -387,6 +462,14 @@ def main():
     except Exception as exc:
         fp32 = {"error": str(exc)}
 
+    ensemble = None
+    if not args.skip_ensemble and ws == 1:
+        try:
+            ensemble = ensemble_section(stream)
+            ensemble["fp32_batched_over_fp64_plain"] = ensemble["fp32_batched"]["value"] / value
+        except Exception as exc:
+            ensemble = {"error": str(exc)}
+
     clocks = clk.summary()
     line = {
         "metric": METRIC,
@@ -420,6 +503,7 @@ def main():
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"},
         },
         "fp32": fp32,
+        "ensemble": ensemble,
         "gpu_launches": int(args.steps * (3 + 3 * stages)),
         "clocks": clocks,
     }

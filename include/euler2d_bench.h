@@ -25,6 +25,20 @@ E2D_API int e2d_bench_fp64_peak(int32_t op, double* tflops);
 #define E2D_BENCH_NK 5
 E2D_API int e2d_bench_kernels(E2DHandle h, int32_t steps, double* ms, int64_t* launches);
 
+/* Kernel-variant selection.  Every variant computes the same values; they differ in
+   tile height, register/occupancy target and grid shape (one CTA per tile, or a
+   persistent grid of resident CTAs striding over the tile table).
+   kernel: 0 = reconstruct (variants 0..4: tile height x min CTAs per SM of (8,1),
+   (8,2), (4,2), (4,4), (16,1)), 1 = flux (variants 0..2: min CTAs per SM 1, 2, 3),
+   2 = update (variant 0).                                                       */
+E2D_API int e2d_set_kernel_choice(E2DHandle h, int32_t kernel, int32_t variant, int32_t persistent);
+/* Autotuner: times every variant and grid shape of the reconstruct and flux kernels
+   and the grid shape of the update kernel on the current state (`reps` launches each,
+   CUDA events on the handle's stream), keeps the fastest and returns the choices in
+   chosen[0..5] = {reconstruct variant, persistent, flux variant, persistent, update
+   variant, persistent}.  Graphs captured before are dropped.                    */
+E2D_API int e2d_autotune(E2DHandle h, int32_t reps, int32_t* chosen);
+
 #ifdef __cplusplus
 }
 #endif

@@ -76,6 +76,8 @@ def load(path: Optional[str] = None):
                           ctypes.POINTER(ctypes.c_int32), vp]
     L.e2d_check_realizable.argtypes = [vp, vp]
     L.e2d_instance_times.argtypes = [vp, vp, vp]
+    L.e2d_set_kernel_choice.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
+    L.e2d_autotune.argtypes = [vp, ctypes.c_int32, vp]
     L.e2d_residual.argtypes = [vp, ctypes.c_double, vp, vp]
     if L.e2d_abi_version() != 1:
         raise RuntimeError("libeuler2d.so ABI version mismatch")
@@ -157,6 +159,16 @@ class DeviceSolver:
             raise RealizabilityError(code, self.L.e2d_last_error().decode(), r)
         _check(code)
         return tt.value, steps.value
+
+    def set_kernel_choice(self, kernel: int, variant: int, persistent: bool = False):
+        _check(self.L.e2d_set_kernel_choice(self.h, kernel, variant, int(persistent)))
+
+    def autotune(self, reps: int = 3) -> dict:
+        """Pick the fastest kernel variants on the current state (same results)."""
+        ch = np.zeros(6, dtype=np.int32)
+        _check(self.L.e2d_autotune(self.h, reps, ch.ctypes.data))
+        return {"reconstruct": (int(ch[0]), bool(ch[1])), "flux": (int(ch[2]), bool(ch[3])),
+                "update": (int(ch[4]), bool(ch[5]))}
 
     def instance_times(self):
         n = max(1, self.problem.cfg.ninstances)

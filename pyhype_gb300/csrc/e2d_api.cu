@@ -79,10 +79,14 @@ struct E2DSolver {
   PathT<float> pf;
   E2DBlock* dblocks = nullptr;
   std::vector<void*> allocs;
-  int4* cell_tiles = nullptr;
+  int4* cell_tiles = nullptr;   // tile height 8 (dt, update, default reconstruct)
   int ncell_tiles = 0;
   int4* face_tiles = nullptr;
   int nface_tiles = 0;
+  TileSet ts{};                  // all tile tables (heights 4, 8, 16)
+  KernelChoice kr{0, false};     // reconstruct variant (autotuned)
+  KernelChoice kf{0, false};     // flux variant
+  KernelChoice ku{0, false};     // update variant
   int nbuf = 0;
   InstanceState* inst = nullptr;
   std::vector<InstanceState> hinst;
@@ -297,13 +301,13 @@ static int bench_kernels_t(E2DHandle h, int32_t steps, double* ms, int64_t* laun
     for (int s = 0; s < h->nstages; ++s) {
       const T* in = p.S.buf[h->stage_input[s]];
       CK(rec(1));
-      CK(launch_reconstruct<T>(p.P, h->cell_tiles, h->ncell_tiles, in, h->inst, p.F, nullptr, h->stream));
+      CK(launch_reconstruct<T>(p.P, h->ts, h->kr, in, h->inst, p.F, nullptr, h->stream));
       CK(fin());
       CK(rec(2));
-      CK(launch_flux<T>(p.P, h->face_tiles, h->nface_tiles, h->inst, p.F, nullptr, h->stream));
+      CK(launch_flux<T>(p.P, h->ts, h->kf, h->inst, p.F, nullptr, h->stream));
       CK(fin());
       CK(rec(3));
-      CK(launch_update<T>(p.P, h->cell_tiles, h->ncell_tiles, p.F, p.S, h->prog[s], h->inst, h->real, nullptr,
+      CK(launch_update<T>(p.P, h->ts, h->ku, p.F, p.S, h->prog[s], h->inst, h->real, nullptr,
                           h->stream));
       CK(fin());
     }
@@ -330,6 +334,60 @@ static int bench_kernels_t(E2DHandle h, int32_t steps, double* ms, int64_t* laun
   return 0;
 }
 
+
+// Times `reps` launches of one kernel class under the handle's current choice.
+template <typename T>
+static int time_kernel(E2DHandle h, int which, int reps, float* ms) {
+  PathT<T>& p = path<T>(h);
+  StageProgram none{};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  for (int r = -1; r < reps; ++r) {  // r = -1 warms up
+    if (r == 0) CK(cudaEventRecord(e0, h->stream));
+    if (which == 0) CK(launch_reconstruct<T>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, nullptr, h->stream));
+    else if (which == 1) CK(launch_flux<T>(p.P, h->ts, h->kf, h->inst, p.F, nullptr, h->stream));
+    else CK(launch_update<T>(p.P, h->ts, h->ku, p.F, p.S, none, h->inst, h->real, nullptr, h->stream));
+  }
+  CK(cudaEventRecord(e1, h->stream));
+  CK(cudaEventSynchronize(e1));
+  CK(cudaEventElapsedTime(ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms /= reps;
+  return 0;
+}
+
+template <typename T>
+static int autotune_t(E2DHandle h, int reps, int32_t* chosen) {
+  const int ninst = (int)h->hinst.size();
+  CK(launch_set_time(h->inst, ninst, h->hinst.empty() ? 0.0 : h->hinst[0].t, 0.0, h->stream));
+  KernelChoice* ch[3] = {&h->kr, &h->kf, &h->ku};
+  const int nvar[3] = {N_RECON_VARIANTS, N_FLUX_VARIANTS, 1};
+  for (int which = 0; which < 3; ++which) {
+    KernelChoice best = *ch[which];
+    float best_ms = 1e30f;
+    for (int v = 0; v < nvar[which]; ++v)
+      for (int pers = 0; pers < 2; ++pers) {
+        *ch[which] = KernelChoice{v, pers != 0};
+        float ms = 0.f;
+        if (int e = time_kernel<T>(h, which, reps, &ms)) return e;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = *ch[which];
+        }
+      }
+    *ch[which] = best;
+    if (chosen) {
+      chosen[2 * which] = best.variant;
+      chosen[2 * which + 1] = best.persistent ? 1 : 0;
+    }
+  }
+  CK(launch_end_step(h->inst, ninst, h->real, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->drop_graphs();
+  return 0;
+}
 
 extern "C" {
 
@@ -421,22 +479,38 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
   if ((ce = cudaMemcpy(h->dblocks, dev_blocks.data(), sizeof(E2DBlock) * cfg->nblocks, cudaMemcpyHostToDevice)) != cudaSuccess)
     return bail(fail(E2D_ERR_CUDA, "block table copy: %s", cudaGetErrorString(ce)));
 
-  // tile tables: cells (ny x nx) and face nodes ((ny+1) x (nx+1)) per block
-  std::vector<int4> ct, ft;
-  for (int b = 0; b < cfg->nblocks; ++b) {
-    const E2DBlock& B = h->hblocks[b];
-    for (int i0 = 0; i0 < B.ny; i0 += TY)
-      for (int j0 = 0; j0 < B.nx; j0 += TX) ct.push_back(make_int4(b, i0, j0, 0));
-    for (int i0 = 0; i0 <= B.ny; i0 += TY)
-      for (int j0 = 0; j0 <= B.nx; j0 += TX) ft.push_back(make_int4(b, i0, j0, 0));
+  // tile tables: cells (ny x nx) at tile heights 4, 8, 16 and face nodes ((ny+1) x (nx+1))
+  {
+    const int heights[3] = {4, 8, 16};
+    for (int v = 0; v < 3; ++v) {
+      std::vector<int4> ct;
+      for (int b = 0; b < cfg->nblocks; ++b) {
+        const E2DBlock& B = h->hblocks[b];
+        for (int i0 = 0; i0 < B.ny; i0 += heights[v])
+          for (int j0 = 0; j0 < B.nx; j0 += TX) ct.push_back(make_int4(b, i0, j0, 0));
+      }
+      int4* d = nullptr;
+      if (int e = h->alloc(&d, ct.size())) return bail(e);
+      if ((ce = cudaMemcpy(d, ct.data(), sizeof(int4) * ct.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail(fail(E2D_ERR_CUDA, "tile copy: %s", cudaGetErrorString(ce)));
+      h->ts.cell[v] = d;
+      h->ts.ncell[v] = (int)ct.size();
+    }
+    std::vector<int4> ft;
+    for (int b = 0; b < cfg->nblocks; ++b) {
+      const E2DBlock& B = h->hblocks[b];
+      for (int i0 = 0; i0 <= B.ny; i0 += TY)
+        for (int j0 = 0; j0 <= B.nx; j0 += TX) ft.push_back(make_int4(b, i0, j0, 0));
+    }
+    if (int e = h->alloc(&h->face_tiles, ft.size())) return bail(e);
+    if ((ce = cudaMemcpy(h->face_tiles, ft.data(), sizeof(int4) * ft.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return bail(fail(E2D_ERR_CUDA, "tile copy: %s", cudaGetErrorString(ce)));
+    h->nface_tiles = (int)ft.size();
+    h->ts.face = h->face_tiles;
+    h->ts.nface = h->nface_tiles;
+    h->cell_tiles = const_cast<int4*>(h->ts.cell[1]);
+    h->ncell_tiles = h->ts.ncell[1];
   }
-  h->ncell_tiles = (int)ct.size();
-  h->nface_tiles = (int)ft.size();
-  if (int e = h->alloc(&h->cell_tiles, ct.size())) return bail(e);
-  if (int e = h->alloc(&h->face_tiles, ft.size())) return bail(e);
-  if ((ce = cudaMemcpy(h->cell_tiles, ct.data(), sizeof(int4) * ct.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
-      (ce = cudaMemcpy(h->face_tiles, ft.data(), sizeof(int4) * ft.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
-    return bail(fail(E2D_ERR_CUDA, "tile copy: %s", cudaGetErrorString(ce)));
 
   // instance time state and realizability counters
   h->hinst.assign(ninst, InstanceState{});
@@ -549,9 +623,9 @@ static int enqueue_stages(E2DHandle h, T* dudt_out, const DebugOutT<T>* dbg) {
   PathT<T>& p = path<T>(h);
   for (int s = 0; s < h->nstages; ++s) {
     const T* in = p.S.buf[h->stage_input[s]];
-    CK(launch_reconstruct<T>(p.P, h->cell_tiles, h->ncell_tiles, in, h->inst, p.F, dbg, h->stream));
-    CK(launch_flux<T>(p.P, h->face_tiles, h->nface_tiles, h->inst, p.F, dbg, h->stream));
-    CK(launch_update<T>(p.P, h->cell_tiles, h->ncell_tiles, p.F, p.S, h->prog[s], h->inst, h->real, dudt_out,
+    CK(launch_reconstruct<T>(p.P, h->ts, h->kr, in, h->inst, p.F, dbg, h->stream));
+    CK(launch_flux<T>(p.P, h->ts, h->kf, h->inst, p.F, dbg, h->stream));
+    CK(launch_update<T>(p.P, h->ts, h->ku, p.F, p.S, h->prog[s], h->inst, h->real, dudt_out,
                         h->stream));
   }
   return 0;
@@ -628,9 +702,9 @@ int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* d) {
     PathT<float>& p = h->pf;
     if (!p.dudt_tmp)
       if (int e = h->alloc(&p.dudt_tmp, 4 * (size_t)h->ncell)) return e;
-    CK(launch_reconstruct<float>(p.P, h->cell_tiles, h->ncell_tiles, p.S.buf[0], h->inst, p.F, nullptr, h->stream));
-    CK(launch_flux<float>(p.P, h->face_tiles, h->nface_tiles, h->inst, p.F, nullptr, h->stream));
-    CK(launch_update<float>(p.P, h->cell_tiles, h->ncell_tiles, p.F, p.S, none, h->inst, h->real, p.dudt_tmp,
+    CK(launch_reconstruct<float>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, nullptr, h->stream));
+    CK(launch_flux<float>(p.P, h->ts, h->kf, h->inst, p.F, nullptr, h->stream));
+    CK(launch_update<float>(p.P, h->ts, h->ku, p.F, p.S, none, h->inst, h->real, p.dudt_tmp,
                             h->stream));
     CK(launch_convert(p.dudt_tmp, dudt_dev, 4 * h->ncell, h->stream));
   } else {
@@ -643,9 +717,9 @@ int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* d) {
       dbg.vflux = d->vflux; dbg.hflux = d->hflux;
       pdb = &dbg;
     }
-    CK(launch_reconstruct<double>(p.P, h->cell_tiles, h->ncell_tiles, p.S.buf[0], h->inst, p.F, pdb, h->stream));
-    CK(launch_flux<double>(p.P, h->face_tiles, h->nface_tiles, h->inst, p.F, pdb, h->stream));
-    CK(launch_update<double>(p.P, h->cell_tiles, h->ncell_tiles, p.F, p.S, none, h->inst, h->real, dudt_dev,
+    CK(launch_reconstruct<double>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, pdb, h->stream));
+    CK(launch_flux<double>(p.P, h->ts, h->kf, h->inst, p.F, pdb, h->stream));
+    CK(launch_update<double>(p.P, h->ts, h->ku, p.F, p.S, none, h->inst, h->real, dudt_dev,
                              h->stream));
     if (d) {
       const size_t bv = sizeof(double) * 4 * h->nvface, bh = sizeof(double) * 4 * h->nhface;
@@ -768,6 +842,22 @@ int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps, int
 int e2d_bench_kernels(E2DHandle h, int32_t steps, double* ms, int64_t* launches) {
   if (!h || !ms || steps < 1) return fail(E2D_ERR_INVALID, "bad argument");
   return E2D_DISPATCH(h, bench_kernels_t, steps, ms, launches);
+}
+
+int e2d_set_kernel_choice(E2DHandle h, int32_t kernel, int32_t variant, int32_t persistent) {
+  if (!h) return fail(E2D_ERR_INVALID, "null handle");
+  const int nvar[3] = {N_RECON_VARIANTS, N_FLUX_VARIANTS, 1};
+  if (kernel < 0 || kernel > 2 || variant < 0 || variant >= nvar[kernel])
+    return fail(E2D_ERR_INVALID, "kernel %d has no variant %d", kernel, variant);
+  KernelChoice* ch[3] = {&h->kr, &h->kf, &h->ku};
+  *ch[kernel] = KernelChoice{variant, persistent != 0};
+  h->drop_graphs();
+  return 0;
+}
+
+int e2d_autotune(E2DHandle h, int32_t reps, int32_t* chosen) {
+  if (!h || reps < 1) return fail(E2D_ERR_INVALID, "bad argument");
+  return E2D_DISPATCH(h, autotune_t, reps, chosen);
 }
 
 }  // extern "C"

@@ -101,16 +101,32 @@ using Params = ParamsT<double>;
 using StateBuffers = StateBuffersT<double>;
 using DebugOut = DebugOutT<double>;
 
+// Tile tables: cell tiles for tile heights 4, 8 and 16 (index 0..2), face-node tiles
+// at height 8.  Each entry is (block, i0, j0, 0).
+struct TileSet {
+  const int4* cell[3];
+  int ncell[3];
+  const int4* face;
+  int nface;
+};
+// Kernel variant chosen by the autotuner (0 = default) and persistent-grid flag.
+struct KernelChoice {
+  int variant;
+  bool persistent;
+};
+constexpr int N_RECON_VARIANTS = 5;  // (tile height, min CTAs/SM): (8,1) (8,2) (4,2) (4,4) (16,1)
+constexpr int N_FLUX_VARIANTS = 3;   // min CTAs/SM: 1, 2, 3
+
 // launchers, instantiated for double (e2d_fp64.cu) and float (e2d_fp32.cu)
 template <typename T>
-cudaError_t launch_reconstruct(const ParamsT<T>& P, const int4* cell_tiles, int ntiles, const T* U,
+cudaError_t launch_reconstruct(const ParamsT<T>& P, const TileSet& ts, KernelChoice kc, const T* U,
                                const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>* dbg,
                                cudaStream_t st);
 template <typename T>
-cudaError_t launch_flux(const ParamsT<T>& P, const int4* face_tiles, int ntiles, const InstanceState* inst,
+cudaError_t launch_flux(const ParamsT<T>& P, const TileSet& ts, KernelChoice kc, const InstanceState* inst,
                         FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st);
 template <typename T>
-cudaError_t launch_update(const ParamsT<T>& P, const int4* cell_tiles, int ntiles, FaceArraysT<T> F,
+cudaError_t launch_update(const ParamsT<T>& P, const TileSet& ts, KernelChoice kc, FaceArraysT<T> F,
                           StateBuffersT<T> S, const StageProgram& prog, InstanceState* inst,
                           RealizState* real, T* dudt_out, cudaStream_t st);
 template <typename T>

@@ -147,22 +147,23 @@ __device__ __forceinline__ void outside_state(const ParamsT<T>& P, const E2DBloc
 // --------------------------------------------------------------------------------------
 // K1: reconstruction
 // --------------------------------------------------------------------------------------
-template <typename T, int LIM, int RECON, bool DBG>
-__global__ void __launch_bounds__(TX * TY) k_reconstruct(ParamsT<T> P, const int4* __restrict__ tiles,
-                                                         const T* __restrict__ U,
-                                                         const InstanceState* __restrict__ inst,
-                                                         FaceArraysT<T> F, DebugOutT<T> dbg) {
-  const int4 tl = tiles[blockIdx.x];
+template <typename T, int LIM, int RECON, bool DBG, int RTY, int MINB>
+__global__ void __launch_bounds__(TX * RTY, MINB) k_reconstruct(ParamsT<T> P, const int4* __restrict__ tiles,
+                                                                int ntiles, const T* __restrict__ U,
+                                                                const InstanceState* __restrict__ inst,
+                                                                FaceArraysT<T> F, DebugOutT<T> dbg) {
+  __shared__ T sW[4][RTY + 2][TX + 2];
+  const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
+  // a grid of ntiles CTAs does one tile each; a smaller (persistent) grid strides
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  const int4 tl = tiles[tile];
   const E2DBlock* B = P.blocks + tl.x;
   const InstanceState* I = inst + B->instance;
-  if (!I->active) return;
+  if (!I->active) continue;
   const double t = I->t;
   const int nx = B->nx, ny = B->ny;
   const int i0 = tl.y, j0 = tl.z;
-  const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
-
-  __shared__ T sW[4][TY + 2][TX + 2];
-  for (int p = threadIdx.x; p < (TY + 2) * (TX + 2); p += TX * TY) {
+  for (int p = threadIdx.x; p < (RTY + 2) * (TX + 2); p += TX * RTY) {
     const int ly = p / (TX + 2), lx = p - ly * (TX + 2);
     const int gi = i0 + ly - 1, gj = j0 + lx - 1;
     const bool in_i = gi >= 0 && gi < ny, in_j = gj >= 0 && gj < nx;
@@ -184,7 +185,7 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct(ParamsT<T> P, const int
 
   const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
   const int i = i0 + ty, j = j0 + tx;
-  if (i >= ny || j >= nx) return;
+  if (i < ny && j < nx) {
   const int64_t c = cell_at(B, i, j);
   const int64_t fE = vf_at(B, i, j + 1), fW = vf_at(B, i, j);
   const int64_t fN = hf_at(B, i + 1, j), fS = hf_at(B, i, j);
@@ -306,22 +307,26 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct(ParamsT<T> P, const int
     recon_to_prim<RECON>(o, G, w);
     store4(F.hR, P.nhface, fN, w);
   }
+  }  // live cell
+  __syncthreads();  // the next tile reuses sW
+  }  // tiles
 }
 
 // --------------------------------------------------------------------------------------
 // K2: one Riemann flux per face
 // --------------------------------------------------------------------------------------
-template <typename T, int FLUX, bool DBG>
-__global__ void __launch_bounds__(TX * TY) k_flux(ParamsT<T> P, const int4* __restrict__ tiles,
-                                                  const InstanceState* __restrict__ inst, FaceArraysT<T> F,
-                                                  DebugOutT<T> dbg) {
-  const int4 tl = tiles[blockIdx.x];
+template <typename T, int FLUX, bool DBG, int MINB>
+__global__ void __launch_bounds__(TX * TY, MINB) k_flux(ParamsT<T> P, const int4* __restrict__ tiles, int ntiles,
+                                                        const InstanceState* __restrict__ inst, FaceArraysT<T> F,
+                                                        DebugOutT<T> dbg) {
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  const int4 tl = tiles[tile];
   const E2DBlock* B = P.blocks + tl.x;
-  if (!inst[B->instance].active) return;
+  if (!inst[B->instance].active) continue;
   const int nx = B->nx, ny = B->ny;
   const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
   const int i = tl.y + ty, j = tl.z + tx;
-  if (i > ny || j > nx) return;
+  if (i > ny || j > nx) continue;
   const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
   const bool cart = B->is_cartesian != 0;
   if (i < ny) {
@@ -351,20 +356,22 @@ __global__ void __launch_bounds__(TX * TY) k_flux(ParamsT<T> P, const int4* __re
     T I[4] = {len * (T(2) * Fy[0]), len * (T(2) * Fy[1]), len * (T(2) * Fy[2]), len * (T(2) * Fy[3])};
     store4(F.hI, P.nhface, f, I);
   }
+  }  // tiles
 }
 
 // --------------------------------------------------------------------------------------
 // K3: divergence + RK stage program (+ positivity on the last stage)
 // --------------------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(TX * TY) k_update(ParamsT<T> P, const int4* __restrict__ tiles, FaceArraysT<T> F,
-                                                    StateBuffersT<T> S, StageProgram prog,
+__global__ void __launch_bounds__(TX * TY) k_update(ParamsT<T> P, const int4* __restrict__ tiles, int ntiles,
+                                                    FaceArraysT<T> F, StateBuffersT<T> S, StageProgram prog,
                                                     InstanceState* __restrict__ inst,
                                                     RealizState* __restrict__ real, T* __restrict__ dudt_out) {
-  const int4 tl = tiles[blockIdx.x];
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  const int4 tl = tiles[tile];
   const E2DBlock* B = P.blocks + tl.x;
   const InstanceState* I = inst + B->instance;
-  if (!I->active) return;
+  if (!I->active) continue;
   const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
   const int i = tl.y + ty, j = tl.z + tx;
   const bool live = i < B->ny && j < B->nx;
@@ -422,6 +429,7 @@ __global__ void __launch_bounds__(TX * TY) k_update(ParamsT<T> P, const int4* __
     const int nb = __syncthreads_count(bad);
     if (threadIdx.x == 0 && nb) atomicAdd(&real->nbad, (unsigned long long)nb);
   }
+  }  // tiles
 }
 
 // --------------------------------------------------------------------------------------
@@ -486,60 +494,124 @@ __global__ void k_realizable(ParamsT<T> P, const int4* __restrict__ tiles, const
 
 namespace e2d {
 // ---- launchers ------------------------------------------------------------------------
-template <typename T, int LIM, int RECON>
-static cudaError_t recon_lim_recon(const ParamsT<T>& P, const int4* tiles, int n, const T* U,
-                                   const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>* dbg,
-                                   cudaStream_t st) {
-  if (dbg) k_reconstruct<T, LIM, RECON, true><<<n, TX * TY, 0, st>>>(P, tiles, U, inst, F, *dbg);
-  else k_reconstruct<T, LIM, RECON, false><<<n, TX * TY, 0, st>>>(P, tiles, U, inst, F, DebugOutT<T>{});
+// Kernel variants the autotuner chooses from (e2d_autotune): tile height and the
+// occupancy target of __launch_bounds__ for k_reconstruct, the occupancy target for
+// k_flux, and for every kernel an optional persistent grid (one wave of resident CTAs
+// striding over the tile table).
+template <typename T, int LIM, int RECON, bool DBG, int RTY, int MINB>
+static cudaError_t recon_launch(const ParamsT<T>& P, const int4* tiles, int n, int grid, const T* U,
+                                const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>& dbg, cudaStream_t st) {
+  auto kern = k_reconstruct<T, LIM, RECON, DBG, RTY, MINB>;
+  if (grid <= 0) {  // persistent: resident CTAs per SM x SMs
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, TX * RTY, 0);
+    grid = sms * (per > 0 ? per : 1);
+  }
+  if (grid > n) grid = n;
+  kern<<<grid, TX * RTY, 0, st>>>(P, tiles, n, U, inst, F, dbg);
   return cudaGetLastError();
+}
+
+template <typename T, int LIM, int RECON>
+static cudaError_t recon_variant(const ParamsT<T>& P, const int4* const* tiles_by_rty, const int* n_by_rty,
+                                 int variant, bool persistent, const T* U, const InstanceState* inst, FaceArraysT<T> F,
+                                 const DebugOutT<T>* dbg, cudaStream_t st) {
+  if (dbg)  // the per-operator outputs are built for the default variant only
+    return recon_launch<T, LIM, RECON, true, 8, 1>(P, tiles_by_rty[1], n_by_rty[1], n_by_rty[1], U, inst, F, *dbg, st);
+  const DebugOutT<T> none{};
+  switch (variant) {
+    case 1: return recon_launch<T, LIM, RECON, false, 8, 2>(P, tiles_by_rty[1], n_by_rty[1], persistent ? 0 : n_by_rty[1], U, inst, F, none, st);
+    case 2: return recon_launch<T, LIM, RECON, false, 4, 2>(P, tiles_by_rty[0], n_by_rty[0], persistent ? 0 : n_by_rty[0], U, inst, F, none, st);
+    case 3: return recon_launch<T, LIM, RECON, false, 4, 4>(P, tiles_by_rty[0], n_by_rty[0], persistent ? 0 : n_by_rty[0], U, inst, F, none, st);
+    case 4: return recon_launch<T, LIM, RECON, false, 16, 1>(P, tiles_by_rty[2], n_by_rty[2], persistent ? 0 : n_by_rty[2], U, inst, F, none, st);
+    default: return recon_launch<T, LIM, RECON, false, 8, 1>(P, tiles_by_rty[1], n_by_rty[1], persistent ? 0 : n_by_rty[1], U, inst, F, none, st);
+  }
 }
 
 template <typename T, int LIM>
-static cudaError_t recon_lim(const ParamsT<T>& P, const int4* tiles, int n, const T* U, const InstanceState* inst,
-                             FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st) {
+static cudaError_t recon_lim(const ParamsT<T>& P, const int4* const* tiles, const int* n, int variant, bool persistent,
+                             const T* U, const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>* dbg,
+                             cudaStream_t st) {
   if (P.recon == E2D_RECON_PRIMITIVE)
-    return recon_lim_recon<T, LIM, E2D_RECON_PRIMITIVE>(P, tiles, n, U, inst, F, dbg, st);
-  return recon_lim_recon<T, LIM, E2D_RECON_CONSERVATIVE>(P, tiles, n, U, inst, F, dbg, st);
+    return recon_variant<T, LIM, E2D_RECON_PRIMITIVE>(P, tiles, n, variant, persistent, U, inst, F, dbg, st);
+  return recon_variant<T, LIM, E2D_RECON_CONSERVATIVE>(P, tiles, n, variant, persistent, U, inst, F, dbg, st);
 }
 
 template <typename T>
-cudaError_t launch_reconstruct(const ParamsT<T>& P, const int4* tiles, int n, const T* U, const InstanceState* inst,
-                               FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st) {
-  if (n <= 0) return cudaSuccess;
+cudaError_t launch_reconstruct(const ParamsT<T>& P, const TileSet& ts, KernelChoice kc, const T* U,
+                               const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st) {
+  const int4* tiles[3] = {ts.cell[0], ts.cell[1], ts.cell[2]};
+  if (ts.ncell[1] <= 0) return cudaSuccess;
   switch (P.limiter) {
-    case E2D_LIM_BARTH_JESPERSEN: return recon_lim<T, E2D_LIM_BARTH_JESPERSEN>(P, tiles, n, U, inst, F, dbg, st);
-    case E2D_LIM_VAN_ALBADA: return recon_lim<T, E2D_LIM_VAN_ALBADA>(P, tiles, n, U, inst, F, dbg, st);
-    case E2D_LIM_VAN_LEER: return recon_lim<T, E2D_LIM_VAN_LEER>(P, tiles, n, U, inst, F, dbg, st);
-    default: return recon_lim<T, E2D_LIM_VENKATAKRISHNAN>(P, tiles, n, U, inst, F, dbg, st);
+    case E2D_LIM_BARTH_JESPERSEN:
+      return recon_lim<T, E2D_LIM_BARTH_JESPERSEN>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st);
+    case E2D_LIM_VAN_ALBADA:
+      return recon_lim<T, E2D_LIM_VAN_ALBADA>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st);
+    case E2D_LIM_VAN_LEER:
+      return recon_lim<T, E2D_LIM_VAN_LEER>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st);
+    default:
+      return recon_lim<T, E2D_LIM_VENKATAKRISHNAN>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st);
   }
 }
 
-template <typename T, int FLUX>
-static cudaError_t flux_t(const ParamsT<T>& P, const int4* tiles, int n, const InstanceState* inst,
-                          FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st) {
-  if (dbg) k_flux<T, FLUX, true><<<n, TX * TY, 0, st>>>(P, tiles, inst, F, *dbg);
-  else k_flux<T, FLUX, false><<<n, TX * TY, 0, st>>>(P, tiles, inst, F, DebugOutT<T>{});
+template <typename T, int FLUX, bool DBG, int MINB>
+static cudaError_t flux_launch(const ParamsT<T>& P, const int4* tiles, int n, bool persistent,
+                               const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>& dbg, cudaStream_t st) {
+  auto kern = k_flux<T, FLUX, DBG, MINB>;
+  int grid = n;
+  if (persistent) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, TX * TY, 0);
+    grid = sms * (per > 0 ? per : 1);
+    if (grid > n) grid = n;
+  }
+  kern<<<grid, TX * TY, 0, st>>>(P, tiles, n, inst, F, dbg);
   return cudaGetLastError();
 }
 
-template <typename T>
-cudaError_t launch_flux(const ParamsT<T>& P, const int4* tiles, int n, const InstanceState* inst, FaceArraysT<T> F,
-                        const DebugOutT<T>* dbg, cudaStream_t st) {
-  if (n <= 0) return cudaSuccess;
-  switch (P.flux) {
-    case E2D_FLUX_HLLL: return flux_t<T, E2D_FLUX_HLLL>(P, tiles, n, inst, F, dbg, st);
-    case E2D_FLUX_HLLE: return flux_t<T, E2D_FLUX_HLLE>(P, tiles, n, inst, F, dbg, st);
-    default: return flux_t<T, E2D_FLUX_ROE>(P, tiles, n, inst, F, dbg, st);
+template <typename T, int FLUX>
+static cudaError_t flux_t(const ParamsT<T>& P, const int4* tiles, int n, KernelChoice kc, const InstanceState* inst,
+                          FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st) {
+  if (dbg) return flux_launch<T, FLUX, true, 1>(P, tiles, n, false, inst, F, *dbg, st);
+  const DebugOutT<T> none{};
+  switch (kc.variant) {
+    case 1: return flux_launch<T, FLUX, false, 2>(P, tiles, n, kc.persistent, inst, F, none, st);
+    case 2: return flux_launch<T, FLUX, false, 3>(P, tiles, n, kc.persistent, inst, F, none, st);
+    default: return flux_launch<T, FLUX, false, 1>(P, tiles, n, kc.persistent, inst, F, none, st);
   }
 }
 
 template <typename T>
-cudaError_t launch_update(const ParamsT<T>& P, const int4* tiles, int n, FaceArraysT<T> F, StateBuffersT<T> S,
-                          const StageProgram& prog, InstanceState* inst, RealizState* real, T* dudt_out,
-                          cudaStream_t st) {
+cudaError_t launch_flux(const ParamsT<T>& P, const TileSet& ts, KernelChoice kc, const InstanceState* inst,
+                        FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st) {
+  if (ts.nface <= 0) return cudaSuccess;
+  switch (P.flux) {
+    case E2D_FLUX_HLLL: return flux_t<T, E2D_FLUX_HLLL>(P, ts.face, ts.nface, kc, inst, F, dbg, st);
+    case E2D_FLUX_HLLE: return flux_t<T, E2D_FLUX_HLLE>(P, ts.face, ts.nface, kc, inst, F, dbg, st);
+    default: return flux_t<T, E2D_FLUX_ROE>(P, ts.face, ts.nface, kc, inst, F, dbg, st);
+  }
+}
+
+template <typename T>
+cudaError_t launch_update(const ParamsT<T>& P, const TileSet& ts, KernelChoice kc, FaceArraysT<T> F,
+                          StateBuffersT<T> S, const StageProgram& prog, InstanceState* inst, RealizState* real,
+                          T* dudt_out, cudaStream_t st) {
+  const int n = ts.ncell[1];
   if (n <= 0) return cudaSuccess;
-  k_update<T><<<n, TX * TY, 0, st>>>(P, tiles, F, S, prog, inst, real, dudt_out);
+  int grid = n;
+  if (kc.persistent) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_update<T>, TX * TY, 0);
+    grid = sms * (per > 0 ? per : 1);
+    if (grid > n) grid = n;
+  }
+  k_update<T><<<grid, TX * TY, 0, st>>>(P, ts.cell[1], n, F, S, prog, inst, real, dudt_out);
   return cudaGetLastError();
 }
 
@@ -560,12 +632,14 @@ cudaError_t launch_realizable(const ParamsT<T>& P, const int4* tiles, int n, con
 }
 
 #define E2D_INSTANTIATE_STAGE_LAUNCHERS(T)                                                                       \
-  template cudaError_t launch_reconstruct<T>(const ParamsT<T>&, const int4*, int, const T*, const InstanceState*, \
-                                             FaceArraysT<T>, const DebugOutT<T>*, cudaStream_t);                 \
-  template cudaError_t launch_flux<T>(const ParamsT<T>&, const int4*, int, const InstanceState*, FaceArraysT<T>,  \
-                                      const DebugOutT<T>*, cudaStream_t);                                        \
-  template cudaError_t launch_update<T>(const ParamsT<T>&, const int4*, int, FaceArraysT<T>, StateBuffersT<T>,    \
-                                        const StageProgram&, InstanceState*, RealizState*, T*, cudaStream_t);    \
+  template cudaError_t launch_reconstruct<T>(const ParamsT<T>&, const TileSet&, KernelChoice, const T*,          \
+                                             const InstanceState*, FaceArraysT<T>, const DebugOutT<T>*,          \
+                                             cudaStream_t);                                                      \
+  template cudaError_t launch_flux<T>(const ParamsT<T>&, const TileSet&, KernelChoice, const InstanceState*,     \
+                                      FaceArraysT<T>, const DebugOutT<T>*, cudaStream_t);                        \
+  template cudaError_t launch_update<T>(const ParamsT<T>&, const TileSet&, KernelChoice, FaceArraysT<T>,         \
+                                        StateBuffersT<T>, const StageProgram&, InstanceState*, RealizState*, T*, \
+                                        cudaStream_t);                                                           \
   template cudaError_t launch_dt<T>(const ParamsT<T>&, const int4*, int, const T*, InstanceState*, cudaStream_t); \
   template cudaError_t launch_realizable<T>(const ParamsT<T>&, const int4*, int, const T*, RealizState*, cudaStream_t);
 

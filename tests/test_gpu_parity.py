@@ -89,3 +89,27 @@ def test_run_stops_at_t_final():
     assert t == tf == t_or
     assert steps == len(dts)
     assert np.array_equal(S.get_state(), Ut)
+
+
+@pytest.mark.parametrize("kernel,variants", [(0, range(5)), (1, range(3)), (2, range(1))])
+@pytest.mark.parametrize("persistent", [False, True])
+def test_kernel_variants_bitwise(kernel, variants, persistent):
+    """Every autotuner variant (tile height, occupancy target, persistent grid)
+    computes the same values."""
+    z = G.load("m2x4_40")
+    for v in variants:
+        P, S = _solver(z)
+        S.set_kernel_choice(kernel, v, persistent)
+        S.set_state(P.to_soa(list(z["ic"])))
+        t, steps = S.run(0.0, G.t_final(z), max_steps=4)
+        assert G.fingerprint(P.from_soa(S.get_state())) == str(z["fingerprints"][3]), (kernel, v, persistent)
+
+
+def test_autotuned_run_bitwise():
+    z = G.load("p100")
+    P, S = _solver(z)
+    S.set_state(P.to_soa(list(z["ic"])))
+    choice = S.autotune(reps=2)
+    assert set(choice) == {"reconstruct", "flux", "update"}
+    t, steps = S.run(0.0, G.t_final(z), max_steps=10)
+    assert G.fingerprint(P.from_soa(S.get_state())) == str(z["fingerprints"][9])
