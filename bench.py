@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=1, help="RK4 steps in the CPU-baseline sample")
     ap.add_argument("--skip-cpu-baseline", action="store_true", help="omit the CPU baseline (profiling runs)")
     ap.add_argument("--skip-ensemble", action="store_true", help="omit the batched-ensemble section")
+    ap.add_argument("--skip-adjoint", action="store_true", help="omit the adjoint section")
     ap.add_argument("--workload", default="multiblock", choices=["multiblock", "ensemble"],
                     help="'ensemble' runs the full 512-instance, 200-step batched comparison instead")
     return ap.parse_args()
@@ -245,40 +246,50 @@ def ensemble_section(stream, full: bool = False, autotune: bool = True):
     out = {"workload": "512 instances, nx,ny in {64..512} (seed 0), explosion IC, Roe/Venkatakrishnan, SSP-RK2, "
                        "CFL 0.5, per-instance dt", "cells": cells}
 
-    def timed(solver, steps):
+    halted = {"fp32": set(), "fp64": set()}
+
+    def timed(solver, steps, key=None):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        solver.device.run(0.0, float("inf"), max_steps=steps)
+        bad = solver.run(steps)
         e1.record(stream)
         torch.cuda.synchronize()
+        if key:
+            halted[key].update(bad)
         return e0.elapsed_time(e1)
 
     E32 = EnsembleSolver(inst, precision=1, problem=P)
     E32.device.set_stream(stream.cuda_stream)
     if autotune:
         out["fp32_autotune"] = E32.device.autotune(reps=2)
-    E32.device.run(0.0, float("inf"), max_steps=w)
-    ms32 = timed(E32, k32)
+    halted["fp32"].update(E32.run(w))
+    ms32 = timed(E32, k32, "fp32")
     out["fp32_batched"] = {"value": cells * stages * k32 / (ms32 * 1e-3), "unit": "cell-stage updates/s",
                            "steps": k32, "ms_per_step": ms32 / k32}
     E64 = EnsembleSolver(inst, precision=0, problem=P)
     E64.device.set_stream(stream.cuda_stream)
-    E64.device.run(0.0, float("inf"), max_steps=w)
-    ms64 = timed(E64, k64)
+    halted["fp64"].update(E64.run(w))
+    ms64 = timed(E64, k64, "fp64")
     out["fp64_batched"] = {"value": cells * stages * k64 / (ms64 * 1e-3), "unit": "cell-stage updates/s",
                            "steps": k64, "ms_per_step": ms64 / k64}
     if w + k64 < w + k32:
-        E64.device.run(0.0, float("inf"), max_steps=k32 - k64)
+        halted["fp64"].update(E64.run(k32 - k64))
     a, b = E64.states(), E32.states()
-    l1 = [float(np.sum(np.abs(y[:, :, 0] - x[:, :, 0])) / np.sum(np.abs(x[:, :, 0]))) for x, y in zip(a, b)]
-    out["fp32_l1_density_rel_vs_fp64"] = {"after_steps": w + k32, "mean": float(np.mean(l1)), "max": float(np.max(l1))}
+    bad = halted["fp32"] | halted["fp64"]
+    l1 = [float(np.sum(np.abs(y[:, :, 0] - x[:, :, 0])) / np.sum(np.abs(x[:, :, 0])))
+          for k, (x, y) in enumerate(zip(a, b)) if k not in bad]
+    out["fp32_l1_density_rel_vs_fp64"] = {"after_steps": w + k32, "mean": float(np.mean(l1)), "max": float(np.max(l1)),
+                                           "median": float(np.median(l1)), "instances": len(l1)}
+    out["halted_unrealizable"] = {"fp32": sorted(halted["fp32"]), "fp64": sorted(halted["fp64"]),
+                                  "note": "the reference scheme reaches NaN on these instances (checked in the CPU "
+                                          "oracle for instance 265); they are excluded from the L1 statistics"}
     # FP64 instances one after another (each its own device problem)
     nseq = 512 if full else 16
     seq_ms, seq_cells = 0.0, 0
     for one in inst[:nseq]:
         S = EnsembleSolver([one], precision=0)
         S.device.set_stream(stream.cuda_stream)
-        S.device.run(0.0, float("inf"), max_steps=1)
+        S.run(1)
         seq_ms += timed(S, k64)
         seq_cells += S.problem.ncell
         S.device.close()
@@ -287,6 +298,76 @@ def ensemble_section(stream, full: bool = False, autotune: bool = True):
     out["fp32_batched_over_fp64_sequential"] = out["fp32_batched"]["value"] / out["fp64_sequential"]["value"]
     E32.device.close()
     E64.device.close()
+    return out
+
+
+def adjoint_section(stream, nsteps: int = 400, ckpt: int = 20, n: int = 256, fd: bool = True):
+    """Adjoint configuration: one 256 x 256 block on [0,10]^2, Reflection sides,
+    Roe/Venkatakrishnan, RK4 at CFL 0.5, 400 steps; tanh-edged explosion with
+    (r, w, cx) = (4, 2, 5); J = sum_n dt_n * (pressure integral along the north wall).
+    Times the recorded forward pass, the reverse pass (segment recompute + reverse
+    kernels) and a plain forward run of the same steps; checks dJ/d(r, w, cx) against
+    central differences (h = 1e-6) at the frozen dt schedule."""
+    import numpy as np
+    import torch
+
+    from pyhype_gb300.adjoint import AdjointSolver, adjoint_problem, smoothed_explosion
+
+    P = adjoint_problem(n=n)
+    A = AdjointSolver(P, "RK4", side="N", nsteps=nsteps, ckpt_every=ckpt)
+    A.device.set_stream(stream.cuda_stream)
+    theta = torch.tensor([4.0, 2.0, 5.0], dtype=torch.float64, device="cuda", requires_grad=True)
+    with torch.cuda.stream(stream):
+        U0 = smoothed_explosion(P, theta[0], theta[1], theta[2])
+    U0d = U0.detach().clone()
+    # warm-up (first-touch allocations of the checkpoint and segment storage)
+    A.forward(U0d)
+    A.backward()
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    e0, e1, e2 = ev(), ev(), ev()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    J = A.forward(U0d)
+    e1.record(stream)
+    A.backward()
+    e2.record(stream)
+    torch.cuda.synchronize()
+    t_fwd, t_bwd = e0.elapsed_time(e1), e1.elapsed_time(e2)
+    # plain forward of the same steps (captured-graph device loop)
+    A.device.set_state_device(U0d.data_ptr())
+    f0, f1 = ev(), ev()
+    f0.record(stream)
+    A.device.run(0.0, float("inf"), max_steps=nsteps)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    t_plain = f0.elapsed_time(f1)
+    out = {"workload": f"{n}x{n} block on [0,10]^2, Reflection, Roe/Venkatakrishnan, RK4, CFL 0.5, {nsteps} steps, "
+                       f"checkpoints every {ckpt}; tanh-edged explosion (r, w, cx) = (4, 2, 5); "
+                       "J = sum dt * north-wall pressure integral",
+           "J": J, "forward_recorded_ms": t_fwd, "backward_ms": t_bwd, "plain_forward_ms": t_plain,
+           "adjoint_cost_over_forward": t_bwd / t_plain,
+           "adjoint_cost_over_recorded_forward": t_bwd / t_fwd}
+    if fd:
+        J1 = A.objective(smoothed_explosion(P, theta[0], theta[1], theta[2]))
+        J1.backward()
+        grad = theta.grad.cpu().numpy()
+        dts = A.dts.copy()
+        h = 1e-6
+        res = {}
+        for k, name in enumerate(("r", "w", "cx")):
+            tp, tm = theta.detach().clone(), theta.detach().clone()
+            tp[k] += h
+            tm[k] -= h
+            Jp = A.forward(smoothed_explosion(P, tp[0], tp[1], tp[2]), dts)
+            Jm = A.forward(smoothed_explosion(P, tm[0], tm[1], tm[2]), dts)
+            fdv = (Jp - Jm) / (2 * h)
+            res[name] = {"adjoint": float(grad[k]), "central_difference": fdv,
+                         "rel_err": abs(fdv - grad[k]) / abs(grad[k])}
+        out["fd_check_h1e-6"] = res
+    A.device.close()
     return out
 
 
@@ -440,19 +521,18 @@ def main():
         g1.record(stream)
         torch.cuda.synchronize()
         ms32 = max_over_ranks(g0.elapsed_time(g1), ws)
-        k32 = np.zeros(5)
-        c32 = np.zeros(5, dtype=np.int64)
-        L.e2d_bench_kernels(S32.h, 2, k32.ctypes.data, c32.ctypes.data)
-        U64 = dev.get_state()
+        U32 = S32.get_state()
         # the FP64 solver has taken e2e steps more; rerun FP64 to the same step count
         S64b = _native.DeviceSolver(P, tableau=solver._time_integrator.tableau())
         S64b.set_stream(stream.cuda_stream)
         S64b.set_state(P.to_soa([b.state.data for b in solver.blocks]))
         S64b.run(0.0, t_final, max_steps=args.warmup + args.steps)
         U64 = S64b.get_state()
-        S32.run(t32, t_final, max_steps=0)
-        U32 = S32.get_state()
         l1 = float(np.sum(np.abs(U32[0] - U64[0])) / np.sum(np.abs(U64[0])))
+        # per-kernel timing advances the FP32 state further: after the comparison
+        k32 = np.zeros(5)
+        c32 = np.zeros(5, dtype=np.int64)
+        L.e2d_bench_kernels(S32.h, 2, k32.ctypes.data, c32.ctypes.data)
         fp32 = {"value": ws * P.ncell * stages * args.steps / (ms32 * 1e-3), "unit": "cell-stage updates/s",
                 "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": ms / ms32,
                 "l1_density_rel_vs_fp64": l1, "l1_after_steps": args.warmup + args.steps,
@@ -469,6 +549,13 @@ def main():
             ensemble["fp32_batched_over_fp64_plain"] = ensemble["fp32_batched"]["value"] / value
         except Exception as exc:
             ensemble = {"error": str(exc)}
+
+    adjoint = None
+    if not args.skip_adjoint and ws == 1:
+        try:
+            adjoint = adjoint_section(stream)
+        except Exception as exc:
+            adjoint = {"error": str(exc)}
 
     clocks = clk.summary()
     line = {
@@ -504,6 +591,7 @@ def main():
         },
         "fp32": fp32,
         "ensemble": ensemble,
+        "adjoint": adjoint,
         "gpu_launches": int(args.steps * (3 + 3 * stages)),
         "clocks": clocks,
     }

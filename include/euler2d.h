@@ -222,6 +222,9 @@ E2D_API int e2d_step(E2DHandle h, double dt, double t);
 /* The Euler2D._solve loop (pyhype/solvers/Euler2D.py:361-376): dt -> clamp to
    t_final - t -> step -> realizability, until t >= t_final or max_steps.  Time is
    non-dimensional (t_final already multiplied by a_inf).  *t_inout is updated.
+   With several instances, *t_inout is ignored on entry (every instance continues
+   from its own time, 0 after e2d_create) and receives instance 0's time; max_steps
+   counts the steps of this call per instance.
    Returns E2D_ERR_UNREALIZABLE (with *real filled) if a step produced rho<=0 or
    E<=0.                                                                            */
 E2D_API int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps,
@@ -236,6 +239,38 @@ E2D_API int e2d_instance_times(E2DHandle h, double* t_out, int32_t* steps_out);
    at solver time t (time-dependent sides) into a caller device buffer of 4 cell
    planes; optional intermediates in dbg.                                           */
 E2D_API int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* dbg);
+
+/* ---- adjoint (reverse mode) -------------------------------------------------------
+   No counterpart in the reference (it has no differentiation); the forward steps are
+   the functions above.  FP64 path, Roe flux, one instance; any limiter,
+   reconstruction type, side kind and explicit tableau.  Subgradients: min/max take the
+   operand the forward selects, Harten's fix the branch taken, the slope's davg == 0
+   branch is constant, a clipped negative limiter value passes nothing back.        */
+
+/* Objective J = sum over steps n of dt_n * P(U^{n+1}), where P(U) sums, over the cells
+   along side `side` (e2d_side) of block `block`, the cell pressure times the length
+   of the cell's boundary face.                                                      */
+typedef struct {
+  int32_t block;
+  int32_t side;
+} E2DPressureObjective;
+
+/* out_dev = (dR/dU)^T lam_dev at the current state and solver time t, R the residual
+   of e2d_residual; both 4 cell planes on the device.                               */
+E2D_API int e2d_residual_vjp(E2DHandle h, double t, const double* lam_dev, double* out_dev);
+/* Recorded forward pass: nsteps RK steps from the current state at time t0, keeping
+   the state every ckpt_every steps.  dts_in == NULL takes each step's CFL dt (no
+   t_final clamp) and writes the schedule to dts_out (nsteps entries, may be NULL);
+   otherwise the given schedule is replayed (finite differences at a frozen dt).
+   *J_out receives J.  Device memory: ceil(nsteps/ckpt_every) states plus, for
+   ckpt_every steps x stages, one state and one set of face states.               */
+E2D_API int e2d_adjoint_forward(E2DHandle h, double t0, int32_t nsteps, int32_t ckpt_every,
+                                const E2DPressureObjective* obj, const double* dts_in, double* dts_out,
+                                double* J_out);
+/* Reverse pass of the last recorded forward pass at its dt schedule: grad_dev (4 cell
+   planes, device) = dJ/dU^0.  Segments between checkpoints are recomputed.  The
+   current state is U^N afterwards.                                                  */
+E2D_API int e2d_adjoint_backward(E2DHandle h, double* grad_dev);
 
 /* ---- allocation-free CFL time step ----------------------------------------------
    No counterpart in the reference.  For callers that may not allocate device

@@ -12,7 +12,7 @@ from typing import Optional
 
 import numpy as np
 
-from .problem import E2DDebug, E2DRealizability, Problem, c_double_p
+from .problem import E2DDebug, E2DPressureObjective, E2DRealizability, Problem, c_double_p
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libeuler2d.so")
@@ -30,6 +30,7 @@ EXPORTS = (
     "e2d_abi_version", "e2d_last_error", "e2d_create", "e2d_destroy", "e2d_set_stream", "e2d_num_cells",
     "e2d_set_state", "e2d_get_state", "e2d_set_state_device", "e2d_get_state_device", "e2d_set_tableau",
     "e2d_compute_dt", "e2d_step", "e2d_run", "e2d_check_realizable", "e2d_residual", "e2d_instance_times",
+    "e2d_residual_vjp", "e2d_adjoint_forward", "e2d_adjoint_backward",
 )
 
 
@@ -79,6 +80,10 @@ def load(path: Optional[str] = None):
     L.e2d_set_kernel_choice.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
     L.e2d_autotune.argtypes = [vp, ctypes.c_int32, vp]
     L.e2d_residual.argtypes = [vp, ctypes.c_double, vp, vp]
+    L.e2d_residual_vjp.argtypes = [vp, ctypes.c_double, vp, vp]
+    L.e2d_adjoint_forward.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, vp, vp,
+                                      ctypes.POINTER(ctypes.c_double)]
+    L.e2d_adjoint_backward.argtypes = [vp, vp]
     if L.e2d_abi_version() != 1:
         raise RuntimeError("libeuler2d.so ABI version mismatch")
     _lib = L
@@ -208,4 +213,44 @@ class DeviceSolver:
         out = dudt.cpu().numpy()
         if debug:
             return out, {k: v.cpu().numpy() for k, v in dbg_t.items()}
+        return out
+
+    # ---- adjoint ------------------------------------------------------------------------
+    def residual_vjp(self, lam, t: float = 0.0):
+        """(dR/dU)^T lam at the current state; lam and the result are device tensors of
+        shape (4, ncell) (FP64)."""
+        import torch
+
+        lam = lam.contiguous()
+        out = torch.empty_like(lam)
+        torch.cuda.synchronize()
+        _check(self.L.e2d_residual_vjp(self.h, float(t), ctypes.c_void_p(lam.data_ptr()),
+                                       ctypes.c_void_p(out.data_ptr())))
+        return out
+
+    def adjoint_forward(self, nsteps: int, ckpt_every: int, block: int, side: int, t0: float = 0.0,
+                        dts: Optional[np.ndarray] = None):
+        """Recorded forward pass of J = sum_n dt_n * P(U^{n+1}) (pressure integral along
+        one block side); returns (J, dt schedule).  ``dts`` replays a frozen schedule."""
+        obj = E2DPressureObjective(int(block), int(side))
+        out = np.zeros(nsteps)
+        J = ctypes.c_double(0.0)
+        din = None
+        if dts is not None:
+            dts = np.ascontiguousarray(dts, dtype=np.float64)
+            assert dts.shape == (nsteps,)
+            din = dts.ctypes.data
+        code = self.L.e2d_adjoint_forward(self.h, float(t0), int(nsteps), int(ckpt_every), ctypes.addressof(obj),
+                                          din, out.ctypes.data, ctypes.byref(J))
+        _check(code)
+        return J.value, (dts.copy() if dts is not None else out)
+
+    def adjoint_backward(self, out=None):
+        """dJ/dU^0 of the last recorded forward pass as a (4, ncell) FP64 device tensor."""
+        import torch
+
+        if out is None:
+            out = torch.empty((4, self.ncell), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        _check(self.L.e2d_adjoint_backward(self.h, ctypes.c_void_p(out.data_ptr())))
         return out

@@ -25,6 +25,7 @@ UNITS = {
     "e2d_api.cu": ["-fmad=false"],
     "e2d_bench.cu": [],
     "e2d_noalloc.cu": ["-fmad=false"],
+    "e2d_adjoint.cu": ["-fmad=false"],
 }
 
 

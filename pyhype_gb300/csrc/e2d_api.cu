@@ -12,7 +12,7 @@
 #include <string>
 #include <vector>
 
-#include "e2d_kernels.cuh"
+#include "e2d_solver.cuh"
 #include "../../include/euler2d_bench.h"
 
 using namespace e2d;
@@ -20,22 +20,6 @@ using namespace e2d;
 namespace {
 
 thread_local std::string g_err;
-
-int fail(int code, const char* fmt, ...) {
-  char buf[512];
-  va_list ap;
-  va_start(ap, fmt);
-  vsnprintf(buf, sizeof buf, fmt, ap);
-  va_end(ap);
-  g_err = buf;
-  return code;
-}
-
-#define CK(call)                                                                          \
-  do {                                                                                    \
-    cudaError_t e_ = (call);                                                              \
-    if (e_ != cudaSuccess) return fail(E2D_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
-  } while (0)
 
 __global__ void k_reset_min(InstanceState* inst, int n) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -50,83 +34,11 @@ __global__ void k_reset_real(RealizState* r) {
 }  // namespace
 
 namespace e2d {
-// records the thread-local message returned by e2d_last_error (used by other units)
 int set_error(int code, const char* msg) {
   g_err = msg;
   return code;
 }
 }  // namespace e2d
-
-// Everything that has the arithmetic type of a path: parameters (with the geometry
-// plane pointers), face arrays and state buffers.
-template <typename T>
-struct PathT {
-  ParamsT<T> P{};
-  T* geo = nullptr;
-  FaceArraysT<T> F{};
-  StateBuffersT<T> S{};
-  T* dudt_tmp = nullptr;  // FP32 residual staging for the FP64 caller buffer
-};
-
-struct E2DSolver {
-  int device = 0;
-  cudaStream_t own = nullptr;
-  cudaStream_t stream = nullptr;
-  E2DConfig cfg{};
-  int prec = E2D_FP64;
-  std::vector<E2DBlock> hblocks;
-  PathT<double> pd;
-  PathT<float> pf;
-  E2DBlock* dblocks = nullptr;
-  std::vector<void*> allocs;
-  int4* cell_tiles = nullptr;   // tile height 8 (dt, update, default reconstruct)
-  int ncell_tiles = 0;
-  int4* face_tiles = nullptr;
-  int nface_tiles = 0;
-  TileSet ts{};                  // all tile tables (heights 4, 8, 16)
-  KernelChoice kr{0, false};     // reconstruct variant (autotuned)
-  KernelChoice kf{0, false};     // flux variant
-  KernelChoice ku{0, false};     // update variant
-  int nbuf = 0;
-  InstanceState* inst = nullptr;
-  std::vector<InstanceState> hinst;
-  RealizState* real = nullptr;
-  int nstages = 0;
-  std::vector<StageProgram> prog;
-  std::vector<int> stage_input;
-  // captured step graphs, keyed by the number of steps they replay
-  std::vector<std::pair<int, cudaGraphExec_t>> graphs;
-  int64_t ncell = 0, nvface = 0, nhface = 0;
-
-  void drop_graphs() {
-    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
-    graphs.clear();
-  }
-  ~E2DSolver() {
-    drop_graphs();
-    for (void* p : allocs) cudaFree(p);
-    if (own) cudaStreamDestroy(own);
-  }
-  template <typename T>
-  int alloc(T** p, size_t count) {
-    void* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, sizeof(T) * (count ? count : 1));
-    if (e != cudaSuccess) return fail(E2D_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", sizeof(T) * count, cudaGetErrorString(e));
-    allocs.push_back(q);
-    *p = static_cast<T*>(q);
-    return 0;
-  }
-};
-
-template <typename T>
-PathT<T>& path(E2DSolver* h);
-template <>
-PathT<double>& path<double>(E2DSolver* h) { return h->pd; }
-template <>
-PathT<float>& path<float>(E2DSolver* h) { return h->pf; }
-
-// Run f<T>(h) for the handle's precision.
-#define E2D_DISPATCH(h, f, ...) ((h)->prec == E2D_FP32 ? f<float>(h, ##__VA_ARGS__) : f<double>(h, ##__VA_ARGS__))
 
 // Stage program of a Butcher tableau (rows = stages; row s uses k_0..k_s).  Buffer 0
 // holds U^n and, after the last stage, U^{n+1}; buffer r+1 holds row r's partial sum
@@ -280,6 +192,7 @@ static int bench_kernels_t(E2DHandle h, int32_t steps, double* ms, int64_t* laun
     I.max_steps = 0x7fffffff;
     I.steps = 0;
     I.halted = 0;
+    I.nbad = 0;
     I.min_bits = 0x7ff0000000000000ULL;
   }
   CK(cudaMemcpyAsync(h->inst, h->hinst.data(), sizeof(InstanceState) * ninst, cudaMemcpyHostToDevice, h->stream));
@@ -361,7 +274,11 @@ static int time_kernel(E2DHandle h, int which, int reps, float* ms) {
 template <typename T>
 static int autotune_t(E2DHandle h, int reps, int32_t* chosen) {
   const int ninst = (int)h->hinst.size();
-  CK(launch_set_time(h->inst, ninst, h->hinst.empty() ? 0.0 : h->hinst[0].t, 0.0, h->stream));
+  // every instance active with dt = 0 while timing; the instance table is put back after
+  std::vector<InstanceState> saved(ninst);
+  CK(cudaMemcpyAsync(saved.data(), h->inst, sizeof(InstanceState) * ninst, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  CK(launch_set_time(h->inst, ninst, 0.0, 0.0, h->stream));
   KernelChoice* ch[3] = {&h->kr, &h->kf, &h->ku};
   const int nvar[3] = {N_RECON_VARIANTS, N_FLUX_VARIANTS, 1};
   for (int which = 0; which < 3; ++which) {
@@ -383,7 +300,7 @@ static int autotune_t(E2DHandle h, int reps, int32_t* chosen) {
       chosen[2 * which + 1] = best.persistent ? 1 : 0;
     }
   }
-  CK(launch_end_step(h->inst, ninst, h->real, h->stream));
+  CK(cudaMemcpyAsync(h->inst, saved.data(), sizeof(InstanceState) * ninst, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   h->drop_graphs();
   return 0;
@@ -613,6 +530,7 @@ int e2d_set_tableau(E2DHandle h, int32_t nstages, const double* a) {
     for (int c = r + 1; c < nstages; ++c)
       if (a[r * nstages + c] != 0.0) return fail(E2D_ERR_INVALID, "tableau must be lower triangular (explicit)");
   if (int e = build_program(h, nstages, a)) return e;
+  h->tableau.assign(a, a + (size_t)nstages * nstages);
   return ensure_buffers(h);
 }
 
@@ -630,10 +548,6 @@ static int enqueue_stages(E2DHandle h, T* dudt_out, const DebugOutT<T>* dbg) {
   }
   return 0;
 }
-
-extern "C" {
-
-}  // extern "C"
 
 template <typename T>
 static int enqueue_run_step_t(E2DHandle h) {
@@ -794,12 +708,18 @@ int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps, int
             E2DRealizability* realo) {
   if (!h || !t_inout) return fail(E2D_ERR_INVALID, "null argument");
   const int ninst = (int)h->hinst.size();
+  // one instance starts at *t_inout; a batch continues every instance from its own time
+  if (ninst > 1) {
+    CK(cudaMemcpyAsync(h->hinst.data(), h->inst, sizeof(InstanceState) * ninst, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
   for (auto& I : h->hinst) {
-    I.t = *t_inout;
+    if (ninst == 1) I.t = *t_inout;
     I.t_final = t_final;
     I.max_steps = max_steps;
     I.steps = 0;
     I.halted = 0;
+    I.nbad = 0;
     I.active = 0;
     I.min_bits = 0x7ff0000000000000ULL;
   }
@@ -820,7 +740,8 @@ int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps, int
       halted = halted || I.halted;
       any = any || (!I.halted && I.t < I.t_final && I.steps < I.max_steps);
     }
-    if (!any || halted) break;
+    // a batch keeps stepping its realizable instances; one instance stops
+    if (!any || (ninst == 1 && halted)) break;
   }
   *t_inout = h->hinst[0].t;
   if (steps_done) *steps_done = h->hinst[0].steps;

@@ -24,14 +24,14 @@ __global__ void k_begin_step(InstanceState* inst, int ninst, double cfl, int use
   I.min_bits = 0x7ff0000000000000ULL;
 }
 
-__global__ void k_end_step(InstanceState* inst, int ninst, const RealizState* real) {
+__global__ void k_end_step(InstanceState* inst, int ninst, const RealizState*) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= ninst) return;
   InstanceState& I = inst[q];
   if (I.active) {
     I.t = I.t + I.dt;
     I.steps += 1;
-    if (real->nbad) { I.halted = 1; }
+    if (I.nbad) I.halted = 1;
   }
   I.active = 0;
 }
@@ -42,6 +42,7 @@ __global__ void k_set_time(InstanceState* inst, int ninst, double t, double dt) 
   inst[q].t = t;
   inst[q].dt = dt;
   inst[q].active = 1;
+  inst[q].nbad = 0;
 }
 
 

@@ -44,6 +44,8 @@ struct InstanceState {
   int32_t steps;       // steps taken
   int32_t max_steps;
   int32_t halted;      // set when a step produced an unrealizable state
+  int32_t nbad;        // unrealizable cells found in this instance's last stage
+  int32_t pad_;
 };
 
 struct RealizState {
@@ -82,6 +84,14 @@ template <typename T>
 struct StateBuffersT {
   T* buf[MAX_STAGES + 1];   // 0 = U^n, 1.. = row partial sums
   T* comp;                  // Kahan compensation of U^n (FP32 path), else null
+  // buf[k] for a run-time k by compare-and-select (a dynamic index into a kernel
+  // parameter array would copy the array to local memory)
+  __device__ __forceinline__ T* at(int k) const {
+    T* p = buf[0];
+#pragma unroll
+    for (int q = 1; q <= MAX_STAGES; ++q) p = (k == q) ? buf[q] : p;
+    return p;
+  }
 };
 
 template <typename T>
@@ -114,8 +124,8 @@ struct KernelChoice {
   int variant;
   bool persistent;
 };
-constexpr int N_RECON_VARIANTS = 5;  // (tile height, min CTAs/SM): (8,1) (8,2) (4,2) (4,4) (16,1)
-constexpr int N_FLUX_VARIANTS = 3;   // min CTAs/SM: 1, 2, 3
+constexpr int N_RECON_VARIANTS = 5;  // (tile height, min CTAs/SM): (8,2) (8,1) (4,2) (4,4) (16,1)
+constexpr int N_FLUX_VARIANTS = 3;   // min CTAs/SM: 4, 1, 6
 
 // launchers, instantiated for double (e2d_fp64.cu) and float (e2d_fp32.cu)
 template <typename T>

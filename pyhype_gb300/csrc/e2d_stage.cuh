@@ -147,19 +147,16 @@ __device__ __forceinline__ void outside_state(const ParamsT<T>& P, const E2DBloc
 // --------------------------------------------------------------------------------------
 // K1: reconstruction
 // --------------------------------------------------------------------------------------
-template <typename T, int LIM, int RECON, bool DBG, int RTY, int MINB>
-__global__ void __launch_bounds__(TX * RTY, MINB) k_reconstruct(ParamsT<T> P, const int4* __restrict__ tiles,
-                                                                int ntiles, const T* __restrict__ U,
-                                                                const InstanceState* __restrict__ inst,
-                                                                FaceArraysT<T> F, DebugOutT<T> dbg) {
-  __shared__ T sW[4][RTY + 2][TX + 2];
+// One tile of cells: the body of k_reconstruct.  Returns early (uniformly per CTA)
+// for an inactive instance; the caller synchronises before sW is refilled.
+template <typename T, int LIM, int RECON, bool DBG, int RTY>
+__device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4 tl, const T* __restrict__ U,
+                                                 const InstanceState* __restrict__ inst, const FaceArraysT<T>& F,
+                                                 const DebugOutT<T>& dbg, T (&sW)[4][RTY + 2][TX + 2]) {
   const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
-  // a grid of ntiles CTAs does one tile each; a smaller (persistent) grid strides
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-  const int4 tl = tiles[tile];
   const E2DBlock* B = P.blocks + tl.x;
   const InstanceState* I = inst + B->instance;
-  if (!I->active) continue;
+  if (!I->active) return;
   const double t = I->t;
   const int nx = B->nx, ny = B->ny;
   const int i0 = tl.y, j0 = tl.z;
@@ -185,7 +182,7 @@ __global__ void __launch_bounds__(TX * RTY, MINB) k_reconstruct(ParamsT<T> P, co
 
   const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
   const int i = i0 + ty, j = j0 + tx;
-  if (i < ny && j < nx) {
+  if (i >= ny || j >= nx) return;
   const int64_t c = cell_at(B, i, j);
   const int64_t fE = vf_at(B, i, j + 1), fW = vf_at(B, i, j);
   const int64_t fN = hf_at(B, i + 1, j), fS = hf_at(B, i, j);
@@ -222,7 +219,18 @@ __global__ void __launch_bounds__(TX * RTY, MINB) k_reconstruct(ParamsT<T> P, co
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
       hot[s] = gx * hx[s] + gy * hy[s];
-      const T davg = (w0 + hot[s]) - w0;
+      T davg;
+      if constexpr (sizeof(T) == 4) {
+        // FP64's round trip (w0 + hot) - w0 is hot itself unless |hot| is below half
+        // an FP64 ulp of w0, where it is zero and the slope takes its davg == 0
+        // branch (psi(1)).  In FP32 the same round trip would zero every |hot| below
+        // 2^-25 |w0| and switch branches where the FP64 path does not, so the FP32 form
+        // applies the FP64 threshold, 2^-53 times the power of two of w0.
+        const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
+        davg = (fabs(hot[s]) < half_ulp64) ? T(0) : hot[s];
+      } else {
+        davg = (w0 + hot[s]) - w0;
+      }
       // slope dmax/davg (davg > 0), dmin/davg (davg < 0), 1 (davg == 0), with a single
       // division so lanes of different signs share one division sequence
       const bool pos = is_pos(davg), neg = is_neg(davg);
@@ -307,26 +315,39 @@ __global__ void __launch_bounds__(TX * RTY, MINB) k_reconstruct(ParamsT<T> P, co
     recon_to_prim<RECON>(o, G, w);
     store4(F.hR, P.nhface, fN, w);
   }
-  }  // live cell
-  __syncthreads();  // the next tile reuses sW
-  }  // tiles
+}
+
+// A grid of ntiles CTAs does one tile each (PERSIST false); a persistent grid of
+// resident CTAs strides over the tile table.  The two forms are separate
+// instantiations so the one-tile form carries no loop state in registers.
+template <typename T, int LIM, int RECON, bool DBG, int RTY, int MINB, bool PERSIST>
+__global__ void __launch_bounds__(TX * RTY, MINB) k_reconstruct(ParamsT<T> P, const int4* __restrict__ tiles,
+                                                                int ntiles, const T* __restrict__ U,
+                                                                const InstanceState* __restrict__ inst,
+                                                                FaceArraysT<T> F, DebugOutT<T> dbg) {
+  __shared__ T sW[4][RTY + 2][TX + 2];
+  if constexpr (!PERSIST) {
+    reconstruct_tile<T, LIM, RECON, DBG, RTY>(P, tiles[blockIdx.x], U, inst, F, dbg, sW);
+  } else {
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+      reconstruct_tile<T, LIM, RECON, DBG, RTY>(P, tiles[tile], U, inst, F, dbg, sW);
+      __syncthreads();  // the next tile refills sW
+    }
+  }
 }
 
 // --------------------------------------------------------------------------------------
 // K2: one Riemann flux per face
 // --------------------------------------------------------------------------------------
-template <typename T, int FLUX, bool DBG, int MINB>
-__global__ void __launch_bounds__(TX * TY, MINB) k_flux(ParamsT<T> P, const int4* __restrict__ tiles, int ntiles,
-                                                        const InstanceState* __restrict__ inst, FaceArraysT<T> F,
-                                                        DebugOutT<T> dbg) {
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-  const int4 tl = tiles[tile];
+template <typename T, int FLUX, bool DBG>
+__device__ __forceinline__ void flux_tile(const ParamsT<T>& P, const int4 tl, const InstanceState* __restrict__ inst,
+                                          const FaceArraysT<T>& F, const DebugOutT<T>& dbg) {
   const E2DBlock* B = P.blocks + tl.x;
-  if (!inst[B->instance].active) continue;
+  if (!inst[B->instance].active) return;
   const int nx = B->nx, ny = B->ny;
   const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
   const int i = tl.y + ty, j = tl.z + tx;
-  if (i > ny || j > nx) continue;
+  if (i > ny || j > nx) return;
   const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
   const bool cart = B->is_cartesian != 0;
   if (i < ny) {
@@ -356,22 +377,30 @@ __global__ void __launch_bounds__(TX * TY, MINB) k_flux(ParamsT<T> P, const int4
     T I[4] = {len * (T(2) * Fy[0]), len * (T(2) * Fy[1]), len * (T(2) * Fy[2]), len * (T(2) * Fy[3])};
     store4(F.hI, P.nhface, f, I);
   }
-  }  // tiles
+}
+
+template <typename T, int FLUX, bool DBG, int MINB, bool PERSIST>
+__global__ void __launch_bounds__(TX * TY, MINB) k_flux(ParamsT<T> P, const int4* __restrict__ tiles, int ntiles,
+                                                        const InstanceState* __restrict__ inst, FaceArraysT<T> F,
+                                                        DebugOutT<T> dbg) {
+  if constexpr (!PERSIST) {
+    flux_tile<T, FLUX, DBG>(P, tiles[blockIdx.x], inst, F, dbg);
+  } else {
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) flux_tile<T, FLUX, DBG>(P, tiles[tile], inst, F, dbg);
+  }
 }
 
 // --------------------------------------------------------------------------------------
 // K3: divergence + RK stage program (+ positivity on the last stage)
 // --------------------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(TX * TY) k_update(ParamsT<T> P, const int4* __restrict__ tiles, int ntiles,
-                                                    FaceArraysT<T> F, StateBuffersT<T> S, StageProgram prog,
-                                                    InstanceState* __restrict__ inst,
-                                                    RealizState* __restrict__ real, T* __restrict__ dudt_out) {
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-  const int4 tl = tiles[tile];
+__device__ __forceinline__ void update_tile(const ParamsT<T>& P, const int4 tl, const FaceArraysT<T>& F,
+                                            const StateBuffersT<T>& S, const StageProgram& prog,
+                                            InstanceState* __restrict__ inst, RealizState* __restrict__ real,
+                                            T* __restrict__ dudt_out) {
   const E2DBlock* B = P.blocks + tl.x;
   const InstanceState* I = inst + B->instance;
-  if (!I->active) continue;
+  if (!I->active) return;
   const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
   const int i = tl.y + ty, j = tl.z + tx;
   const bool live = i < B->ny && j < B->nx;
@@ -394,12 +423,14 @@ __global__ void __launch_bounds__(TX * TY) k_update(ParamsT<T> P, const int4* __
       for (int v = 0; v < 4; ++v) dudt_out[v * P.ncell + c] = k[v];
     }
     const double dt = I->dt;
-    for (int u = 0; u < prog.nupd; ++u) {
-      const StageUpdate up = prog.upd[u];
-      const T* src = S.buf[up.src];
+#pragma unroll
+    for (int u = 0; u < MAX_STAGES; ++u) {  // unrolled: the program is read from kernel parameters
+      if (u >= prog.nupd) break;
+      const StageUpdate& up = prog.upd[u];
+      const T* src = S.at(up.src);
       const T dta = T(dt * up.a);
       if (!up.kahan) {
-        T* dst = S.buf[up.dst];
+        T* dst = S.at(up.dst);
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
           const T base = up.src_zero ? T(0) : src[v * P.ncell + c];
@@ -427,9 +458,24 @@ __global__ void __launch_bounds__(TX * TY) k_update(ParamsT<T> P, const int4* __
   }
   if (prog.final_stage) {
     const int nb = __syncthreads_count(bad);
-    if (threadIdx.x == 0 && nb) atomicAdd(&real->nbad, (unsigned long long)nb);
+    if (threadIdx.x == 0 && nb) {
+      atomicAdd(&real->nbad, (unsigned long long)nb);
+      atomicAdd(&inst[B->instance].nbad, nb);  // halts this instance only
+    }
   }
-  }  // tiles
+}
+
+template <typename T, bool PERSIST>
+__global__ void __launch_bounds__(TX * TY) k_update(ParamsT<T> P, const int4* __restrict__ tiles, int ntiles,
+                                                    FaceArraysT<T> F, StateBuffersT<T> S, StageProgram prog,
+                                                    InstanceState* __restrict__ inst,
+                                                    RealizState* __restrict__ real, T* __restrict__ dudt_out) {
+  if constexpr (!PERSIST) {
+    update_tile<T>(P, tiles[blockIdx.x], F, S, prog, inst, real, dudt_out);
+  } else {
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+      update_tile<T>(P, tiles[tile], F, S, prog, inst, real, dudt_out);
+  }
 }
 
 // --------------------------------------------------------------------------------------
@@ -498,19 +544,26 @@ namespace e2d {
 // occupancy target of __launch_bounds__ for k_reconstruct, the occupancy target for
 // k_flux, and for every kernel an optional persistent grid (one wave of resident CTAs
 // striding over the tile table).
+// one wave of resident CTAs (resident CTAs per SM x SMs), at most n
+template <typename K>
+static int persistent_grid(K kern, int threads, int n) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, threads, 0);
+  const int g = sms * (per > 0 ? per : 1);
+  return g < n ? g : n;
+}
+
 template <typename T, int LIM, int RECON, bool DBG, int RTY, int MINB>
-static cudaError_t recon_launch(const ParamsT<T>& P, const int4* tiles, int n, int grid, const T* U,
+static cudaError_t recon_launch(const ParamsT<T>& P, const int4* tiles, int n, bool persistent, const T* U,
                                 const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>& dbg, cudaStream_t st) {
-  auto kern = k_reconstruct<T, LIM, RECON, DBG, RTY, MINB>;
-  if (grid <= 0) {  // persistent: resident CTAs per SM x SMs
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, TX * RTY, 0);
-    grid = sms * (per > 0 ? per : 1);
+  if (persistent) {
+    auto kern = k_reconstruct<T, LIM, RECON, DBG, RTY, MINB, true>;
+    kern<<<persistent_grid(kern, TX * RTY, n), TX * RTY, 0, st>>>(P, tiles, n, U, inst, F, dbg);
+  } else {
+    k_reconstruct<T, LIM, RECON, DBG, RTY, MINB, false><<<n, TX * RTY, 0, st>>>(P, tiles, n, U, inst, F, dbg);
   }
-  if (grid > n) grid = n;
-  kern<<<grid, TX * RTY, 0, st>>>(P, tiles, n, U, inst, F, dbg);
   return cudaGetLastError();
 }
 
@@ -519,14 +572,14 @@ static cudaError_t recon_variant(const ParamsT<T>& P, const int4* const* tiles_b
                                  int variant, bool persistent, const T* U, const InstanceState* inst, FaceArraysT<T> F,
                                  const DebugOutT<T>* dbg, cudaStream_t st) {
   if (dbg)  // the per-operator outputs are built for the default variant only
-    return recon_launch<T, LIM, RECON, true, 8, 1>(P, tiles_by_rty[1], n_by_rty[1], n_by_rty[1], U, inst, F, *dbg, st);
+    return recon_launch<T, LIM, RECON, true, 8, 1>(P, tiles_by_rty[1], n_by_rty[1], false, U, inst, F, *dbg, st);
   const DebugOutT<T> none{};
   switch (variant) {
-    case 1: return recon_launch<T, LIM, RECON, false, 8, 2>(P, tiles_by_rty[1], n_by_rty[1], persistent ? 0 : n_by_rty[1], U, inst, F, none, st);
-    case 2: return recon_launch<T, LIM, RECON, false, 4, 2>(P, tiles_by_rty[0], n_by_rty[0], persistent ? 0 : n_by_rty[0], U, inst, F, none, st);
-    case 3: return recon_launch<T, LIM, RECON, false, 4, 4>(P, tiles_by_rty[0], n_by_rty[0], persistent ? 0 : n_by_rty[0], U, inst, F, none, st);
-    case 4: return recon_launch<T, LIM, RECON, false, 16, 1>(P, tiles_by_rty[2], n_by_rty[2], persistent ? 0 : n_by_rty[2], U, inst, F, none, st);
-    default: return recon_launch<T, LIM, RECON, false, 8, 1>(P, tiles_by_rty[1], n_by_rty[1], persistent ? 0 : n_by_rty[1], U, inst, F, none, st);
+    case 1: return recon_launch<T, LIM, RECON, false, 8, 1>(P, tiles_by_rty[1], n_by_rty[1], persistent, U, inst, F, none, st);
+    case 2: return recon_launch<T, LIM, RECON, false, 4, 2>(P, tiles_by_rty[0], n_by_rty[0], persistent, U, inst, F, none, st);
+    case 3: return recon_launch<T, LIM, RECON, false, 4, 4>(P, tiles_by_rty[0], n_by_rty[0], persistent, U, inst, F, none, st);
+    case 4: return recon_launch<T, LIM, RECON, false, 16, 1>(P, tiles_by_rty[2], n_by_rty[2], persistent, U, inst, F, none, st);
+    default: return recon_launch<T, LIM, RECON, false, 8, 2>(P, tiles_by_rty[1], n_by_rty[1], persistent, U, inst, F, none, st);
   }
 }
 
@@ -559,17 +612,12 @@ cudaError_t launch_reconstruct(const ParamsT<T>& P, const TileSet& ts, KernelCho
 template <typename T, int FLUX, bool DBG, int MINB>
 static cudaError_t flux_launch(const ParamsT<T>& P, const int4* tiles, int n, bool persistent,
                                const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>& dbg, cudaStream_t st) {
-  auto kern = k_flux<T, FLUX, DBG, MINB>;
-  int grid = n;
   if (persistent) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, TX * TY, 0);
-    grid = sms * (per > 0 ? per : 1);
-    if (grid > n) grid = n;
+    auto kern = k_flux<T, FLUX, DBG, MINB, true>;
+    kern<<<persistent_grid(kern, TX * TY, n), TX * TY, 0, st>>>(P, tiles, n, inst, F, dbg);
+  } else {
+    k_flux<T, FLUX, DBG, MINB, false><<<n, TX * TY, 0, st>>>(P, tiles, n, inst, F, dbg);
   }
-  kern<<<grid, TX * TY, 0, st>>>(P, tiles, n, inst, F, dbg);
   return cudaGetLastError();
 }
 
@@ -579,9 +627,9 @@ static cudaError_t flux_t(const ParamsT<T>& P, const int4* tiles, int n, KernelC
   if (dbg) return flux_launch<T, FLUX, true, 1>(P, tiles, n, false, inst, F, *dbg, st);
   const DebugOutT<T> none{};
   switch (kc.variant) {
-    case 1: return flux_launch<T, FLUX, false, 2>(P, tiles, n, kc.persistent, inst, F, none, st);
-    case 2: return flux_launch<T, FLUX, false, 3>(P, tiles, n, kc.persistent, inst, F, none, st);
-    default: return flux_launch<T, FLUX, false, 1>(P, tiles, n, kc.persistent, inst, F, none, st);
+    case 1: return flux_launch<T, FLUX, false, 1>(P, tiles, n, kc.persistent, inst, F, none, st);
+    case 2: return flux_launch<T, FLUX, false, 6>(P, tiles, n, kc.persistent, inst, F, none, st);
+    default: return flux_launch<T, FLUX, false, 4>(P, tiles, n, kc.persistent, inst, F, none, st);
   }
 }
 
@@ -602,16 +650,12 @@ cudaError_t launch_update(const ParamsT<T>& P, const TileSet& ts, KernelChoice k
                           T* dudt_out, cudaStream_t st) {
   const int n = ts.ncell[1];
   if (n <= 0) return cudaSuccess;
-  int grid = n;
   if (kc.persistent) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_update<T>, TX * TY, 0);
-    grid = sms * (per > 0 ? per : 1);
-    if (grid > n) grid = n;
+    auto kern = k_update<T, true>;
+    kern<<<persistent_grid(kern, TX * TY, n), TX * TY, 0, st>>>(P, ts.cell[1], n, F, S, prog, inst, real, dudt_out);
+  } else {
+    k_update<T, false><<<n, TX * TY, 0, st>>>(P, ts.cell[1], n, F, S, prog, inst, real, dudt_out);
   }
-  k_update<T><<<grid, TX * TY, 0, st>>>(P, ts.cell[1], n, F, S, prog, inst, real, dudt_out);
   return cudaGetLastError();
 }
 
@@ -642,5 +686,20 @@ cudaError_t launch_realizable(const ParamsT<T>& P, const int4* tiles, int n, con
                                         cudaStream_t);                                                           \
   template cudaError_t launch_dt<T>(const ParamsT<T>&, const int4*, int, const T*, InstanceState*, cudaStream_t); \
   template cudaError_t launch_realizable<T>(const ParamsT<T>&, const int4*, int, const T*, RealizState*, cudaStream_t);
+
+// for units that include this header but call the launchers instantiated elsewhere
+#define E2D_EXTERN_STAGE_LAUNCHERS(T)                                                                           \
+  extern template cudaError_t launch_reconstruct<T>(const ParamsT<T>&, const TileSet&, KernelChoice, const T*,   \
+                                                    const InstanceState*, FaceArraysT<T>, const DebugOutT<T>*,   \
+                                                    cudaStream_t);                                               \
+  extern template cudaError_t launch_flux<T>(const ParamsT<T>&, const TileSet&, KernelChoice, const InstanceState*, \
+                                             FaceArraysT<T>, const DebugOutT<T>*, cudaStream_t);                 \
+  extern template cudaError_t launch_update<T>(const ParamsT<T>&, const TileSet&, KernelChoice, FaceArraysT<T>,  \
+                                               StateBuffersT<T>, const StageProgram&, InstanceState*, RealizState*, \
+                                               T*, cudaStream_t);                                                \
+  extern template cudaError_t launch_dt<T>(const ParamsT<T>&, const int4*, int, const T*, InstanceState*,        \
+                                           cudaStream_t);                                                        \
+  extern template cudaError_t launch_realizable<T>(const ParamsT<T>&, const int4*, int, const T*, RealizState*,  \
+                                                   cudaStream_t);
 
 }  // namespace e2d

@@ -96,6 +96,10 @@ class E2DRealizability(ctypes.Structure):
     ]
 
 
+class E2DPressureObjective(ctypes.Structure):
+    _fields_ = [("block", ctypes.c_int32), ("side", ctypes.c_int32)]
+
+
 class E2DDebug(ctypes.Structure):
     _fields_ = [(name, c_double_p) for name in
                 ("gx", "gy", "phi", "vL", "vR", "hL", "hR", "vflux_raw", "hflux_raw", "vflux", "hflux")]

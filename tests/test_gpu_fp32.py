@@ -42,7 +42,7 @@ def test_fp32_density_l1_vs_fp64(name, steps, bound):
     t64, n64 = S64.run(0.0, tf, max_steps=steps)
     t32, n32 = S32.run(0.0, tf, max_steps=steps)
     assert n64 == n32 == steps
-    assert abs(t32 - t64) <= 1e-5 * t64  # dt from FP32 states, reduced in FP64
+    assert abs(t32 - t64) <= 2 * bound * t64  # CFL dt of states that differ by the same order
     U64, U32 = S64.get_state(), S32.get_state()
     err = _l1_rel(U32[0], U64[0])
     assert err < bound, f"L1 density error {err:.3e}"
