@@ -342,12 +342,17 @@ static void face_flux(const Ctx* C, const double* WL, const double* WR, double* 
 }
 
 /* ---------------------------------------------------------------- limiter psi ----- */
+/* pyhype/limiters/limiters.py:25-62.  Van Albada and Venkatakrishnan form s*s, which
+   overflows for s > 1.34e154 and makes the reference return inf/inf = NaN; both already
+   equal 1.0 exactly from s ~ 1e17, so the slope is capped at 1e30: every finite value of
+   the reference is unchanged and its NaN becomes 1 (the one deliberate deviation). */
+#define SLOPE_CAP 1e30
 static double psi(int lim, double s) {
   switch (lim) {
     case E2D_LIM_BARTH_JESPERSEN: return np_min(1.0, s);
-    case E2D_LIM_VAN_ALBADA: { double s2 = s * s; return (s2 + s) / (s2 + 1); }
+    case E2D_LIM_VAN_ALBADA: { if (s > SLOPE_CAP) s = SLOPE_CAP; double s2 = s * s; return (s2 + s) / (s2 + 1); }
     case E2D_LIM_VAN_LEER: return (fabs(s) + s) / (s + 1);
-    default: { double s2 = s * s; return (s2 + 2 * s) / (s2 + s + 2); }
+    default: { if (s > SLOPE_CAP) s = SLOPE_CAP; double s2 = s * s; return (s2 + 2 * s) / (s2 + s + 2); }
   }
 }
 

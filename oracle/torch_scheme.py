@@ -110,9 +110,15 @@ def reflect(q, c, s):
     return unrotate(r, c, s)
 
 
+SLOPE_CAP = 1e30  # the slope cap of the CUDA path and the C oracle (psi is exactly 1 beyond ~1e17)
+
+
 def psi(lim, s):
     if lim == "BarthJespersen":
         return torch.where(vlt(s, torch.ones_like(s)), s, torch.ones_like(s))
+    if lim in ("VanAlbada", "Venkatakrishnan"):
+        cap = torch.full_like(s, SLOPE_CAP)
+        s = torch.where(vlt(cap, s), cap, s)
     if lim == "VanAlbada":
         s2 = s * s
         return (s2 + s) / (s2 + 1)

@@ -47,10 +47,10 @@ struct AdjProgramT {
 // minimum over faces, clip), recording the selections the reverse pass needs.
 template <typename T>
 struct LimiterTrace {
-  T sl[4];       // slope per face
-  T davg[4];     // face difference per face
-  int sign[4];   // +1 davg > 0, -1 davg < 0, 0 davg == 0 (slope 1)
   int sel;       // face whose psi is phi (the first of equal values)
+  T sl;          // that face's slope
+  T davg;        // that face's difference
+  int sign;      // +1 davg > 0, -1 davg < 0, 0 davg == 0 (slope 1)
   bool clipped;  // phi was negative and set to 0
   int imax, imin;  // stencil index (w0, we, ea, so, no) of the max and of the min
 };
@@ -73,7 +73,8 @@ __device__ __forceinline__ void limiter_forward(T w0, T we, T ea, T so, T no, T 
     if (vlt(nb[q], mn)) { mn = nb[q]; imn = q + 1; }
   }
   const T dmax = mx - w0, dmin = mn - w0;
-  int sel = 0;
+  int sel = 0, ssign = 0;
+  T ssl = T(0), sdavg = T(0);
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     hot[s] = gx * hx[s] + gy * hy[s];
@@ -88,22 +89,21 @@ __device__ __forceinline__ void limiter_forward(T w0, T we, T ea, T so, T no, T 
     const T q = (pos ? dmax : dmin) / ((pos || neg) ? davg : T(1));
     const T sl = (pos || neg) ? q : T(1);
     const T p = psi<LIM>(sl);
-    if (s == 0) {
-      ph = p;
-    } else if (vlt(p, ph)) {
+    if (s == 0 || vlt(p, ph)) {
       ph = p;
       sel = s;
-    }
-    if (tr) {
-      tr->sl[s] = sl;
-      tr->davg[s] = davg;
-      tr->sign[s] = pos ? 1 : (neg ? -1 : 0);
+      ssl = sl;
+      sdavg = davg;
+      ssign = pos ? 1 : (neg ? -1 : 0);
     }
   }
   const bool clipped = is_neg(ph);
   ph = clipped ? T(0) : ph;
   if (tr) {
     tr->sel = sel;
+    tr->sl = ssl;
+    tr->davg = sdavg;
+    tr->sign = ssign;
     tr->clipped = clipped;
     tr->imax = imx;
     tr->imin = imn;
@@ -263,62 +263,70 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_vjp(ParamsT<T> P, const
   const T cS = P.geo.hface[E2D_F_COS][fS], sS = P.geo.hface[E2D_F_SIN][fS];
   const int rotV = cart ? 0 : 1, rotH = cart ? 2 : 1;
 
+  // Face states, then their adjoints, live in shared memory between the phases (one
+  // slot per side and variable and thread): loops that are not unrolled keep one
+  // variable's limiter, or one side's conversion, in registers at a time.
+  __shared__ T sL[16][TX * TY];
+
   // Phase A: forward limited face states (the forward kernel's expressions)
-  T face[4][4];
-#pragma unroll
+#pragma unroll 1
   for (int v = 0; v < 4; ++v) {
     T hot[4], ph;
-    limiter_forward<T, LIM>(sW[v][ty + 1][tx + 1], sW[v][ty + 1][tx], sW[v][ty + 1][tx + 2], sW[v][ty][tx + 1],
-                            sW[v][ty + 2][tx + 1], LcE, LsE, LcW, LsW, LcN, LsN, LcS, LsS, ia, hx, hy, hot, ph,
-                            nullptr);
+    const T w0 = sW[v][ty + 1][tx + 1];
+    limiter_forward<T, LIM>(w0, sW[v][ty + 1][tx], sW[v][ty + 1][tx + 2], sW[v][ty][tx + 1], sW[v][ty + 2][tx + 1],
+                            LcE, LsE, LcW, LsW, LcN, LsN, LcS, LsS, ia, hx, hy, hot, ph, nullptr);
 #pragma unroll
-    for (int s = 0; s < 4; ++s) face[s][v] = sW[v][ty + 1][tx + 1] + ph * hot[s];
+    for (int s = 0; s < 4; ++s) sL[s * 4 + v][threadIdx.x] = w0 + ph * hot[s];
   }
 
-  // Phase B: face adjoints through conversion and rotation; own-face boundary states
-  T lf[4][4];
-  {
-    T lw[4];
-    load_face(F.vL, P.nvface, fE, lw);
-    face_state_vjp<RECON>(face[E2D_E], rotV, cE, sE, G, lw, lf[E2D_E]);
-    load_face(F.vR, P.nvface, fW, lw);
-    face_state_vjp<RECON>(face[E2D_W], rotV, cW, sW_, G, lw, lf[E2D_W]);
-    load_face(F.hL, P.nhface, fN, lw);
-    face_state_vjp<RECON>(face[E2D_N], rotH, cN, sN, G, lw, lf[E2D_N]);
-    load_face(F.hR, P.nhface, fS, lw);
-    face_state_vjp<RECON>(face[E2D_S], rotH, cS, sS, G, lw, lf[E2D_S]);
-  }
-  // block-boundary faces whose outside state is this cell's own face state (with the
+  // Phase B: per side, the face-state adjoint through conversion and rotation, plus
+  // the boundary face's outside state when it is this cell's own face state (with the
   // side's reflection); ghost-valued outside states are handled in phase D
-  {
-    const int side_of[4] = {E2D_W, E2D_E, E2D_S, E2D_N};
-    const bool at[4] = {j == 0, j == nx - 1, i == 0, i == ny - 1};
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      if (!at[q]) continue;
-      const int side = side_of[q];
+  for (int side = 0; side < 4; ++side) {
+    T q[4], lw[4], lq[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) q[v] = sL[side * 4 + v][threadIdx.x];
+    const bool vert = side == E2D_E || side == E2D_W;
+    const T fc = side == E2D_E ? cE : side == E2D_W ? cW : side == E2D_N ? cN : cS;
+    const T fs = side == E2D_E ? sE : side == E2D_W ? sW_ : side == E2D_N ? sN : sS;
+    const int rot = vert ? rotV : rotH;
+    // this cell's face state is the left state of its E/N face, the right state of W/S
+    if (side == E2D_E) load_face(F.vL, P.nvface, fE, lw);
+    else if (side == E2D_W) load_face(F.vR, P.nvface, fW, lw);
+    else if (side == E2D_N) load_face(F.hL, P.nhface, fN, lw);
+    else load_face(F.hR, P.nhface, fS, lw);
+    face_state_vjp<RECON>(q, rot, fc, fs, G, lw, lq);
+    const bool at = side == E2D_E ? j == nx - 1 : side == E2D_W ? j == 0 : side == E2D_N ? i == ny - 1 : i == 0;
+    if (at) {
+      const int k = vert ? i : j;
       const double *gd, *fd;
-      const int kind = side_kind_at(B, side, (side == E2D_E || side == E2D_W) ? i : j, t, gd, fd);
-      if (kind != E2D_SIDE_REFLECT && kind != E2D_SIDE_OUTLET) continue;
-      T o[4] = {face[side][0], face[side][1], face[side][2], face[side][3]};
-      T bc, bs;
-      if (kind == E2D_SIDE_REFLECT) {
-        boundary_cs(P, B, side, (side == E2D_E || side == E2D_W) ? i : j, bc, bs);
-        reflect(o, bc, bs);
-      }
-      T lw[4], lo[4];
-      if (side == E2D_W) { load_face(F.vL, P.nvface, fW, lw); face_state_vjp<RECON>(o, rotV, cW, sW_, G, lw, lo); }
-      else if (side == E2D_E) { load_face(F.vR, P.nvface, fE, lw); face_state_vjp<RECON>(o, rotV, cE, sE, G, lw, lo); }
-      else if (side == E2D_S) { load_face(F.hL, P.nhface, fS, lw); face_state_vjp<RECON>(o, rotH, cS, sS, G, lw, lo); }
-      else { load_face(F.hR, P.nhface, fN, lw); face_state_vjp<RECON>(o, rotH, cN, sN, G, lw, lo); }
-      if (kind == E2D_SIDE_REFLECT) reflect_vjp(lo, bc, bs);
+      const int kind = side_kind_at(B, side, k, t, gd, fd);
+      if (kind == E2D_SIDE_REFLECT || kind == E2D_SIDE_OUTLET) {
+        T o[4] = {q[0], q[1], q[2], q[3]};
+        T bc = T(0), bs = T(0);
+        if (kind == E2D_SIDE_REFLECT) {
+          boundary_cs(P, B, side, k, bc, bs);
+          reflect(o, bc, bs);
+        }
+        T lo[4];
+        // the outside state is the other side's state of the same face
+        if (side == E2D_E) load_face(F.vR, P.nvface, fE, lw);
+        else if (side == E2D_W) load_face(F.vL, P.nvface, fW, lw);
+        else if (side == E2D_N) load_face(F.hR, P.nhface, fN, lw);
+        else load_face(F.hL, P.nhface, fS, lw);
+        face_state_vjp<RECON>(o, rot, fc, fs, G, lw, lo);
+        if (kind == E2D_SIDE_REFLECT) reflect_vjp(lo, bc, bs);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) lf[side][v] += lo[v];
+        for (int v = 0; v < 4; ++v) lq[v] += lo[v];
+      }
     }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) sL[side * 4 + v][threadIdx.x] = lq[v];
   }
 
   // Phase C: limiter and gradient reverse, one variable at a time
-#pragma unroll
+#pragma unroll 1
   for (int v = 0; v < 4; ++v) {
     const T w0 = sW[v][ty + 1][tx + 1], we = sW[v][ty + 1][tx], ea = sW[v][ty + 1][tx + 2];
     const T so = sW[v][ty][tx + 1], no = sW[v][ty + 2][tx + 1];
@@ -328,31 +336,26 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_vjp(ParamsT<T> P, const
     T lw0 = T(0), lph = T(0), lhot[4];
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-      lw0 += lf[s][v];
-      lph += lf[s][v] * hot[s];
-      lhot[s] = lf[s][v] * ph;
+      const T l = sL[s * 4 + v][threadIdx.x];
+      lw0 += l;
+      lph += l * hot[s];
+      lhot[s] = l * ph;
     }
     T lst[5] = {T(0), T(0), T(0), T(0), T(0)};  // w0, we, ea, so, no
     if (!tr.clipped) {
-      const int s = tr.sel;
-      const T lsl = lph * psi_deriv<LIM>(tr.sl[s]);
-      const T davg = tr.davg[s];
+      const T lsl = lph * psi_deriv<LIM>(tr.sl);
       T ld = T(0), lden = T(0);
-      if (tr.sign[s] != 0) {
-        ld = lsl / davg;
-        lden = -lsl * tr.sl[s] / davg;
+      if (tr.sign != 0) {
+        ld = lsl / tr.davg;
+        lden = -lsl * tr.sl / tr.davg;
       }
       // davg = (w0 + hot) - w0 carries hot through with derivative 1
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (q == s) lhot[q] += lden;
-      if (tr.sign[s] > 0) {
-        lst[tr.imax] += ld;
-        lw0 -= ld;
-      } else if (tr.sign[s] < 0) {
-        lst[tr.imin] += ld;
-        lw0 -= ld;
-      }
+      for (int q = 0; q < 4; ++q) lhot[q] += (q == tr.sel) ? lden : T(0);
+      const int im = tr.sign > 0 ? tr.imax : (tr.sign < 0 ? tr.imin : -1);
+#pragma unroll
+      for (int q = 0; q < 5; ++q) lst[q] += (q == im) ? ld : T(0);
+      lw0 -= (im >= 0) ? ld : T(0);
     }
     T lgx = T(0), lgy = T(0);
 #pragma unroll

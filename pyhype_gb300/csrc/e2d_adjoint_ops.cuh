@@ -43,7 +43,7 @@ __device__ __forceinline__ void reflect_vjp(T* lq, T c, T s) { reflect(lq, c, s)
 // d psi / d s of the limiter functions (s >= 0 here: the slope is dmax/davg with
 // davg > 0 or dmin/davg with davg < 0).  The rational derivatives are written as
 // ((numerator)/d)/d so that large s does not overflow; beyond s = 1e100 (and in the
-// capped region of the FP32 slope) they are zero to working precision.
+// capped region of the slope) they are zero to working precision.
 template <int LIM, typename T>
 __device__ __forceinline__ T psi_deriv(T s) {
   if (LIM == E2D_LIM_BARTH_JESPERSEN) return (s < T(1)) ? T(1) : T(0);  // min(1, s)
@@ -51,11 +51,7 @@ __device__ __forceinline__ T psi_deriv(T s) {
     const T d = s + T(1);
     return ((sgn(s) + T(1)) - (fabs(s) + s) / d) / d;
   }
-  if constexpr (sizeof(T) == 4) {
-    if (s > T(1e15)) return T(0);
-  } else {
-    if (s > T(1e100)) return T(0);
-  }
+  if (vlt(sizeof(T) == 4 ? T(SLOPE_CAP_FP32) : T(SLOPE_CAP_FP64), s)) return T(0);  // capped: constant
   if (LIM == E2D_LIM_VAN_ALBADA) {  // (s^2 + s)/(s^2 + 1)
     const T d = s * s + T(1);
     return ((T(1) + T(2) * s - s * s) / d) / d;

@@ -162,4 +162,5 @@ def test_ic_parameter_gradient_vs_central_differences(cx):
         Jm = A.forward(smoothed_explosion(P, tm[0], tm[1], tm[2]), dts)
         fd = (Jp - Jm) / (2 * h)
         print(f"cx {cx} param {k}: adjoint {grad[k]:.12e} fd {fd:.12e} rel {abs(fd - grad[k]) / abs(grad[k]):.2e}")
-        assert abs(fd - grad[k]) <= 1e-6 * abs(grad[k])
+        # 1e-6 relative, plus the round-off of the difference quotient (J to ~1e-15)
+        assert abs(fd - grad[k]) <= 1e-6 * abs(grad[k]) + 1e-15 * abs(J.item()) / h
