@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--skip-cpu-baseline", action="store_true", help="omit the CPU baseline (profiling runs)")
     ap.add_argument("--skip-ensemble", action="store_true", help="omit the batched-ensemble section")
     ap.add_argument("--skip-adjoint", action="store_true", help="omit the adjoint section")
+    ap.add_argument("--skip-dmr", action="store_true", help="omit the double-Mach-reflection section")
     ap.add_argument("--workload", default="multiblock", choices=["multiblock", "ensemble"],
                     help="'ensemble' runs the full 512-instance, 200-step batched comparison instead")
     return ap.parse_args()
@@ -371,6 +372,44 @@ def adjoint_section(stream, nsteps: int = 400, ckpt: int = 20, n: int = 256, fd:
     return out
 
 
+def dmr_section(stream):
+    """Mach-10 double-Mach reflection: [0,4] x [0,1] as 5 blocks of 400 x 500 cells
+    (dx = dy = 0.002), HLLL/Venkatakrishnan/Green-Gauss, primitive reconstruction,
+    SSP-RK2 at CFL 0.4 to t = 0.2, FP64 and FP32 through Euler2D; FP32 L1 density
+    difference at t_final."""
+    import numpy as np
+    import torch
+
+    from pyhype_gb300.configs import double_mach
+    from pyhype_gb300.solvers import Euler2D
+
+    out = {"workload": "double-Mach reflection, 5 blocks x 400x500 cells, HLLL/Venkatakrishnan, primitive "
+                       "reconstruction, SSP-RK2, CFL 0.4, t_final 0.2"}
+    states = {}
+    for prec in ("fp64", "fp32"):
+        cfg, gen = double_mach()
+        sim = Euler2D(cfg, gen, precision=prec)
+        sim.device.set_stream(stream.cuda_stream)
+        sim._pre_process_solve()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim._solve()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        sim._post_process_solve()
+        cells = sim.problem.ncell
+        out[prec] = {"value": cells * 2 * sim.num_time_step / (ms * 1e-3), "unit": "cell-stage updates/s",
+                     "steps": sim.num_time_step, "seconds": ms * 1e-3, "t_final_reached": sim.t >= sim.t_final}
+        states[prec] = np.concatenate([b.state.data[:, :, 0].ravel() for b in sim.blocks])
+        sim.device.close()
+    a, b = states["fp64"], states["fp32"]
+    out["fp32_l1_density_rel_vs_fp64"] = float(np.sum(np.abs(b - a)) / np.sum(np.abs(a)))
+    out["fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def run_reference(args, ws, rank):
     """--impl reference: the reference algorithm's CPU implementation (C restatement,
     all host threads) on the same workload; rank 0 only."""
@@ -557,6 +596,13 @@ def main():
         except Exception as exc:
             adjoint = {"error": str(exc)}
 
+    dmr = None
+    if not args.skip_dmr and ws == 1:
+        try:
+            dmr = dmr_section(stream)
+        except Exception as exc:
+            dmr = {"error": str(exc)}
+
     clocks = clk.summary()
     line = {
         "metric": METRIC,
@@ -592,6 +638,7 @@ def main():
         "fp32": fp32,
         "ensemble": ensemble,
         "adjoint": adjoint,
+        "dmr": dmr,
         "gpu_launches": int(args.steps * (3 + 3 * stages)),
         "clocks": clocks,
     }

@@ -76,12 +76,16 @@ def smoothed_explosion(problem: Problem, r, w, cx, cy=5.0, device="cuda") -> tor
 
 
 class AdjointSolver:
-    """A single-instance FP64 problem set up for the recorded forward / reverse pass."""
+    """A single-instance problem set up for the recorded forward / reverse pass, on the
+    FP64 path or (``precision="fp32"``) the FP32 form, whose reverse kernels run in FP32
+    (J, dt and the returned gradient are FP64 values)."""
 
     def __init__(self, problem: Problem, integrator: str = "RK4", block: int = 0, side: str = "N",
-                 nsteps: int = 400, ckpt_every: int = 20):
-        self.problem = problem
-        self.device = DeviceSolver(problem, tableau=named_tableau(integrator))
+                 nsteps: int = 400, ckpt_every: int = 20, precision: str = "fp64"):
+        if precision not in ("fp64", "fp32"):
+            raise ValueError(f"precision must be 'fp64' or 'fp32', not {precision!r}")
+        self.problem = problem if precision == "fp64" else problem.with_precision(1)
+        self.device = DeviceSolver(self.problem, tableau=named_tableau(integrator))
         self.block, self.side = int(block), SIDE[side] if isinstance(side, str) else int(side)
         self.nsteps, self.ckpt_every = int(nsteps), int(ckpt_every)
         self._record = 0

@@ -55,14 +55,23 @@ struct LimiterTrace {
   int imax, imin;  // stencil index (w0, we, ea, so, no) of the max and of the min
 };
 
+// interface averages and Green-Gauss gradient of one variable (forward expressions)
+template <typename T>
+__device__ __forceinline__ void green_gauss(T w0, T we, T ea, T so, T no, T LcE, T LsE, T LcW, T LsW, T LcN, T LsN,
+                                            T LcS, T LsS, T ia, T& gx, T& gy) {
+  const T ie = T(0.5) * (w0 + ea), iw = T(0.5) * (we + w0);
+  const T in = T(0.5) * (w0 + no), is = T(0.5) * (so + w0);
+  gx = (ie * LcE + iw * (-LcW) + in * LcN + is * (-LcS)) * ia;
+  gy = (ie * LsE + iw * (-LsW) + in * LsN + is * (-LsS)) * ia;
+}
+
 template <typename T, int LIM>
 __device__ __forceinline__ void limiter_forward(T w0, T we, T ea, T so, T no, T LcE, T LsE, T LcW, T LsW, T LcN,
                                                 T LsN, T LcS, T LsS, T ia, const T* hx, const T* hy, T* hot, T& ph,
-                                                LimiterTrace<T>* tr) {
-  const T ie = T(0.5) * (w0 + ea), iw = T(0.5) * (we + w0);
-  const T in = T(0.5) * (w0 + no), is = T(0.5) * (so + w0);
-  const T gx = (ie * LcE + iw * (-LcW) + in * LcN + is * (-LcS)) * ia;
-  const T gy = (ie * LsE + iw * (-LsW) + in * LsN + is * (-LsS)) * ia;
+                                                LimiterTrace<T>* tr, T* gxo = nullptr, T* gyo = nullptr) {
+  T gx, gy;
+  green_gauss(w0, we, ea, so, no, LcE, LsE, LcW, LsW, LcN, LsN, LcS, LsS, ia, gx, gy);
+  if (gxo) { *gxo = gx; *gyo = gy; }
   // vmax(a, b) keeps a unless a < b; vmin(a, b) keeps a unless b < a
   const T nb[4] = {we, ea, so, no};
   T mx = w0, mn = w0;
@@ -204,12 +213,16 @@ __device__ __forceinline__ void load_face(const T* __restrict__ a, int64_t strid
   q[3] = a[3 * stride + f];
 }
 
+// tile height of the reverse reconstruction (128 threads: its per-thread shared-memory
+// staging of 36 values fits the static limit)
+constexpr int VTY = 4;
+
 template <typename T, int LIM, int RECON>
-__global__ void __launch_bounds__(TX * TY) k_reconstruct_vjp(ParamsT<T> P, const int4* __restrict__ tiles,
-                                                             const T* __restrict__ U,
-                                                             const InstanceState* __restrict__ inst,
-                                                             FaceArraysT<T> F, T* __restrict__ st) {
-  __shared__ T sW[4][TY + 2][TX + 2];
+__global__ void __launch_bounds__(TX * VTY, 4) k_reconstruct_vjp(ParamsT<T> P, const int4* __restrict__ tiles,
+                                                              const T* __restrict__ U,
+                                                              const InstanceState* __restrict__ inst,
+                                                              FaceArraysT<T> F, T* __restrict__ st) {
+  __shared__ T sW[4][VTY + 2][TX + 2];
   const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
   const int4 tl = tiles[blockIdx.x];
   const E2DBlock* B = P.blocks + tl.x;
@@ -219,7 +232,7 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_vjp(ParamsT<T> P, const
   const int nx = B->nx, ny = B->ny;
   const int i0 = tl.y, j0 = tl.z;
   // stencil tile in reconstruction variables, ghosts formed as in the forward kernel
-  for (int p = threadIdx.x; p < (TY + 2) * (TX + 2); p += TX * TY) {
+  for (int p = threadIdx.x; p < (VTY + 2) * (TX + 2); p += TX * VTY) {
     const int ly = p / (TX + 2), lx = p - ly * (TX + 2);
     const int gi = i0 + ly - 1, gj = j0 + lx - 1;
     const bool in_i = gi >= 0 && gi < ny, in_j = gj >= 0 && gj < nx;
@@ -263,20 +276,29 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_vjp(ParamsT<T> P, const
   const T cS = P.geo.hface[E2D_F_COS][fS], sS = P.geo.hface[E2D_F_SIN][fS];
   const int rotV = cart ? 0 : 1, rotH = cart ? 2 : 1;
 
-  // Face states, then their adjoints, live in shared memory between the phases (one
-  // slot per side and variable and thread): loops that are not unrolled keep one
-  // variable's limiter, or one side's conversion, in registers at a time.
-  __shared__ T sL[16][TX * TY];
+  // Shared-memory staging, one slot per thread: the forward limiter's result and
+  // selections per variable (phase A, read again in phase C instead of a second
+  // limiter evaluation), and the 16 face adjoints (phase B) that phase C consumes one
+  // variable at a time.
+  __shared__ T sTr[4][5][TX * VTY];   // per variable: phi, gx, gy, selected slope, its davg
+  __shared__ int sTi[4][TX * VTY];    // per variable: sel | sign | clipped | imax | imin
+  __shared__ T sL[16][TX * VTY];
+  const int tid = threadIdx.x;
 
-  // Phase A: forward limited face states (the forward kernel's expressions)
+  // Phase A: forward limiter (the forward kernel's expressions)
 #pragma unroll 1
   for (int v = 0; v < 4; ++v) {
-    T hot[4], ph;
-    const T w0 = sW[v][ty + 1][tx + 1];
-    limiter_forward<T, LIM>(w0, sW[v][ty + 1][tx], sW[v][ty + 1][tx + 2], sW[v][ty][tx + 1], sW[v][ty + 2][tx + 1],
-                            LcE, LsE, LcW, LsW, LcN, LsN, LcS, LsS, ia, hx, hy, hot, ph, nullptr);
-#pragma unroll
-    for (int s = 0; s < 4; ++s) sL[s * 4 + v][threadIdx.x] = w0 + ph * hot[s];
+    T hot[4], ph, gx, gy;
+    LimiterTrace<T> tr;
+    limiter_forward<T, LIM>(sW[v][ty + 1][tx + 1], sW[v][ty + 1][tx], sW[v][ty + 1][tx + 2], sW[v][ty][tx + 1],
+                            sW[v][ty + 2][tx + 1], LcE, LsE, LcW, LsW, LcN, LsN, LcS, LsS, ia, hx, hy, hot, ph, &tr,
+                            &gx, &gy);
+    sTr[v][0][tid] = ph;
+    sTr[v][1][tid] = gx;
+    sTr[v][2][tid] = gy;
+    sTr[v][3][tid] = tr.sl;
+    sTr[v][4][tid] = tr.davg;
+    sTi[v][tid] = tr.sel | ((tr.sign + 1) << 2) | (tr.clipped ? 16 : 0) | (tr.imax << 5) | (tr.imin << 8);
   }
 
   // Phase B: per side, the face-state adjoint through conversion and rotation, plus
@@ -286,7 +308,10 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_vjp(ParamsT<T> P, const
   for (int side = 0; side < 4; ++side) {
     T q[4], lw[4], lq[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) q[v] = sL[side * 4 + v][threadIdx.x];
+    for (int v = 0; v < 4; ++v) {  // the limited face state w0 + phi * hot of the forward
+      const T hot = sTr[v][1][tid] * hx[side] + sTr[v][2][tid] * hy[side];
+      q[v] = sW[v][ty + 1][tx + 1] + sTr[v][0][tid] * hot;
+    }
     const bool vert = side == E2D_E || side == E2D_W;
     const T fc = side == E2D_E ? cE : side == E2D_W ? cW : side == E2D_N ? cN : cS;
     const T fs = side == E2D_E ? sE : side == E2D_W ? sW_ : side == E2D_N ? sN : sS;
@@ -322,23 +347,29 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_vjp(ParamsT<T> P, const
       }
     }
 #pragma unroll
-    for (int v = 0; v < 4; ++v) sL[side * 4 + v][threadIdx.x] = lq[v];
+    for (int v = 0; v < 4; ++v) sL[side * 4 + v][tid] = lq[v];
   }
 
   // Phase C: limiter and gradient reverse, one variable at a time
 #pragma unroll 1
   for (int v = 0; v < 4; ++v) {
-    const T w0 = sW[v][ty + 1][tx + 1], we = sW[v][ty + 1][tx], ea = sW[v][ty + 1][tx + 2];
-    const T so = sW[v][ty][tx + 1], no = sW[v][ty + 2][tx + 1];
-    T hot[4], ph;
+    const T ph = sTr[v][0][tid], gx = sTr[v][1][tid], gy = sTr[v][2][tid];
     LimiterTrace<T> tr;
-    limiter_forward<T, LIM>(w0, we, ea, so, no, LcE, LsE, LcW, LsW, LcN, LsN, LcS, LsS, ia, hx, hy, hot, ph, &tr);
+    tr.sl = sTr[v][3][tid];
+    tr.davg = sTr[v][4][tid];
+    const int packed = sTi[v][tid];
+    tr.sel = packed & 3;
+    tr.sign = ((packed >> 2) & 3) - 1;
+    tr.clipped = (packed & 16) != 0;
+    tr.imax = (packed >> 5) & 7;
+    tr.imin = (packed >> 8) & 7;
     T lw0 = T(0), lph = T(0), lhot[4];
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-      const T l = sL[s * 4 + v][threadIdx.x];
+      const T l = sL[s * 4 + v][tid];
+      const T hot = gx * hx[s] + gy * hy[s];
       lw0 += l;
-      lph += l * hot[s];
+      lph += l * hot;
       lhot[s] = l * ph;
     }
     T lst[5] = {T(0), T(0), T(0), T(0), T(0)};  // w0, we, ea, so, no

@@ -164,3 +164,23 @@ def test_ic_parameter_gradient_vs_central_differences(cx):
         print(f"cx {cx} param {k}: adjoint {grad[k]:.12e} fd {fd:.12e} rel {abs(fd - grad[k]) / abs(grad[k]):.2e}")
         # 1e-6 relative, plus the round-off of the difference quotient (J to ~1e-15)
         assert abs(fd - grad[k]) <= 1e-6 * abs(grad[k]) + 1e-15 * abs(J.item()) / h
+
+
+def test_fp32_adjoint_close_to_fp64():
+    """The FP32 form's reverse pass (FP32 state, face states and reverse kernels) at the
+    FP64 pass's dt schedule: dJ/dU0 within a stated distance of the FP64 gradient."""
+    from pyhype_gb300.adjoint import AdjointSolver, adjoint_problem, smoothed_explosion
+
+    P = adjoint_problem(n=64)
+    U0 = smoothed_explosion(P, 4.0, 2.0, 5.3)
+    A64 = AdjointSolver(P, "RK4", side="N", nsteps=40, ckpt_every=10)
+    J64 = A64.forward(U0)
+    g64 = A64.backward().cpu().numpy()
+    A32 = AdjointSolver(P, "RK4", side="N", nsteps=40, ckpt_every=10, precision="fp32")
+    J32 = A32.forward(U0, A64.dts.copy())
+    g32 = A32.backward().cpu().numpy()
+    rel_J = abs(J32 - J64) / abs(J64)
+    rel_g = float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))
+    print(f"FP32 adjoint: J rel {rel_J:.2e}, gradient L2 rel {rel_g:.2e}")
+    assert rel_J < 1e-5
+    assert rel_g < 1e-3
