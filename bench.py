@@ -55,8 +55,13 @@ def parse():
     ap.add_argument("--skip-ensemble", action="store_true", help="omit the batched-ensemble section")
     ap.add_argument("--skip-adjoint", action="store_true", help="omit the adjoint section")
     ap.add_argument("--skip-dmr", action="store_true", help="omit the double-Mach-reflection section")
-    ap.add_argument("--workload", default="multiblock", choices=["multiblock", "ensemble"],
-                    help="'ensemble' runs the full 512-instance, 200-step batched comparison instead")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
+                    help="arithmetic of the timed multiblock run (fp32: the FP32 form; for profiling)")
+    ap.add_argument("--workload", default="multiblock",
+                    choices=["multiblock", "ensemble", "adjoint", "adjoint-study"],
+                    help="'ensemble' runs the full 512-instance, 200-step batched comparison instead; "
+                         "'adjoint' one recorded forward + reverse pass on an n x n block for --steps steps; "
+                         "'adjoint-study' the finite-difference convergence study of the reverse pass")
     return ap.parse_args()
 
 
@@ -302,7 +307,8 @@ def ensemble_section(stream, full: bool = False, autotune: bool = True):
     return out
 
 
-def adjoint_section(stream, nsteps: int = 400, ckpt: int = 20, n: int = 256, fd: bool = True):
+def adjoint_section(stream, nsteps: int = 400, ckpt: int = 20, n: int = 256, fd: bool = True,
+                    precision: str = "fp64"):
     """Adjoint configuration: one 256 x 256 block on [0,10]^2, Reflection sides,
     Roe/Venkatakrishnan, RK4 at CFL 0.5, 400 steps; tanh-edged explosion with
     (r, w, cx) = (4, 2, 5); J = sum_n dt_n * (pressure integral along the north wall).
@@ -315,7 +321,7 @@ def adjoint_section(stream, nsteps: int = 400, ckpt: int = 20, n: int = 256, fd:
     from pyhype_gb300.adjoint import AdjointSolver, adjoint_problem, smoothed_explosion
 
     P = adjoint_problem(n=n)
-    A = AdjointSolver(P, "RK4", side="N", nsteps=nsteps, ckpt_every=ckpt)
+    A = AdjointSolver(P, "RK4", side="N", nsteps=nsteps, ckpt_every=ckpt, precision=precision)
     A.device.set_stream(stream.cuda_stream)
     theta = torch.tensor([4.0, 2.0, 5.0], dtype=torch.float64, device="cuda", requires_grad=True)
     with torch.cuda.stream(stream):
@@ -350,7 +356,7 @@ def adjoint_section(stream, nsteps: int = 400, ckpt: int = 20, n: int = 256, fd:
                        "J = sum dt * north-wall pressure integral",
            "J": J, "forward_recorded_ms": t_fwd, "backward_ms": t_bwd, "plain_forward_ms": t_plain,
            "adjoint_cost_over_forward": t_bwd / t_plain,
-           "adjoint_cost_over_recorded_forward": t_bwd / t_fwd}
+           "adjoint_cost_over_recorded_forward": t_bwd / t_fwd, "precision": precision}
     if fd:
         J1 = A.objective(smoothed_explosion(P, theta[0], theta[1], theta[2]))
         J1.backward()
@@ -370,6 +376,41 @@ def adjoint_section(stream, nsteps: int = 400, ckpt: int = 20, n: int = 256, fd:
         out["fd_check_h1e-6"] = res
     A.device.close()
     return out
+
+
+def adjoint_study(limiters=("Venkatakrishnan", "BarthJespersen"), steps=(100, 200, 400), n: int = 256):
+    """Central differences of J against the reverse pass, for several step counts and
+    difference steps h, on the adjoint configuration off its symmetry point
+    ((r, w, cx) = (4, 2, 5.3)); prints one line per case."""
+    import torch
+
+    from pyhype_gb300.adjoint import AdjointSolver, adjoint_problem, smoothed_explosion
+
+    res = {}
+    for lim in limiters:
+        P = adjoint_problem(n=n, limiter=lim)
+        for nsteps in steps:
+            A = AdjointSolver(P, "RK4", side="N", nsteps=nsteps, ckpt_every=20)
+            theta = torch.tensor([4.0, 2.0, 5.3], dtype=torch.float64, device="cuda", requires_grad=True)
+            J = A.objective(smoothed_explosion(P, theta[0], theta[1], theta[2]))
+            J.backward()
+            g = theta.grad.cpu().numpy()
+            dts = A.dts.copy()
+            row = {"J": J.item(), "adjoint": g.tolist(), "rel_err": {}}
+            for h in (1e-2, 1e-3, 1e-4, 1e-5, 1e-6, 1e-7):
+                errs = []
+                for k in range(3):
+                    tp, tm = theta.detach().clone(), theta.detach().clone()
+                    tp[k] += h
+                    tm[k] -= h
+                    fd = (A.forward(smoothed_explosion(P, tp[0], tp[1], tp[2]), dts)
+                          - A.forward(smoothed_explosion(P, tm[0], tm[1], tm[2]), dts)) / (2 * h)
+                    errs.append(abs(fd - g[k]) / max(abs(g[k]), 1e-300))
+                row["rel_err"][f"{h:g}"] = errs
+            res[f"{lim} {n}x{n} {nsteps} steps"] = row
+            print(json.dumps({f"{lim} {n}x{n} {nsteps} steps": row}), flush=True)
+            A.device.close()
+    return res
 
 
 def dmr_section(stream):
@@ -454,6 +495,23 @@ def main():
         return
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
+    if args.workload == "adjoint":
+        import torch
+
+        torch.cuda.set_device(local)
+        if rank == 0:
+            st = torch.cuda.Stream()
+            res = adjoint_section(st, nsteps=args.steps, ckpt=max(1, args.steps // 2), n=args.n, fd=False,
+                                  precision=args.precision)
+            print(json.dumps({"metric": "adjoint cost", "adjoint": res}), flush=True)
+        return
+    if args.workload == "adjoint-study":
+        import torch
+
+        torch.cuda.set_device(local)
+        if rank == 0:
+            adjoint_study()
+        return
     if args.workload == "ensemble":
         import torch
 
@@ -475,6 +533,23 @@ def main():
     solver, cfg = make_solver(args.n)
     dev = solver.device
     P = solver.problem
+    if args.precision == "fp32":  # the FP32 form alone (profiling runs; the default line is FP64)
+        S32 = _native.DeviceSolver(P.with_precision(1), tableau=solver._time_integrator.tableau())
+        S32.set_state(P.to_soa([b.state.data for b in solver.blocks]))
+        t32, _ = S32.run(0.0, 1e30, max_steps=args.warmup)
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        g0.record()
+        S32.run(t32, 1e30, max_steps=args.steps)
+        g1.record()
+        torch.cuda.synchronize()
+        ms32 = g0.elapsed_time(g1)
+        if rank == 0:
+            print(json.dumps({"metric": "cell-stage updates/s (FP32 form, multiblock explosion)", "value":
+                              P.ncell * 4 * args.steps / (ms32 * 1e-3), "unit": "cell-stage updates/s",
+                              "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                              "ms_per_step": ms32 / args.steps, "dtype": "f32", "cells": P.ncell}), flush=True)
+        return
     stream = torch.cuda.Stream()
     dev.set_stream(stream.cuda_stream)
     solver.upload()
@@ -593,6 +668,9 @@ def main():
     if not args.skip_adjoint and ws == 1:
         try:
             adjoint = adjoint_section(stream)
+            a32 = adjoint_section(stream, fd=False, precision="fp32")
+            adjoint["fp32"] = {k: a32[k] for k in ("J", "backward_ms", "plain_forward_ms",
+                                                   "adjoint_cost_over_forward")}
         except Exception as exc:
             adjoint = {"error": str(exc)}
 

@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(TX * TY) k_flux_vjp(ParamsT<T> P, const int4* 
   const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
   const int i = tl.y + ty, j = tl.z + tx;
   if (i > ny || j > nx) return;
-  const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
+  const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
   const bool cart = B->is_cartesian != 0;
   const T* ia = P.geo.cell[E2D_G_INV_A];
   // dUdt = 0.5*(I_W - I_E + I_S - I_N)/A: a face is the W (S) face of the cell above
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(TX * VTY, 4) k_reconstruct_vjp(ParamsT<T> P, c
                                                               const InstanceState* __restrict__ inst,
                                                               FaceArraysT<T> F, T* __restrict__ st) {
   __shared__ T sW[4][VTY + 2][TX + 2];
-  const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
+  const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
   const int4 tl = tiles[blockIdx.x];
   const E2DBlock* B = P.blocks + tl.x;
   const InstanceState* I = inst + B->instance;
@@ -539,7 +539,7 @@ __global__ void __launch_bounds__(TX * TY) k_adjoint_gather(ParamsT<T> P, const 
   if (RECON == E2D_RECON_PRIMITIVE) {
     T q[4];
     load_cell(U, P.ncell, c, q);
-    const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
+    const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
     ly[0] = T(0); ly[1] = T(0); ly[2] = T(0); ly[3] = T(0);
     cons_to_prim_vjp(q, G, lr, ly);
   } else {
@@ -592,7 +592,7 @@ __global__ void __launch_bounds__(OBJ_THREADS) k_side_pressure(ParamsT<T> P, int
                                                                double* __restrict__ J) {
   const E2DBlock* B = P.blocks + b;
   const int n = (side == E2D_E || side == E2D_W) ? B->ny : B->nx;
-  const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
+  const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
   double acc = 0.0;
   for (int k = threadIdx.x; k < n; k += OBJ_THREADS) {
     int64_t c, f;
@@ -629,7 +629,7 @@ __global__ void k_side_pressure_grad(ParamsT<T> P, int b, int side, const T* __r
   side_cell_face<T>(B, side, k, c, f, vert);
   const T len = vert ? P.geo.vface[E2D_F_L][f] : P.geo.hface[E2D_F_L][f];
   const T rho = U[c], u = U[P.ncell + c] / rho, v = U[2 * P.ncell + c] / rho;
-  const T g = T(coef) * len * T(P.gm1);
+  const T g = T(coef) * len * P.gas[1];
   lam[c] += g * T(0.5) * (u * u + v * v);
   lam[P.ncell + c] -= g * u;
   lam[2 * P.ncell + c] -= g * v;

@@ -176,6 +176,10 @@ static int init_path(E2DSolver* h) {
   p.P.gm1 = cfg->gm1;
   p.P.gm = cfg->gamma / (cfg->gamma - 1.0);
   p.P.k = 1.0 / (cfg->gamma - 1.0);
+  p.P.gas[0] = T(p.P.gamma);
+  p.P.gas[1] = T(p.P.gm1);
+  p.P.gas[2] = T(p.P.gm);
+  p.P.gas[3] = T(p.P.k);
   p.P.cfl = cfg->cfl;
   p.P.flux = cfg->flux;
   p.P.limiter = cfg->limiter;

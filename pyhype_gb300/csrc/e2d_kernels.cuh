@@ -60,6 +60,7 @@ struct ParamsT {
   int64_t ncell, nvface, nhface;
   DevGeometryT<T> geo;
   double gamma, gm1, gm, k, cfl;
+  T gas[4];                 // gamma, gamma-1, gamma/(gamma-1), 1/(gamma-1) in the path's type
   int flux, limiter, recon;
 };
 

@@ -153,7 +153,7 @@ template <typename T, int LIM, int RECON, bool DBG, int RTY>
 __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4 tl, const T* __restrict__ U,
                                                  const InstanceState* __restrict__ inst, const FaceArraysT<T>& F,
                                                  const DebugOutT<T>& dbg, T (&sW)[4][RTY + 2][TX + 2]) {
-  const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
+  const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
   const E2DBlock* B = P.blocks + tl.x;
   const InstanceState* I = inst + B->instance;
   if (!I->active) return;
@@ -348,7 +348,7 @@ __device__ __forceinline__ void flux_tile(const ParamsT<T>& P, const int4 tl, co
   const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
   const int i = tl.y + ty, j = tl.z + tx;
   if (i > ny || j > nx) return;
-  const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
+  const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
   const bool cart = B->is_cartesian != 0;
   if (i < ny) {
     const int64_t f = vf_at(B, i, j);
@@ -495,9 +495,9 @@ __global__ void __launch_bounds__(TX * TY) k_dt(ParamsT<T> P, const int4* __rest
     const int64_t c = cell_at(B, i, j);
     T q[4], w[4];
     load_cell(U, P.ncell, c, q);
-    const Gas<T> G{T(P.gamma), T(P.gm1), T(P.gm), T(P.k)};
+    const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
     cons_to_prim(q, G, w);
-    const T a = sqrt(T(P.gamma) * w[3] / w[0]);
+    const T a = sqrt(P.gas[0] * w[3] / w[0]);
     const T tx_ = P.geo.cell[E2D_G_CFL_DX][c] / (fabs(w[1]) + a);
     const T ty_ = P.geo.cell[E2D_G_CFL_DY][c] / (fabs(w[2]) + a);
     m = double(vmin(tx_, ty_));  // the reduction itself is FP64 on every path
