@@ -379,6 +379,12 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
   h->hblocks.assign(blocks, blocks + cfg->nblocks);
 
   h->prec = cfg->precision;
+  if (h->prec == E2D_FP32) {
+    // FP32 defaults measured on GB300 (2x4x1024^2): 4-row reconstruction tiles at 4
+    // CTAs/SM and the persistent flux grid at 6 CTAs/SM
+    h->kr = KernelChoice{3, false};
+    h->kf = KernelChoice{2, true};
+  }
   if (int e = (h->prec == E2D_FP32 ? upload_geometry<float>(h, geo) : upload_geometry<double>(h, geo)))
     return bail(e);
   // block table with MIXED side coordinates moved to the device
@@ -731,12 +737,16 @@ int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps, int
   k_reset_real<<<1, 1, 0, h->stream>>>(h->real);
   CK(cudaGetLastError());
   // steps per host check: enough to amortise the launch of a graph, few enough that
-  // the inactive tail after t_final is cheap
-  const int chunk = max_steps < 8 ? (max_steps > 0 ? max_steps : 1) : 8;
-  cudaGraphExec_t gx = nullptr;
-  if (int e = get_graph(h, chunk, &gx)) return e;
+  // the inactive tail after t_final is cheap; the last chunk is cut to max_steps (every
+  // active instance advances one step per replayed step, so none needs more)
+  int64_t launched = 0;
   for (;;) {
+    const int64_t left = (int64_t)max_steps - launched;
+    const int chunk = left >= 8 ? 8 : (left > 0 ? (int)left : 1);
+    cudaGraphExec_t gx = nullptr;
+    if (int e = get_graph(h, chunk, &gx)) return e;
     CK(cudaGraphLaunch(gx, h->stream));
+    launched += chunk;
     CK(cudaMemcpyAsync(h->hinst.data(), h->inst, sizeof(InstanceState) * ninst, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     bool any = false, halted = false;
