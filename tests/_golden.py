@@ -20,14 +20,22 @@ def fingerprint(arrays) -> str:
     return h.hexdigest()[:32]
 
 
-def _device_bc(name: str, side: str):
+def _device_bc(name: str, side: str, W=None):
     """Device boundary condition for the fixtures' custom reference BC objects (the
-    double-Mach setup of make_golden.py)."""
+    double-Mach setup and the supersonic-wedge inlet of make_golden.py).  ``W`` is a
+    Dirichlet side's recorded non-dimensional primitive state."""
     from pyhype_gb300.configs import double_mach_bcs
 
     west, south, north = double_mach_bcs()
     if name == "Dirichlet":
-        return west()
+        if W is None:
+            return west()
+        from pyhype_gb300.boundary_conditions.base import PrimitiveDirichletBC
+        from pyhype_gb300.fluids import Air
+        from pyhype_gb300.states import PrimitiveState
+
+        # already non-dimensional: the unit far field makes the class's scaling exact
+        return PrimitiveDirichletBC(PrimitiveState(Air(1.0, 1.0), array=np.asarray(W, dtype=float).reshape(1, 1, 4)))
     if name == "Switch":
         return {"S": south, "N": north}[side]()
     return None if name == "None" else name
@@ -42,7 +50,8 @@ def mesh_dict(z) -> dict:
         for s, side in enumerate("EWNS"):
             nb = int(z["neighbors"][k, s])
             d["Neighbor" + side] = None if nb < 0 else nb
-            d["BCType" + side] = _device_bc(str(z["bc"][k, s]), side)
+            W = z["dirichlet_W"][k, s] if "dirichlet_W" in z.files else None
+            d["BCType" + side] = _device_bc(str(z["bc"][k, s]), side, W)
         for corner in ("NE", "NW", "SE", "SW"):
             d["Neighbor" + corner] = None
             d["BCType" + corner] = None

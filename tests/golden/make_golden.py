@@ -252,6 +252,42 @@ def dmr_example_mesh():
     )
 
 
+def wedge_mesh():
+    """examples/supersonic_wedge/mesh.py:6-77: a 2 x 2 square and a 15-degree wedge
+    block, Mach-2 inlet on the west (the reference's PrimitiveDirichletBC state, made
+    non-dimensional as that class does, applied through the harness Dirichlet BC).
+    The example numbers its blocks 1 and 2, which the reference's block builder
+    cannot read (blocks/base.py:531 looks blocks up from 0); they are 0 and 1 here."""
+    W = PrimitiveState(fluid=AIR, array=np.array([1.0, 2.0, 0.0, 1 / AIR.gamma()]).reshape((1, 1, 4)))
+    W.make_non_dimensional()
+    inlet = DirichletBC(W.data.reshape(4).copy())
+    tan15 = np.tan(15 * np.pi / 180)
+    b1 = {"nBLK": 0, "NW": [0, 2], "NE": [2, 2], "SW": [0, 0], "SE": [2, 0],
+          "NeighborE": 1, "NeighborW": None, "NeighborN": None, "NeighborS": None,
+          "BCTypeE": None, "BCTypeW": inlet, "BCTypeN": "OutletDirichlet", "BCTypeS": "Reflection"}
+    b2 = {"nBLK": 1, "NW": [2, 2], "NE": [4, 2 + 2 * tan15], "SW": [2, 0], "SE": [4, 2 * tan15],
+          "NeighborE": None, "NeighborW": 0, "NeighborN": None, "NeighborS": None,
+          "BCTypeE": "OutletDirichlet", "BCTypeW": None, "BCTypeN": "OutletDirichlet", "BCTypeS": "Reflection"}
+    for b in (b1, b2):
+        for c in ("NE", "NW", "SE", "SW"):
+            b["Neighbor" + c] = None
+            b["BCType" + c] = None
+    return {0: b1, 1: b2}
+
+
+class FloodIC(InitialCondition):
+    """initial_conditions/supersonic_flood.py:32-54 at the block's full shape."""
+
+    def __init__(self, W):
+        self.W = W
+
+    def apply_to_block(self, block):
+        s = PrimitiveState(fluid=block.config.fluid, array=np.array(self.W).reshape((1, 1, 4))).to_type(
+            ConservativeState)
+        block.state.data = np.broadcast_to(s.data, block.state.data.shape).copy()
+        block.state.make_non_dimensional()
+
+
 def rect_mesh(nbx, nby, east, north, bc="Reflection"):
     return RectagularMeshGenerator.generate(
         BCE=[bc], BCW=[bc], BCN=[bc], BCS=[bc],
@@ -298,6 +334,9 @@ CASES = {
     "dmr_example": (dict(nx=12, ny=12, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState, time_integrator="RK2", CFL=0.4), dmr_example_mesh, lambda: DMRExampleIC(), 5, "all", 2, None),
     "ssprk2_hlll": (dict(nx=20, ny=16, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState, CFL=0.4), lambda: single_block(0, 10, 0, 8), lambda: ExplosionIC(**MOVING), 4, "all", None, [[1], [0.5, 0.5]]),
 }
+CASES["wedge"] = (dict(nx=16, ny=16, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState,
+                      time_integrator="RK2", CFL=0.3), wedge_mesh, lambda: FloodIC([1.0, 2.0, 0.0, 1 / AIR.gamma()]),
+                  8, "all", 3, None)
 CASES["dmr5"] = (dict(nx=16, ny=20, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState, CFL=0.4,
                      t_final=0.2, fluid=AIR_UNIT), lambda: dmr_mesh(5), lambda: DMRIC(), 8, "all", 3, [[1], [0.5, 0.5]])
 for _ti in ("ExplicitEuler1", "RK2", "Ralston2", "RK3", "RK3SSP", "Ralston3", "Ralston4", "DormandPrince5"):
@@ -315,6 +354,7 @@ def encode_mesh(mesh_cfg, out):
     corners = np.zeros((len(names), 4, 2))
     nbr = np.full((len(names), 4), -1, dtype=np.int64)
     bc = np.empty((len(names), 4), dtype="U16")
+    dirichlet = np.zeros((len(names), 4, 4))
     for k, n in enumerate(names):
         d = mesh_cfg[n]
         for c, key in enumerate(("SW", "SE", "NW", "NE")):
@@ -327,11 +367,13 @@ def encode_mesh(mesh_cfg, out):
                 bc[k, s] = "Switch"
             elif isinstance(b, DirichletBC):
                 bc[k, s] = "Dirichlet"
+                dirichlet[k, s] = b.W
             else:
                 bc[k, s] = "None" if b is None else str(b)
     out["corners"] = corners
     out["neighbors"] = nbr
     out["bc"] = bc
+    out["dirichlet_W"] = dirichlet  # non-dimensional primitive states of Dirichlet sides
 
 
 def record_geometry(solver, out):
