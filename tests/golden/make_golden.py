@@ -275,6 +275,20 @@ def wedge_mesh():
     return {0: b1, 1: b2}
 
 
+def jet_mesh():
+    """examples/jet/mesh.py:1-54: nine blocks stacked in y, the middle one's west side
+    a subsonic Dirichlet inlet (non-dimensional, as the reference's class makes it),
+    slip walls on the rest of the west side, outlets elsewhere."""
+    from pyhype.mesh.base import QuadMeshGenerator
+
+    W = PrimitiveState(fluid=AIR, array=np.array([1.0, 0.1, 0.0, 2.0 / AIR.gamma()]).reshape((1, 1, 4)))
+    W.make_non_dimensional()
+    inlet = DirichletBC(W.data.reshape(4).copy())
+    bcw = ["Slipwall"] * 4 + [inlet] + ["Slipwall"] * 4
+    return QuadMeshGenerator(nx_blk=1, ny_blk=9, BCE=["OutletDirichlet"] * 9, BCW=bcw, BCN=["OutletDirichlet"],
+                             BCS=["OutletDirichlet"], NE=(1, 0.5), SW=(0, 0), NW=(0, 0.5), SE=(1, 0))
+
+
 class FloodIC(InitialCondition):
     """initial_conditions/supersonic_flood.py:32-54 at the block's full shape."""
 
@@ -337,6 +351,9 @@ CASES = {
 CASES["wedge"] = (dict(nx=16, ny=16, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState,
                       time_integrator="RK2", CFL=0.3), wedge_mesh, lambda: FloodIC([1.0, 2.0, 0.0, 1 / AIR.gamma()]),
                   8, "all", 3, None)
+CASES["jet"] = (dict(nx=24, ny=6, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState,
+                    time_integrator="RK2", CFL=0.4), jet_mesh, lambda: FloodIC([1.0, 0.0, 0.0, 1 / AIR.gamma()]),
+                6, "all", 2, None)
 CASES["dmr5"] = (dict(nx=16, ny=20, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState, CFL=0.4,
                      t_final=0.2, fluid=AIR_UNIT), lambda: dmr_mesh(5), lambda: DMRIC(), 8, "all", 3, [[1], [0.5, 0.5]])
 for _ti in ("ExplicitEuler1", "RK2", "Ralston2", "RK3", "RK3SSP", "Ralston3", "Ralston4", "DormandPrince5"):
