@@ -37,7 +37,7 @@ extern "C" {
 #define E2D_API
 #endif
 
-#define E2D_ABI_VERSION 1
+#define E2D_ABI_VERSION 2
 
 /* ---- status codes ---------------------------------------------------------- */
 #define E2D_OK 0
@@ -128,6 +128,9 @@ typedef struct {
   double gamma;              /* 1.4                                     */
   double gm1;                /* gamma - 1 as formed by the host (1.4-1) */
   double cfl;
+  int32_t nqp;               /* face quadrature points per face: 1 (0 = 1), 2, 3
+                                (SolverConfig.fvm_num_quadrature_points)          */
+  int32_t reserved;
 } E2DConfig;
 
 /* Geometry planes (host pointers), each the concatenation over blocks.
@@ -156,10 +159,16 @@ enum e2d_face_plane {
   E2D_F_SIN,        /* sin(theta)                                              */
   E2D_F_NFACE
 };
+#define E2D_MAX_QP 3
 typedef struct {
   const double* cell[E2D_G_NCELL];
   const double* vface[E2D_F_NFACE];
   const double* hface[E2D_F_NFACE];
+  /* With nqp > 1: quadrature point - centroid of point q (in the order of
+     pyhype/mesh/quadratures.py:33-37) per side, [q][0..3] = x for E, W, N, S and
+     [q][4..7] = y, cell planes; unused (NULL) with one point, whose offsets are the
+     E2D_G_HX_* / E2D_G_HY_* planes.                                                */
+  const double* qp[E2D_MAX_QP][8];
 } E2DGeometry;
 
 /* Result of the positivity check (pyhype/solvers/Euler2D.py:310-318). */
@@ -242,8 +251,8 @@ E2D_API int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug
 
 /* ---- adjoint (reverse mode) -------------------------------------------------------
    No counterpart in the reference (it has no differentiation); the forward steps are
-   the functions above.  FP64 path, Roe flux, one instance; any limiter,
-   reconstruction type, side kind and explicit tableau.  Subgradients: min/max take the
+   the functions above.  Roe flux, one instance, one face quadrature point; FP64 or
+   FP32 path, any limiter, reconstruction type, side kind and explicit tableau.  Subgradients: min/max take the
    operand the forward selects, Harten's fix the branch taken, the slope's davg == 0
    branch is constant, a clipped negative limiter value passes nothing back.        */
 

@@ -455,21 +455,27 @@ static void block_residual(const Ctx* C, int b, const double* U, double t, doubl
   const double gm1 = C->cfg->gm1;
   const E2DGeometry* G = C->geo;
   const int64_t nv = (int64_t)ny * (nx + 1), nh = (int64_t)(ny + 1) * nx;
+  /* face quadrature (pyhype/mesh/quadratures.py:33-37): points in the reference's order,
+     weights as Python forms them; the one-point rule's offsets are the HX/HY planes */
+  const int nqp = C->cfg->nqp > 1 ? C->cfg->nqp : 1;
+  const double wq[3][3] = {{2.0, 0.0, 0.0}, {1.0, 1.0, 0.0}, {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0}};
+  const double* qw = wq[nqp - 1];
+#define HOT(side, q, v) ((((side) * nqp + (q)) * 4 + (v)) * n)
 
   Scratch S;
   S.W = malloc(sizeof(double) * 4 * n);
   S.gE = malloc(sizeof(double) * 4 * ny); S.gW = malloc(sizeof(double) * 4 * ny);
   S.gN = malloc(sizeof(double) * 4 * nx); S.gS = malloc(sizeof(double) * 4 * nx);
-  S.oE = malloc(sizeof(double) * 4 * ny); S.oW = malloc(sizeof(double) * 4 * ny);
-  S.oN = malloc(sizeof(double) * 4 * nx); S.oS = malloc(sizeof(double) * 4 * nx);
+  S.oE = malloc(sizeof(double) * 4 * nqp * ny); S.oW = malloc(sizeof(double) * 4 * nqp * ny);
+  S.oN = malloc(sizeof(double) * 4 * nqp * nx); S.oS = malloc(sizeof(double) * 4 * nqp * nx);
   S.iEW = malloc(sizeof(double) * 4 * nv);
   S.iNS = malloc(sizeof(double) * 4 * nh);
   S.gx = malloc(sizeof(double) * 4 * n); S.gy = malloc(sizeof(double) * 4 * n);
-  S.hot = malloc(sizeof(double) * 16 * n);
+  S.hot = malloc(sizeof(double) * 16 * nqp * n);
   S.phi = malloc(sizeof(double) * 4 * n);
-  S.face = malloc(sizeof(double) * 16 * n);
-  S.vf = malloc(sizeof(double) * 4 * nv);
-  S.hf = malloc(sizeof(double) * 4 * nh);
+  S.face = malloc(sizeof(double) * 16 * nqp * n);
+  S.vf = malloc(sizeof(double) * 4 * nqp * nv);
+  S.hf = malloc(sizeof(double) * 4 * nqp * nh);
 
   /* 1. reconstruction-type state (QuadBlock -> ReconstructionBlock.from_block) */
 #pragma omp parallel for schedule(static)
@@ -529,10 +535,12 @@ static void block_residual(const Ctx* C, int b, const double* U, double t, doubl
         double gy = (e * ylE + w * ylW + nn * ylN + s * ylS) * a;
         S.gx[v * n + loc] = gx;
         S.gy[v * n + loc] = gy;
-        for (int side = 0; side < 4; ++side) {
-          double dx = G->cell[E2D_G_HX_E + side][c], dy = G->cell[E2D_G_HY_E + side][c];
-          S.hot[(side * 4 + v) * n + loc] = gx * dx + gy * dy;
-        }
+        for (int side = 0; side < 4; ++side)
+          for (int q = 0; q < nqp; ++q) {
+            double dx = nqp == 1 ? G->cell[E2D_G_HX_E + side][c] : G->qp[q][side][c];
+            double dy = nqp == 1 ? G->cell[E2D_G_HY_E + side][c] : G->qp[q][4 + side][c];
+            S.hot[HOT(side, q, v) + loc] = gx * dx + gy * dy;
+          }
       }
     }
   /* 5. limiter */
@@ -550,15 +558,17 @@ static void block_residual(const Ctx* C, int b, const double* U, double t, doubl
         double mx = np_max(np_max(np_max(np_max(u0, we), ea), so), no);
         double mn = np_min(np_min(np_min(np_min(u0, we), ea), so), no);
         double dmax = mx - u0, dmin = mn - u0;
+        /* minimum over the E, W, N, S quadrature points in that order */
         double ph = 0.0;
-        for (int side = 0; side < 4; ++side) {
-          double davg = (u0 + S.hot[(side * 4 + v) * n + loc]) - u0;
-          double s = 1.0;
-          if (davg > 0) s = dmax / davg;
-          else if (davg < 0) s = dmin / davg;
-          double p = psi(lim, s);
-          ph = side == 0 ? p : np_min(ph, p);
-        }
+        for (int side = 0; side < 4; ++side)
+          for (int q = 0; q < nqp; ++q) {
+            double davg = (u0 + S.hot[HOT(side, q, v) + loc]) - u0;
+            double s = 1.0;
+            if (davg > 0) s = dmax / davg;
+            else if (davg < 0) s = dmin / davg;
+            double p = psi(lim, s);
+            ph = (side == 0 && q == 0) ? p : np_min(ph, p);
+          }
         S.phi[v * n + loc] = (ph < 0) ? 0.0 : ph;
       }
     }
@@ -568,41 +578,44 @@ static void block_residual(const Ctx* C, int b, const double* U, double t, doubl
     for (int j = 0; j < nx; ++j) {
       int64_t loc = (int64_t)i * nx + j;
       for (int side = 0; side < 4; ++side)
-        for (int v = 0; v < 4; ++v)
-          S.face[(side * 4 + v) * n + loc] = Wv(v, i, j) + S.phi[v * n + loc] * S.hot[(side * 4 + v) * n + loc];
+        for (int q = 0; q < nqp; ++q)
+          for (int v = 0; v < 4; ++v)
+            S.face[HOT(side, q, v) + loc] = Wv(v, i, j) + S.phi[v * n + loc] * S.hot[HOT(side, q, v) + loc];
     }
   /* 7. outside states of the block boundary faces (fvm/base.py:305-325 + BC) */
   for (int side = 0; side < 4; ++side) {
     int len = (side == E2D_E || side == E2D_W) ? ny : nx;
     double* dst = side == E2D_E ? S.oE : side == E2D_W ? S.oW : side == E2D_N ? S.oN : S.oS;
     const double* gh = side == E2D_E ? S.gE : side == E2D_W ? S.gW : side == E2D_N ? S.gN : S.gS;
-    for (int k = 0; k < len; ++k) {
-      const double *gd, *fd;
-      int kind = side_cell_kind(B, side, k, t, &gd, &fd);
-      double* o = dst + 4 * k;
-      if (kind == E2D_SIDE_NEIGHBOR || kind == E2D_SIDE_COPY) {
-        for (int v = 0; v < 4; ++v) o[v] = gh[4 * k + v];
-      } else if (kind == E2D_SIDE_DIRICHLET) {
-        for (int v = 0; v < 4; ++v) o[v] = fd[v];
-      } else {
-        int64_t loc = own_boundary_cell(B, side, k) - B->cell_offset;
-        for (int v = 0; v < 4; ++v) o[v] = S.face[(side * 4 + v) * n + loc];
-        if (kind == E2D_SIDE_REFLECT) {
-          double c, s;
-          boundary_cs(C, B, side, k, &c, &s);
-          reflect(o, c, s);
+    for (int q = 0; q < nqp; ++q)
+      for (int k = 0; k < len; ++k) {
+        const double *gd, *fd;
+        int kind = side_cell_kind(B, side, k, t, &gd, &fd);
+        double* o = dst + 4 * ((int64_t)q * len + k);
+        if (kind == E2D_SIDE_NEIGHBOR || kind == E2D_SIDE_COPY) {
+          for (int v = 0; v < 4; ++v) o[v] = gh[4 * k + v];
+        } else if (kind == E2D_SIDE_DIRICHLET) {
+          for (int v = 0; v < 4; ++v) o[v] = fd[v];
+        } else {
+          int64_t loc = own_boundary_cell(B, side, k) - B->cell_offset;
+          for (int v = 0; v < 4; ++v) o[v] = S.face[HOT(side, q, v) + loc];
+          if (kind == E2D_SIDE_REFLECT) {
+            double c, s;
+            boundary_cs(C, B, side, k, &c, &s);
+            reflect(o, c, s);
+          }
         }
       }
-    }
   }
   /* 8. east-west sweep */
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < ny; ++i)
-    for (int j = 0; j <= nx; ++j) {
+    for (int j = 0; j <= nx; ++j)
+     for (int q = 0; q < nqp; ++q) {
       double L[4], R[4], WL[4], WR[4], F[4];
       for (int v = 0; v < 4; ++v) {
-        L[v] = j == 0 ? S.oW[4 * i + v] : S.face[(E2D_E * 4 + v) * n + (int64_t)i * nx + j - 1];
-        R[v] = j == nx ? S.oE[4 * i + v] : S.face[(E2D_W * 4 + v) * n + (int64_t)i * nx + j];
+        L[v] = j == 0 ? S.oW[4 * ((int64_t)q * ny + i) + v] : S.face[HOT(E2D_E, q, v) + (int64_t)i * nx + j - 1];
+        R[v] = j == nx ? S.oE[4 * ((int64_t)q * ny + i) + v] : S.face[HOT(E2D_W, q, v) + (int64_t)i * nx + j];
       }
       int64_t f = VF(B, i, j);
       double c = G->vface[E2D_F_COS][f], s = G->vface[E2D_F_SIN][f];
@@ -610,7 +623,7 @@ static void block_residual(const Ctx* C, int b, const double* U, double t, doubl
       recon_to_prim(L, recon, gm1, WL);
       recon_to_prim(R, recon, gm1, WR);
       face_flux(C, WL, WR, F);
-      if (dbg) {
+      if (dbg && q == 0) {  /* intermediates of the first quadrature point */
         for (int v = 0; v < 4; ++v) {
           if (dbg->vL) dbg->vL[v * C->nvface + f] = WL[v];
           if (dbg->vR) dbg->vR[v * C->nvface + f] = WR[v];
@@ -619,18 +632,19 @@ static void block_residual(const Ctx* C, int b, const double* U, double t, doubl
       }
       if (!B->is_cartesian) unrotate(F, c, s);
       for (int v = 0; v < 4; ++v) {
-        S.vf[v * nv + (int64_t)i * (nx + 1) + j] = F[v];
-        if (dbg && dbg->vflux) dbg->vflux[v * C->nvface + f] = F[v];
+        S.vf[((int64_t)q * 4 + v) * nv + (int64_t)i * (nx + 1) + j] = F[v];
+        if (dbg && dbg->vflux && q == 0) dbg->vflux[v * C->nvface + f] = F[v];
       }
-    }
+     }
   /* 9. north-south sweep */
 #pragma omp parallel for schedule(static)
   for (int j = 0; j < nx; ++j)
-    for (int i = 0; i <= ny; ++i) {
+    for (int i = 0; i <= ny; ++i)
+     for (int q = 0; q < nqp; ++q) {
       double L[4], R[4], WL[4], WR[4], F[4];
       for (int v = 0; v < 4; ++v) {
-        L[v] = i == 0 ? S.oS[4 * j + v] : S.face[(E2D_N * 4 + v) * n + (int64_t)(i - 1) * nx + j];
-        R[v] = i == ny ? S.oN[4 * j + v] : S.face[(E2D_S * 4 + v) * n + (int64_t)i * nx + j];
+        L[v] = i == 0 ? S.oS[4 * ((int64_t)q * nx + j) + v] : S.face[HOT(E2D_N, q, v) + (int64_t)(i - 1) * nx + j];
+        R[v] = i == ny ? S.oN[4 * ((int64_t)q * nx + j) + v] : S.face[HOT(E2D_S, q, v) + (int64_t)i * nx + j];
       }
       int64_t f = HF(B, i, j);
       double c = G->hface[E2D_F_COS][f], s = G->hface[E2D_F_SIN][f];
@@ -639,7 +653,7 @@ static void block_residual(const Ctx* C, int b, const double* U, double t, doubl
       recon_to_prim(L, recon, gm1, WL);
       recon_to_prim(R, recon, gm1, WR);
       face_flux(C, WL, WR, F);
-      if (dbg) {
+      if (dbg && q == 0) {
         for (int v = 0; v < 4; ++v) {
           if (dbg->hL) dbg->hL[v * C->nhface + f] = WL[v];
           if (dbg->hR) dbg->hR[v * C->nhface + f] = WR[v];
@@ -649,11 +663,12 @@ static void block_residual(const Ctx* C, int b, const double* U, double t, doubl
       if (B->is_cartesian) unrotate90(F);
       else unrotate(F, c, s);
       for (int v = 0; v < 4; ++v) {
-        S.hf[v * nh + (int64_t)i * nx + j] = F[v];
-        if (dbg && dbg->hflux) dbg->hflux[v * C->nhface + f] = F[v];
+        S.hf[((int64_t)q * 4 + v) * nh + (int64_t)i * nx + j] = F[v];
+        if (dbg && dbg->hflux && q == 0) dbg->hflux[v * C->nhface + f] = F[v];
       }
-    }
-  /* 10. integration over faces (1-point rule, weight 2) and dUdt */
+     }
+  /* 10. Gauss integration over faces, L * (sum_q w_q F_q) summed from 0 in point order
+     (fvm/base.py:171-190), and dUdt */
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < ny; ++i)
     for (int j = 0; j < nx; ++j) {
@@ -662,13 +677,18 @@ static void block_residual(const Ctx* C, int b, const double* U, double t, doubl
       double LS = G->hface[E2D_F_L][HF(B, i, j)], LN = G->hface[E2D_F_L][HF(B, i + 1, j)];
       double A = G->cell[E2D_G_A][c];
       for (int v = 0; v < 4; ++v) {
-        double IW = LW * (0.0 + 2 * S.vf[v * nv + (int64_t)i * (nx + 1) + j]);
-        double IE = LE * (0.0 + 2 * S.vf[v * nv + (int64_t)i * (nx + 1) + j + 1]);
-        double IS = LS * (0.0 + 2 * S.hf[v * nh + (int64_t)i * nx + j]);
-        double IN = LN * (0.0 + 2 * S.hf[v * nh + (int64_t)(i + 1) * nx + j]);
+        double sW = 0.0, sE = 0.0, sS = 0.0, sN = 0.0;
+        for (int q = 0; q < nqp; ++q) {
+          sW = sW + qw[q] * S.vf[((int64_t)q * 4 + v) * nv + (int64_t)i * (nx + 1) + j];
+          sE = sE + qw[q] * S.vf[((int64_t)q * 4 + v) * nv + (int64_t)i * (nx + 1) + j + 1];
+          sS = sS + qw[q] * S.hf[((int64_t)q * 4 + v) * nh + (int64_t)i * nx + j];
+          sN = sN + qw[q] * S.hf[((int64_t)q * 4 + v) * nh + (int64_t)(i + 1) * nx + j];
+        }
+        double IW = LW * sW, IE = LE * sE, IS = LS * sS, IN = LN * sN;
         dudt[v * C->ncell + c] = 0.5 * (IW - IE + IS - IN) / A;
       }
     }
+#undef HOT
   if (dbg) {
     for (int v = 0; v < 4; ++v)
       for (int64_t l = 0; l < n; ++l) {

@@ -84,7 +84,7 @@ def load(path: Optional[str] = None):
     L.e2d_adjoint_forward.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, vp, vp,
                                       ctypes.POINTER(ctypes.c_double)]
     L.e2d_adjoint_backward.argtypes = [vp, vp]
-    if L.e2d_abi_version() != 1:
+    if L.e2d_abi_version() != 2:
         raise RuntimeError("libeuler2d.so ABI version mismatch")
     _lib = L
     return L

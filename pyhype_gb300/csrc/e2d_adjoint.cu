@@ -87,6 +87,7 @@ int check_supported(E2DSolver* h) {
   if (h->cfg.flux != E2D_FLUX_ROE) return fail(E2D_ERR_UNSUPPORTED, "the adjoint supports the Roe flux");
   if (h->hinst.size() != 1) return fail(E2D_ERR_UNSUPPORTED, "the adjoint runs on single-instance problems");
   if (h->nstages < 1) return fail(E2D_ERR_INVALID, "no tableau set");
+  if (h->cfg.nqp > 1) return fail(E2D_ERR_UNSUPPORTED, "the adjoint is built for one face quadrature point");
   return 0;
 }
 

@@ -121,7 +121,9 @@ template <typename T>
 static int upload_geometry(E2DSolver* h, const E2DGeometry* geo) {
   PathT<T>& p = path<T>(h);
   const int64_t ncell = h->ncell, nv = h->nvface, nh = h->nhface;
-  const size_t ngeo = (size_t)E2D_G_NCELL * ncell + (size_t)E2D_F_NFACE * (nv + nh);
+  const int nqp = h->cfg.nqp > 1 ? h->cfg.nqp : 1;
+  const size_t nq = nqp > 1 ? (size_t)8 * nqp * ncell : 0;
+  const size_t ngeo = (size_t)E2D_G_NCELL * ncell + (size_t)E2D_F_NFACE * (nv + nh) + nq;
   if (int e = h->alloc(&p.geo, ngeo)) return e;
   std::vector<T> tmp;
   auto put = [&](T* dst, const double* src, int64_t n) -> int {
@@ -147,6 +149,15 @@ static int upload_geometry(E2DSolver* h, const E2DGeometry* geo) {
     if (int e = put(q, geo->hface[k], nh)) return e;
     p.P.geo.hface[k] = q;
   }
+  for (int qi = 0; qi < E2D_MAX_QP; ++qi)
+    for (int k = 0; k < 8; ++k) p.P.geo.qp[qi][k] = nullptr;
+  if (nqp > 1)
+    for (int qi = 0; qi < nqp; ++qi)
+      for (int k = 0; k < 8; ++k, q += ncell) {
+        if (!geo->qp[qi][k]) return fail(E2D_ERR_INVALID, "quadrature point %d plane %d missing", qi, k);
+        if (int e = put(q, geo->qp[qi][k], ncell)) return e;
+        p.P.geo.qp[qi][k] = q;
+      }
   return 0;
 }
 
@@ -155,11 +166,12 @@ template <typename T>
 static int init_path(E2DSolver* h) {
   PathT<T>& p = path<T>(h);
   const int64_t nv = h->nvface, nh = h->nhface;
-  if (int e = h->alloc(&p.F.vL, 4 * (size_t)nv)) return e;
-  if (int e = h->alloc(&p.F.vR, 4 * (size_t)nv)) return e;
+  const int nqp = h->cfg.nqp > 1 ? h->cfg.nqp : 1;
+  if (int e = h->alloc(&p.F.vL, 4 * (size_t)nqp * nv)) return e;
+  if (int e = h->alloc(&p.F.vR, 4 * (size_t)nqp * nv)) return e;
   if (int e = h->alloc(&p.F.vI, 4 * (size_t)nv)) return e;
-  if (int e = h->alloc(&p.F.hL, 4 * (size_t)nh)) return e;
-  if (int e = h->alloc(&p.F.hR, 4 * (size_t)nh)) return e;
+  if (int e = h->alloc(&p.F.hL, 4 * (size_t)nqp * nh)) return e;
+  if (int e = h->alloc(&p.F.hR, 4 * (size_t)nqp * nh)) return e;
   if (int e = h->alloc(&p.F.hI, 4 * (size_t)nh)) return e;
   p.S.comp = nullptr;
   if (h->prec == E2D_FP32) {
@@ -184,6 +196,10 @@ static int init_path(E2DSolver* h) {
   p.P.flux = cfg->flux;
   p.P.limiter = cfg->limiter;
   p.P.recon = cfg->recon;
+  // Gauss-Legendre weights as the reference's Python forms them (quadratures.py:33-37)
+  const double w[3][3] = {{2.0, 0.0, 0.0}, {1.0, 1.0, 0.0}, {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0}};
+  p.P.nqp = nqp;
+  for (int k = 0; k < E2D_MAX_QP; ++k) p.P.qw[k] = T(w[nqp - 1][k]);
   return 0;
 }
 
@@ -322,6 +338,7 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
   if (cfg->precision != E2D_FP64 && cfg->precision != E2D_FP32) return fail(E2D_ERR_INVALID, "unknown precision");
   if (cfg->flux < 0 || cfg->flux > 2 || cfg->limiter < 0 || cfg->limiter > 3 || cfg->recon < 0 || cfg->recon > 1)
     return fail(E2D_ERR_INVALID, "unknown flux/limiter/reconstruction code");
+  if (cfg->nqp < 0 || cfg->nqp > E2D_MAX_QP) return fail(E2D_ERR_INVALID, "nqp must be 1, 2 or 3");
   const int ninst = cfg->ninstances > 0 ? cfg->ninstances : 1;
   // validate the block table before anything touches the device
   int64_t ncell = 0, nv = 0, nh = 0;
@@ -616,6 +633,8 @@ int e2d_step(E2DHandle h, double dt, double t) {
 
 int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* d) {
   if (!h || !dudt_dev) return fail(E2D_ERR_INVALID, "null argument");
+  if (d && h->cfg.nqp > 1)
+    return fail(E2D_ERR_UNSUPPORTED, "per-operator outputs are built for one face quadrature point");
   const int ninst = (int)h->hinst.size();
   CK(launch_set_time(h->inst, ninst, t, 0.0, h->stream));
   StageProgram none{};

@@ -18,10 +18,12 @@ struct DevGeometryT {
   const T* cell[E2D_G_NCELL];
   const T* vface[E2D_F_NFACE];
   const T* hface[E2D_F_NFACE];
+  const T* qp[E2D_MAX_QP][8];  // with nqp > 1: point - centroid, x (E, W, N, S) then y
 };
 
-// Face-indexed left/right states (primitive, rotated into the face frame) and the
-// integrated face fluxes L*(2F), 4 planes each.
+// Face-indexed left/right states (primitive, rotated into the face frame), 4 planes
+// per face quadrature point (point q at plane offset 4q), and the integrated face
+// fluxes L * sum_q w_q F_q, 4 planes.
 template <typename T>
 struct FaceArraysT {
   T* vL;
@@ -62,6 +64,8 @@ struct ParamsT {
   double gamma, gm1, gm, k, cfl;
   T gas[4];                 // gamma, gamma-1, gamma/(gamma-1), 1/(gamma-1) in the path's type
   int flux, limiter, recon;
+  int nqp;                  // face quadrature points (1, 2, 3)
+  T qw[E2D_MAX_QP];         // their weights (2; 1, 1; 5/9, 8/9, 5/9)
 };
 
 // One update of the RK stage program: dst = src + (dt * a) * k (buffers by id).

@@ -337,6 +337,198 @@ __global__ void __launch_bounds__(TX * RTY, MINB) k_reconstruct(ParamsT<T> P, co
 }
 
 // --------------------------------------------------------------------------------------
+// K1 with 2 or 3 face quadrature points (SolverConfig.fvm_num_quadrature_points,
+// pyhype/mesh/quadratures.py:33-90, fvm/SecondOrderMUSCL.py:128-158): the high-order
+// term is evaluated at every point of every face, the limiter takes the minimum over
+// the E, W, N, S points in that order (limiters/base.py:147-187), and a limited state
+// is written per point (face-array plane offset 4q).  The high-order term is formed
+// once for the limiter and once more for the face state, by the same expression.
+// --------------------------------------------------------------------------------------
+template <typename T, int LIM, int RECON, int NQP>
+__global__ void __launch_bounds__(TX * TY) k_reconstruct_qp(ParamsT<T> P, const int4* __restrict__ tiles,
+                                                            const T* __restrict__ U,
+                                                            const InstanceState* __restrict__ inst,
+                                                            FaceArraysT<T> F) {
+  __shared__ T sW[4][TY + 2][TX + 2];
+  const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
+  const int4 tl = tiles[blockIdx.x];
+  const E2DBlock* B = P.blocks + tl.x;
+  const InstanceState* I = inst + B->instance;
+  if (!I->active) return;
+  const double t = I->t;
+  const int nx = B->nx, ny = B->ny;
+  const int i0 = tl.y, j0 = tl.z;
+  for (int p = threadIdx.x; p < (TY + 2) * (TX + 2); p += TX * TY) {
+    const int ly = p / (TX + 2), lx = p - ly * (TX + 2);
+    const int gi = i0 + ly - 1, gj = j0 + lx - 1;
+    const bool in_i = gi >= 0 && gi < ny, in_j = gj >= 0 && gj < nx;
+    T q[4], r[4] = {T(0), T(0), T(0), T(0)};
+    bool ok = true;
+    if (in_i && in_j) load_cell(U, P.ncell, cell_at(B, gi, gj), q);
+    else if (in_i && gj == -1) ghost_cons(P, B, E2D_W, gi, U, t, q);
+    else if (in_i && gj == nx) ghost_cons(P, B, E2D_E, gi, U, t, q);
+    else if (in_j && gi == -1) ghost_cons(P, B, E2D_S, gj, U, t, q);
+    else if (in_j && gi == ny) ghost_cons(P, B, E2D_N, gj, U, t, q);
+    else ok = false;
+    if (ok) to_recon<RECON>(q, G, r);
+    sW[0][ly][lx] = r[0];
+    sW[1][ly][lx] = r[1];
+    sW[2][ly][lx] = r[2];
+    sW[3][ly][lx] = r[3];
+  }
+  __syncthreads();
+
+  const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
+  const int i = i0 + ty, j = j0 + tx;
+  if (i >= ny || j >= nx) return;
+  const int64_t c = cell_at(B, i, j);
+  const int64_t fE = vf_at(B, i, j + 1), fW = vf_at(B, i, j);
+  const int64_t fN = hf_at(B, i + 1, j), fS = hf_at(B, i, j);
+  const T LcE = P.geo.vface[E2D_F_LC][fE], LsE = P.geo.vface[E2D_F_LS][fE];
+  const T LcW = P.geo.vface[E2D_F_LC][fW], LsW = P.geo.vface[E2D_F_LS][fW];
+  const T LcN = P.geo.hface[E2D_F_LC][fN], LsN = P.geo.hface[E2D_F_LS][fN];
+  const T LcS = P.geo.hface[E2D_F_LC][fS], LsS = P.geo.hface[E2D_F_LS][fS];
+  const T ia = P.geo.cell[E2D_G_INV_A][c];
+
+  T gxs[4], gys[4], phs[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    const T w0 = sW[v][ty + 1][tx + 1];
+    const T we = sW[v][ty + 1][tx];
+    const T ea = sW[v][ty + 1][tx + 2];
+    const T so = sW[v][ty][tx + 1];
+    const T no = sW[v][ty + 2][tx + 1];
+    const T ie = T(0.5) * (w0 + ea), iw = T(0.5) * (we + w0);
+    const T in = T(0.5) * (w0 + no), is = T(0.5) * (so + w0);
+    const T gx = (ie * LcE + iw * (-LcW) + in * LcN + is * (-LcS)) * ia;
+    const T gy = (ie * LsE + iw * (-LsW) + in * LsN + is * (-LsS)) * ia;
+    const T dmax = vmax(vmax(vmax(vmax(w0, we), ea), so), no) - w0;
+    const T dmin = vmin(vmin(vmin(vmin(w0, we), ea), so), no) - w0;
+    T ph = T(0);
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+#pragma unroll
+      for (int q = 0; q < NQP; ++q) {
+        const T hot = gx * P.geo.qp[q][s][c] + gy * P.geo.qp[q][4 + s][c];
+        T davg;
+        if constexpr (sizeof(T) == 4) {
+          const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
+          davg = (fabs(hot) < half_ulp64) ? T(0) : hot;
+        } else {
+          davg = (w0 + hot) - w0;
+        }
+        const bool pos = is_pos(davg), neg = is_neg(davg);
+        const T qs = (pos ? dmax : dmin) / ((pos || neg) ? davg : T(1));
+        const T sl = (pos || neg) ? qs : T(1);
+        const T p = psi<LIM>(sl);
+        ph = (s == 0 && q == 0) ? p : vmin(ph, p);
+      }
+    phs[v] = is_neg(ph) ? T(0) : ph;
+    gxs[v] = gx;
+    gys[v] = gy;
+  }
+
+  const bool cart = B->is_cartesian != 0;
+#pragma unroll
+  for (int s = 0; s < 4; ++s)
+#pragma unroll
+    for (int q = 0; q < NQP; ++q) {
+      T fq[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const T hot = gxs[v] * P.geo.qp[q][s][c] + gys[v] * P.geo.qp[q][4 + s][c];
+        fq[v] = sW[v][ty + 1][tx + 1] + phs[v] * hot;
+      }
+      const bool vert = s == E2D_E || s == E2D_W;
+      const int64_t f = s == E2D_E ? fE : s == E2D_W ? fW : s == E2D_N ? fN : fS;
+      const T fc = vert ? P.geo.vface[E2D_F_COS][f] : P.geo.hface[E2D_F_COS][f];
+      const T fs = vert ? P.geo.vface[E2D_F_SIN][f] : P.geo.hface[E2D_F_SIN][f];
+      const int64_t stride = vert ? P.nvface : P.nhface;
+      // this cell's own face state: left state of its E/N face, right state of W/S
+      {
+        T qv[4] = {fq[0], fq[1], fq[2], fq[3]}, w[4];
+        if (vert) {
+          if (!cart) rotate(qv, fc, fs);
+        } else {
+          if (cart) rotate90(qv);
+          else rotate(qv, fc, fs);
+        }
+        recon_to_prim<RECON>(qv, G, w);
+        T* dst = s == E2D_E ? F.vL : s == E2D_W ? F.vR : s == E2D_N ? F.hL : F.hR;
+        store4(dst + (int64_t)q * 4 * stride, stride, f, w);
+      }
+      // the outside state of a block-boundary face, for this point
+      const bool at = s == E2D_E ? j == nx - 1 : s == E2D_W ? j == 0 : s == E2D_N ? i == ny - 1 : i == 0;
+      if (at) {
+        T gr[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+          gr[v] = s == E2D_E ? sW[v][ty + 1][tx + 2] : s == E2D_W ? sW[v][ty + 1][tx]
+                : s == E2D_N ? sW[v][ty + 2][tx + 1] : sW[v][ty][tx + 1];
+        T o[4], w[4];
+        outside_state(P, B, s, vert ? i : j, t, gr, fq, o);
+        if (vert) {
+          if (!cart) rotate(o, fc, fs);
+        } else {
+          if (cart) rotate90(o);
+          else rotate(o, fc, fs);
+        }
+        recon_to_prim<RECON>(o, G, w);
+        T* dst = s == E2D_E ? F.vR : s == E2D_W ? F.vL : s == E2D_N ? F.hR : F.hL;
+        store4(dst + (int64_t)q * 4 * stride, stride, f, w);
+      }
+    }
+}
+
+// K2 with 2 or 3 quadrature points: one Riemann flux per face and point, un-rotated,
+// integrated as L * sum_q w_q F_q summed from zero in point order
+// (pyhype/fvm/base.py:171-190).
+template <typename T, int FLUX, int NQP>
+__global__ void __launch_bounds__(TX * TY) k_flux_qp(ParamsT<T> P, const int4* __restrict__ tiles,
+                                                     const InstanceState* __restrict__ inst, FaceArraysT<T> F) {
+  const int4 tl = tiles[blockIdx.x];
+  const E2DBlock* B = P.blocks + tl.x;
+  if (!inst[B->instance].active) return;
+  const int nx = B->nx, ny = B->ny;
+  const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
+  const int i = tl.y + ty, j = tl.z + tx;
+  if (i > ny || j > nx) return;
+  const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
+  const bool cart = B->is_cartesian != 0;
+#pragma unroll
+  for (int dir = 0; dir < 2; ++dir) {
+    const bool vert = dir == 0;
+    if (vert ? i >= ny : j >= nx) continue;
+    const int64_t f = vert ? vf_at(B, i, j) : hf_at(B, i, j);
+    const int64_t stride = vert ? P.nvface : P.nhface;
+    const T* Ls = vert ? F.vL : F.hL;
+    const T* Rs = vert ? F.vR : F.hR;
+    const T fc = vert ? P.geo.vface[E2D_F_COS][f] : P.geo.hface[E2D_F_COS][f];
+    const T fs = vert ? P.geo.vface[E2D_F_SIN][f] : P.geo.hface[E2D_F_SIN][f];
+    T acc[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+    for (int q = 0; q < NQP; ++q) {
+      const int64_t o = (int64_t)q * 4 * stride + f;
+      T L[4] = {Ls[o], Ls[o + stride], Ls[o + 2 * stride], Ls[o + 3 * stride]};
+      T R[4] = {Rs[o], Rs[o + stride], Rs[o + 2 * stride], Rs[o + 3 * stride]};
+      T Fq[4];
+      riemann<FLUX>(L, R, G, Fq);
+      if (vert) {
+        if (!cart) unrotate(Fq, fc, fs);
+      } else {
+        if (cart) unrotate90(Fq);
+        else unrotate(Fq, fc, fs);
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[v] = acc[v] + P.qw[q] * Fq[v];
+    }
+    const T len = vert ? P.geo.vface[E2D_F_L][f] : P.geo.hface[E2D_F_L][f];
+    T Iv[4] = {len * acc[0], len * acc[1], len * acc[2], len * acc[3]};
+    store4(vert ? F.vI : F.hI, stride, f, Iv);
+  }
+}
+
+// --------------------------------------------------------------------------------------
 // K2: one Riemann flux per face
 // --------------------------------------------------------------------------------------
 template <typename T, int FLUX, bool DBG>
@@ -592,11 +784,36 @@ static cudaError_t recon_lim(const ParamsT<T>& P, const int4* const* tiles, cons
   return recon_variant<T, LIM, E2D_RECON_CONSERVATIVE>(P, tiles, n, variant, persistent, U, inst, F, dbg, st);
 }
 
+template <typename T, int LIM, int RECON>
+static cudaError_t recon_qp(const ParamsT<T>& P, const TileSet& ts, const T* U, const InstanceState* inst,
+                            FaceArraysT<T> F, cudaStream_t st) {
+  if (P.nqp == 3)
+    k_reconstruct_qp<T, LIM, RECON, 3><<<ts.ncell[1], TX * TY, 0, st>>>(P, ts.cell[1], U, inst, F);
+  else
+    k_reconstruct_qp<T, LIM, RECON, 2><<<ts.ncell[1], TX * TY, 0, st>>>(P, ts.cell[1], U, inst, F);
+  return cudaGetLastError();
+}
+
+template <typename T, int LIM>
+static cudaError_t recon_qp_lim(const ParamsT<T>& P, const TileSet& ts, const T* U, const InstanceState* inst,
+                                FaceArraysT<T> F, cudaStream_t st) {
+  if (P.recon == E2D_RECON_PRIMITIVE) return recon_qp<T, LIM, E2D_RECON_PRIMITIVE>(P, ts, U, inst, F, st);
+  return recon_qp<T, LIM, E2D_RECON_CONSERVATIVE>(P, ts, U, inst, F, st);
+}
+
 template <typename T>
 cudaError_t launch_reconstruct(const ParamsT<T>& P, const TileSet& ts, KernelChoice kc, const T* U,
                                const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st) {
   const int4* tiles[3] = {ts.cell[0], ts.cell[1], ts.cell[2]};
   if (ts.ncell[1] <= 0) return cudaSuccess;
+  if (P.nqp > 1) {  // several face quadrature points: one kernel form, no per-operator outputs
+    switch (P.limiter) {
+      case E2D_LIM_BARTH_JESPERSEN: return recon_qp_lim<T, E2D_LIM_BARTH_JESPERSEN>(P, ts, U, inst, F, st);
+      case E2D_LIM_VAN_ALBADA: return recon_qp_lim<T, E2D_LIM_VAN_ALBADA>(P, ts, U, inst, F, st);
+      case E2D_LIM_VAN_LEER: return recon_qp_lim<T, E2D_LIM_VAN_LEER>(P, ts, U, inst, F, st);
+      default: return recon_qp_lim<T, E2D_LIM_VENKATAKRISHNAN>(P, ts, U, inst, F, st);
+    }
+  }
   switch (P.limiter) {
     case E2D_LIM_BARTH_JESPERSEN:
       return recon_lim<T, E2D_LIM_BARTH_JESPERSEN>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st);
@@ -633,10 +850,25 @@ static cudaError_t flux_t(const ParamsT<T>& P, const int4* tiles, int n, KernelC
   }
 }
 
+template <typename T, int FLUX>
+static cudaError_t flux_qp(const ParamsT<T>& P, const TileSet& ts, const InstanceState* inst, FaceArraysT<T> F,
+                           cudaStream_t st) {
+  if (P.nqp == 3) k_flux_qp<T, FLUX, 3><<<ts.nface, TX * TY, 0, st>>>(P, ts.face, inst, F);
+  else k_flux_qp<T, FLUX, 2><<<ts.nface, TX * TY, 0, st>>>(P, ts.face, inst, F);
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t launch_flux(const ParamsT<T>& P, const TileSet& ts, KernelChoice kc, const InstanceState* inst,
                         FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st) {
   if (ts.nface <= 0) return cudaSuccess;
+  if (P.nqp > 1) {
+    switch (P.flux) {
+      case E2D_FLUX_HLLL: return flux_qp<T, E2D_FLUX_HLLL>(P, ts, inst, F, st);
+      case E2D_FLUX_HLLE: return flux_qp<T, E2D_FLUX_HLLE>(P, ts, inst, F, st);
+      default: return flux_qp<T, E2D_FLUX_ROE>(P, ts, inst, F, st);
+    }
+  }
   switch (P.flux) {
     case E2D_FLUX_HLLL: return flux_t<T, E2D_FLUX_HLLL>(P, ts.face, ts.nface, kc, inst, F, dbg, st);
     case E2D_FLUX_HLLE: return flux_t<T, E2D_FLUX_HLLE>(P, ts.face, ts.nface, kc, inst, F, dbg, st);

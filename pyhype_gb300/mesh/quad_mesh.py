@@ -88,6 +88,36 @@ def _one_point(p1: np.ndarray, p2: np.ndarray) -> np.ndarray:
     return 0.5 * ((p2 - p1) * p + (p2 + p1))
 
 
+# Gauss-Legendre rules on [-1, 1] as (point, weight) in the reference's order
+# (pyhype/mesh/quadratures.py:33-37)
+QUADRATURE = {
+    1: ((0, 2),),
+    2: ((-1 / np.sqrt(3), 1), (1 / np.sqrt(3), 1)),
+    3: ((-np.sqrt(3 / 5), 5 / 9), (0, 8 / 9), (np.sqrt(3 / 5), 5 / 9)),
+}
+
+
+def quadrature_points(g: "BlockGeometry", nqp: int):
+    """Face quadrature points of every cell of a block (pyhype/mesh/quadratures.py:
+    40-90): a list over the rule's points of (weight, {side: (x, y)}), each point
+    0.5*((p2 - p1)*p + (p2 + p1)) between the side's end nodes (E: NE->SE, W: NW->SW,
+    N: NE->NW, S: SE->SW), arrays of shape (ny, nx)."""
+    x, y = g.nodes_x, g.nodes_y
+    ends = {
+        "E": ((x[1:, 1:], y[1:, 1:]), (x[:-1, 1:], y[:-1, 1:])),
+        "W": ((x[1:, :-1], y[1:, :-1]), (x[:-1, :-1], y[:-1, :-1])),
+        "N": ((x[1:, 1:], y[1:, 1:]), (x[1:, :-1], y[1:, :-1])),
+        "S": ((x[:-1, 1:], y[:-1, 1:]), (x[:-1, :-1], y[:-1, :-1])),
+    }
+    out = []
+    for p, w in QUADRATURE[nqp]:
+        pts = {}
+        for side, ((x1, y1), (x2, y2)) in ends.items():
+            pts[side] = (0.5 * ((x2 - x1) * p + (x2 + x1)), 0.5 * ((y2 - y1) * p + (y2 + y1)))
+        out.append((w, pts))
+    return out
+
+
 def _length(x1, x2, y1, y2):
     dx = x1 - x2
     dy = y1 - y2

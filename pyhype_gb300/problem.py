@@ -76,7 +76,12 @@ class E2DConfig(ctypes.Structure):
         ("gamma", ctypes.c_double),
         ("gm1", ctypes.c_double),
         ("cfl", ctypes.c_double),
+        ("nqp", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
+
+
+MAX_QP = 3
 
 
 class E2DGeometry(ctypes.Structure):
@@ -84,6 +89,7 @@ class E2DGeometry(ctypes.Structure):
         ("cell", c_double_p * N_CELL_PLANES),
         ("vface", c_double_p * N_FACE_PLANES),
         ("hface", c_double_p * N_FACE_PLANES),
+        ("qp", (c_double_p * 8) * MAX_QP),
     ]
 
 
@@ -221,8 +227,13 @@ def build_problem(
     instance_of: Optional[Dict[int, int]] = None,
     sizes: Optional[Dict[int, tuple]] = None,
     geometries: Optional[Dict[int, BlockGeometry]] = None,
+    nqp: int = 1,
 ) -> Problem:
     """Assemble the block table and the geometry planes.
+
+    ``nqp`` is the number of face quadrature points (1, 2 or 3,
+    ``SolverConfig.fvm_num_quadrature_points``); with more than one the offsets of
+    every point from the centroid are added as extra cell planes.
 
     ``sizes`` optionally gives per-block ``(nx, ny)`` (independent batched instances);
     otherwise every block uses ``nx, ny`` as the reference does
@@ -329,6 +340,23 @@ def build_problem(
         geometry.vface[p] = _ptr(vface[p])
         geometry.hface[p] = _ptr(hface[p])
     keep += [cell, vface, hface]
+    if nqp not in (1, 2, 3):
+        raise ValueError(f"fvm_num_quadrature_points must be 1, 2 or 3, not {nqp}")
+    if nqp > 1:
+        from .mesh.quad_mesh import quadrature_points
+
+        qoff = np.empty((nqp, 8, cell_off))
+        for k, g in enumerate(geos):
+            B = blocks[k]
+            c0, n = B.cell_offset, B.nx * B.ny
+            for q, (_, pts) in enumerate(quadrature_points(g, nqp)):
+                for si, sd in enumerate(SIDES):
+                    qoff[q, si, c0:c0 + n] = (pts[sd][0] - g.xc).ravel()
+                    qoff[q, 4 + si, c0:c0 + n] = (pts[sd][1] - g.yc).ravel()
+        for q in range(nqp):
+            for k in range(8):
+                geometry.qp[q][k] = _ptr(qoff[q, k])
+        keep.append(qoff)
 
     cfg = E2DConfig()
     cfg.nblocks = nb
@@ -340,6 +368,7 @@ def build_problem(
     cfg.gamma = gamma
     cfg.gm1 = gm1
     cfg.cfl = cfl
+    cfg.nqp = nqp
     return Problem(cfg=cfg, blocks=blocks, geometry=geometry, block_geometry=geos, block_ids=ids,
                    cell_offsets=cell_offsets, ncell=cell_off, nvface=vface_off, nhface=hface_off, _keep=keep)
 
@@ -352,8 +381,8 @@ def problem_from_config(config, mesh_dict: Dict[int, dict], precision: int = 0) 
         raise ValueError(f"No MUSCL finite volume method has been specialized with order {config.fvm_spatial_order}")
     if config.nghost != 1:
         raise ValueError("Number of ghost cells must be equal to 1 for this method.")
-    if config.fvm_num_quadrature_points != 1:
-        raise NotImplementedError("only the one-point face quadrature (fvm_num_quadrature_points=1) is built")
+    if config.fvm_num_quadrature_points not in (1, 2, 3):
+        raise ValueError("fvm_num_quadrature_points must be 1, 2 or 3 (pyhype/mesh/quadratures.py:33-37)")
     if config.fvm_gradient_type != "GreenGauss":
         raise ValueError(f"Gradient type {config.fvm_gradient_type} is not available.")
     if config.interface_interpolation != "arithmetic_average":
@@ -365,5 +394,5 @@ def problem_from_config(config, mesh_dict: Dict[int, dict], precision: int = 0) 
         limiter=config.fvm_slope_limiter_type,
         recon=config.reconstruction_type.__name__,
         gamma=fluid.gamma(), gm1=fluid.gamma() - 1, cfl=config.CFL, fluid=fluid,
-        precision=precision,
+        precision=precision, nqp=int(config.fvm_num_quadrature_points),
     )

@@ -98,7 +98,7 @@ def problem(z, precision: int = 0, reference_geometry: bool = True):
         mesh_dict(z), int(z["nx"]), int(z["ny"]),
         flux=str(z["flux"]), limiter=str(z["limiter"]), recon=str(z["recon"]),
         gamma=air.gamma(), gm1=air.gamma() - 1, cfl=float(z["cfl"]), fluid=air, precision=precision,
-        geometries=geos,
+        geometries=geos, nqp=int(z["nqp"]) if "nqp" in z.files else 1,
     )
 
 

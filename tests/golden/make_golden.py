@@ -354,6 +354,15 @@ CASES["wedge"] = (dict(nx=16, ny=16, fvm_flux_function_type="HLLL", reconstructi
 CASES["jet"] = (dict(nx=24, ny=6, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState,
                     time_integrator="RK2", CFL=0.4), jet_mesh, lambda: FloodIC([1.0, 0.0, 0.0, 1 / AIR.gamma()]),
                 6, "all", 2, None)
+CASES["qp2_roe"] = (dict(nx=20, ny=16, fvm_num_quadrature_points=2), lambda: single_block(0, 10, 0, 8),
+                    lambda: ExplosionIC(**MOVING), 5, "all", None, None)
+CASES["qp3_hlll_prim"] = (dict(nx=16, ny=12, fvm_num_quadrature_points=3, fvm_flux_function_type="HLLL",
+                               reconstruction_type=PrimitiveState, fvm_slope_limiter_type="VanAlbada"),
+                          lambda: rect_mesh(2, 2, 10.0, 8.0, bc="OutletDirichlet"), lambda: ExplosionIC(**MOVING), 5,
+                          "all", None, None)
+CASES["qp2_skew"] = (dict(nx=12, ny=12, fvm_num_quadrature_points=2, fvm_flux_function_type="HLLL",
+                          reconstruction_type=PrimitiveState, time_integrator="RK2", CFL=0.4), dmr_example_mesh,
+                     lambda: DMRExampleIC(), 4, "all", None, None)
 CASES["dmr5"] = (dict(nx=16, ny=20, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState, CFL=0.4,
                      t_final=0.2, fluid=AIR_UNIT), lambda: dmr_mesh(5), lambda: DMRIC(), 8, "all", 3, [[1], [0.5, 0.5]])
 for _ti in ("ExplicitEuler1", "RK2", "Ralston2", "RK3", "RK3SSP", "Ralston3", "Ralston4", "DormandPrince5"):
@@ -410,9 +419,13 @@ def record_geometry(solver, out):
             out[p + f"th{side}"] = f.theta[:, :, 0]
             out[p + f"nx{side}"] = f.norm.x[:, :, 0]
             out[p + f"ny{side}"] = f.norm.y[:, :, 0]
-            q = blk.qp[getattr(Direction, {"E": "east", "W": "west", "N": "north", "S": "south"}[side])][0]
-            out[p + f"qx{side}"] = q.x[:, :, 0]
-            out[p + f"qy{side}"] = q.y[:, :, 0]
+            qps = blk.qp[getattr(Direction, {"E": "east", "W": "west", "N": "north", "S": "south"}[side])]
+            out[p + f"qx{side}"] = qps[0].x[:, :, 0]
+            out[p + f"qy{side}"] = qps[0].y[:, :, 0]
+            if len(qps) > 1:  # every point of a multi-point rule, in the reference's order
+                for k, q in enumerate(qps):
+                    out[p + f"qx{side}_{k}"] = q.x[:, :, 0]
+                    out[p + f"qy{side}_{k}"] = q.y[:, :, 0]
             # the run-time rotation evaluates np.sin/np.cos on numpy float64 scalars
             # (pyhype/utils/utils.py:75-85); record that scalar path for the theta arrays
             th = f.theta[:, :, 0]
@@ -492,6 +505,7 @@ def run_case(name):
     out["nx"] = np.array(cfg.nx)
     out["ny"] = np.array(cfg.ny)
     out["cfl"] = np.array(cfg.CFL)
+    out["nqp"] = np.array(cfg.fvm_num_quadrature_points)
     out["t_final"] = np.array(cfg.t_final)
     out["a_inf"] = np.array(cfg.fluid.far_field.a)
     out["flux"] = np.array(cfg.fvm_flux_function_type)

@@ -28,7 +28,7 @@ def test_library_exports_all_declared_symbols():
     L = _native.load()
     for name in declared():
         assert hasattr(L, name), name
-    assert L.e2d_abi_version() == 1
+    assert L.e2d_abi_version() == 2
     assert set(_native.EXPORTS) <= set(declared())
 
 

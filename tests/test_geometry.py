@@ -4,6 +4,7 @@ import pytest
 
 import _golden as G
 from pyhype_gb300.mesh import RectagularMeshGenerator, build_block_geometry
+from pyhype_gb300.mesh.quad_mesh import quadrature_points
 
 
 @pytest.mark.parametrize("name", G.cases())
@@ -16,12 +17,18 @@ def test_block_geometry_bitwise(name):
         p = f"geo{int(b)}_"
         pairs = [("nodes_x", g.nodes_x), ("nodes_y", g.nodes_y), ("xc", g.xc), ("yc", g.yc),
                  ("A", g.A), ("dx", g.dx), ("dy", g.dy)]
+        nqp = int(z["nqp"]) if "nqp" in z.files else 1
+        qps = quadrature_points(g, nqp)
         for s in "EWNS":
             L, th, nxx, nyy = g.side(s)
             pairs += [("L" + s, L), ("th" + s, th), ("nx" + s, nxx), ("ny" + s, nyy),
-                      ("qx" + s, getattr(g, f"q{s}_x")), ("qy" + s, getattr(g, f"q{s}_y")),
                       # the rotations take cos/sin of theta per element at run time
                       ("cos_scalar" + s, np.cos(th)), ("sin_scalar" + s, np.sin(th))]
+            if nqp == 1:
+                pairs += [("qx" + s, getattr(g, f"q{s}_x")), ("qy" + s, getattr(g, f"q{s}_y"))]
+            else:  # every point of the multi-point rule
+                for k, (_, pts) in enumerate(qps):
+                    pairs += [(f"qx{s}_{k}", pts[s][0]), (f"qy{s}_{k}", pts[s][1])]
         for key, arr in pairs:
             assert np.array_equal(arr, z[p + key]), f"block {b} {key}"
         assert g.is_cartesian == bool(z[p + "is_cartesian"])

@@ -63,7 +63,8 @@ def test_steps_vs_reference(name):
         assert G.fingerprint(blocks) == str(z["fingerprints"][step - 1]), f"fingerprint after step {step}"
 
 
-@pytest.mark.parametrize("name", ["p100", "m2x4_40", "dmr_example", "dmr5", "ti_DormandPrince5", "bc_mixed"])
+@pytest.mark.parametrize("name", ["p100", "m2x4_40", "dmr_example", "dmr5", "ti_DormandPrince5", "bc_mixed",
+                                  "wedge", "qp2_skew", "qp3_hlll_prim"])
 def test_device_loop_vs_reference(name):
     """The device-resident time loop (dt, clamp, stages, t += dt on the GPU, replayed
     from a CUDA graph) reproduces the reference's whole run."""
