@@ -314,7 +314,7 @@ def adjoint_section(stream, nsteps: int = 400, ckpt: int = 20, n: int = 256, fd:
     (r, w, cx) = (4, 2, 5); J = sum_n dt_n * (pressure integral along the north wall).
     Times the recorded forward pass, the reverse pass (segment recompute + reverse
     kernels) and a plain forward run of the same steps; checks dJ/d(r, w, cx) against
-    central differences (h = 1e-6) at the frozen dt schedule."""
+    central differences (h = 1e-6 and 1e-3) at the frozen dt schedule."""
     import numpy as np
     import torch
 
@@ -362,18 +362,27 @@ def adjoint_section(stream, nsteps: int = 400, ckpt: int = 20, n: int = 256, fd:
         J1.backward()
         grad = theta.grad.cpu().numpy()
         dts = A.dts.copy()
-        h = 1e-6
+        gnorm = float(np.linalg.norm(grad))
         res = {}
         for k, name in enumerate(("r", "w", "cx")):
-            tp, tm = theta.detach().clone(), theta.detach().clone()
-            tp[k] += h
-            tm[k] -= h
-            Jp = A.forward(smoothed_explosion(P, tp[0], tp[1], tp[2]), dts)
-            Jm = A.forward(smoothed_explosion(P, tm[0], tm[1], tm[2]), dts)
-            fdv = (Jp - Jm) / (2 * h)
-            res[name] = {"adjoint": float(grad[k]), "central_difference": fdv,
-                         "rel_err": abs(fdv - grad[k]) / abs(grad[k])}
-        out["fd_check_h1e-6"] = res
+            row = {"adjoint": float(grad[k]), "central_difference": {}, "err_over_grad_norm": {}}
+            for h in (1e-6, 1e-3):
+                tp, tm = theta.detach().clone(), theta.detach().clone()
+                tp[k] += h
+                tm[k] -= h
+                Jp = A.forward(smoothed_explosion(P, tp[0], tp[1], tp[2]), dts)
+                Jm = A.forward(smoothed_explosion(P, tm[0], tm[1], tm[2]), dts)
+                fdv = (Jp - Jm) / (2 * h)
+                row["central_difference"][f"h={h:g}"] = fdv
+                row["err_over_grad_norm"][f"h={h:g}"] = abs(fdv - grad[k]) / gnorm
+            res[name] = row
+        out["fd_check"] = res
+        out["fd_check_note"] = (
+            "frozen dt schedule; errors relative to |dJ/d(r,w,cx)|. cx = 5 is the mirror-symmetry point "
+            "(dJ/dcx = 0 exactly; the reverse pass gives the first-of-equals subgradient there). Over 400 steps "
+            "with this limiter J jumps at round-off scale where the reference's slope rule switches "
+            "(psi = 0.75 at davg == 0, about 1 one ulp away), so h = 1e-6 differences measure the jumps; "
+            "h = 1e-3 differences track the derivative")
     A.device.close()
     return out
 

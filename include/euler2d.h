@@ -248,6 +248,15 @@ E2D_API int e2d_instance_times(E2DHandle h, double* t_out, int32_t* steps_out);
    at solver time t (time-dependent sides) into a caller device buffer of 4 cell
    planes; optional intermediates in dbg.                                           */
 E2D_API int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* dbg);
+/* Ghost layer of every block at solver time t, in the reconstruction variables
+   (Blocks.apply_boundary_condition followed by the ghost conversion of
+   ReconstructionBlock.from_block: pyhype/blocks/base.py:448-471,
+   pyhype/blocks/ghost.py:149-216, pyhype/blocks/quad_block.py:120-134).  ghosts_dev
+   is a caller device buffer of 4 planes of nghost = sum over blocks of 2 (nx + ny)
+   doubles; block b's layer starts at the sum of the earlier blocks' lengths and
+   holds E (ny cells, south to north), W (ny), N (nx, west to east), S (nx).  The
+   kernels form these values on the fly; this entry point writes them out.          */
+E2D_API int e2d_ghost_layer(E2DHandle h, double t, double* ghosts_dev);
 
 /* ---- adjoint (reverse mode) -------------------------------------------------------
    No counterpart in the reference (it has no differentiation); the forward steps are

@@ -729,6 +729,34 @@ OR_API int oracle_residual(const E2DConfig* cfg, const E2DBlock* blk, const E2DG
   return 0;
 }
 
+/* Ghost layer of every block in the reconstruction variables, the values
+   ReconstructionBlock.from_block holds after Blocks.apply_boundary_condition
+   (pyhype/blocks/base.py:448-471, pyhype/blocks/ghost.py:149-216,
+   pyhype/blocks/quad_block.py:120-134).  out: 4 planes of nghost = sum of 2 (nx + ny)
+   values; per block E (ny), W (ny), N (nx), S (nx), blocks in table order. */
+OR_API int oracle_ghost_layer(const E2DConfig* cfg, const E2DBlock* blk, const E2DGeometry* geo,
+                              const double* U, double t, double* out) {
+  Ctx C;
+  ctx_init(&C, cfg, blk, geo);
+  int64_t nghost = 0;
+  for (int b = 0; b < cfg->nblocks; ++b) nghost += 2 * (int64_t)(blk[b].nx + blk[b].ny);
+  int64_t o = 0;
+  for (int b = 0; b < cfg->nblocks; ++b) {
+    const int sides[4] = {E2D_E, E2D_W, E2D_N, E2D_S};
+    for (int si = 0; si < 4; ++si) {
+      const int side = sides[si];
+      const int len = (side == E2D_E || side == E2D_W) ? blk[b].ny : blk[b].nx;
+      for (int k = 0; k < len; ++k, ++o) {
+        double g[4], r[4];
+        ghost_cons(&C, b, side, k, U, t, g);
+        to_recon(g, cfg->recon, cfg->gm1, r);
+        for (int v = 0; v < 4; ++v) out[v * nghost + o] = r[v];
+      }
+    }
+  }
+  return 0;
+}
+
 /* ExplicitRungeKutta.integrate (explicit_runge_kutta.py:47-80): stage s evaluates
    k_s at the current stage state, then forms U^n + (dt*a[s][0])*k_0 + ... term by
    term in order, skipping zero coefficients. */

@@ -34,6 +34,7 @@ def lib():
         L.oracle_step.argtypes = [vp, vp, vp, vp, ctypes.c_int, vp, ctypes.c_double, ctypes.c_double]
         L.oracle_dt.argtypes = [vp, vp, vp, vp, vp]
         L.oracle_realizable.argtypes = [vp, vp, vp, vp, vp]
+        L.oracle_ghost_layer.argtypes = [vp, vp, vp, vp, ctypes.c_double, vp]
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         L.oracle_max_threads.restype = ctypes.c_int
         _lib = L
@@ -79,6 +80,14 @@ class Oracle:
             self._dbg = d
         self.L.oracle_residual(*self._args(), U.ctypes.data, float(t), out.ctypes.data, dbg_ptr)
         return (out, dbg_arrays) if debug else out
+
+    def ghost_layer(self, U: np.ndarray, t: float = 0.0) -> np.ndarray:
+        """Ghost layer of every block, (4, nghost) in the reconstruction variables
+        (``Problem.split_ghosts`` takes it apart per block and side)."""
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(4, self.P.ncell)
+        out = np.zeros((4, self.P.nghost))
+        self.L.oracle_ghost_layer(*self._args(), U.ctypes.data, float(t), out.ctypes.data)
+        return out
 
     def step(self, U: np.ndarray, tableau: np.ndarray, dt: float, t: float = 0.0) -> np.ndarray:
         U = np.array(U, dtype=np.float64, copy=True).reshape(4, self.P.ncell)

@@ -30,7 +30,7 @@ EXPORTS = (
     "e2d_abi_version", "e2d_last_error", "e2d_create", "e2d_destroy", "e2d_set_stream", "e2d_num_cells",
     "e2d_set_state", "e2d_get_state", "e2d_set_state_device", "e2d_get_state_device", "e2d_set_tableau",
     "e2d_compute_dt", "e2d_step", "e2d_run", "e2d_check_realizable", "e2d_residual", "e2d_instance_times",
-    "e2d_residual_vjp", "e2d_adjoint_forward", "e2d_adjoint_backward",
+    "e2d_residual_vjp", "e2d_adjoint_forward", "e2d_adjoint_backward", "e2d_ghost_layer",
 )
 
 
@@ -81,6 +81,7 @@ def load(path: Optional[str] = None):
     L.e2d_autotune.argtypes = [vp, ctypes.c_int32, vp]
     L.e2d_residual.argtypes = [vp, ctypes.c_double, vp, vp]
     L.e2d_residual_vjp.argtypes = [vp, ctypes.c_double, vp, vp]
+    L.e2d_ghost_layer.argtypes = [vp, ctypes.c_double, vp]
     L.e2d_adjoint_forward.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, vp, vp,
                                       ctypes.POINTER(ctypes.c_double)]
     L.e2d_adjoint_backward.argtypes = [vp, vp]
@@ -214,6 +215,16 @@ class DeviceSolver:
         if debug:
             return out, {k: v.cpu().numpy() for k, v in dbg_t.items()}
         return out
+
+    def ghost_layer(self, t: float = 0.0) -> np.ndarray:
+        """Ghost layer of every block at solver time t, (4, nghost) host copy in the
+        reconstruction variables (``Problem.split_ghosts`` takes it apart)."""
+        import torch
+
+        out = torch.zeros((4, self.problem.nghost), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        _check(self.L.e2d_ghost_layer(self.h, float(t), ctypes.c_void_p(out.data_ptr())))
+        return out.cpu().numpy()
 
     # ---- adjoint ------------------------------------------------------------------------
     def residual_vjp(self, lam, t: float = 0.0):

@@ -600,6 +600,29 @@ static int launch_dt_path(E2DHandle h) {
   return 0;
 }
 
+template <typename T>
+static int ghost_layer_path(E2DHandle h, double t, double* out) {
+  PathT<T>& p = path<T>(h);
+  std::vector<int64_t> base(h->hblocks.size());
+  int64_t n = 0;
+  int maxlen = 0;
+  for (size_t b = 0; b < h->hblocks.size(); ++b) {
+    const int len = 2 * (h->hblocks[b].nx + h->hblocks[b].ny);
+    base[b] = n;
+    n += len;
+    if (len > maxlen) maxlen = len;
+  }
+  int64_t* dbase = nullptr;
+  CK(cudaMalloc(&dbase, sizeof(int64_t) * base.size()));
+  cudaError_t e = cudaMemcpyAsync(dbase, base.data(), sizeof(int64_t) * base.size(), cudaMemcpyHostToDevice,
+                                  h->stream);
+  if (e == cudaSuccess) e = launch_ghost_layer<T>(p.P, p.S.buf[0], t, dbase, out, n, maxlen, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(dbase);
+  CK(e);
+  return 0;
+}
+
 extern "C" {
 
 int e2d_compute_dt(E2DHandle h, double* dt_host) {
@@ -675,6 +698,11 @@ int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* d) {
   CK(launch_end_step(h->inst, ninst, h->real, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return 0;
+}
+
+int e2d_ghost_layer(E2DHandle h, double t, double* ghosts_dev) {
+  if (!h || !ghosts_dev) return fail(E2D_ERR_INVALID, "null argument");
+  return E2D_DISPATCH(h, ghost_layer_path, t, ghosts_dev);
 }
 
 int e2d_instance_times(E2DHandle h, double* t_out, int32_t* steps_out) {

@@ -907,6 +907,48 @@ cudaError_t launch_realizable(const ParamsT<T>& P, const int4* tiles, int n, con
   return cudaGetLastError();
 }
 
+// Ghost layer of every block in the reconstruction variables: the values that
+// Blocks.apply_boundary_condition leaves in the ghost blocks and that
+// ReconstructionBlock.from_block converts (pyhype/blocks/base.py:448-471,
+// pyhype/blocks/ghost.py:149-216, pyhype/blocks/quad_block.py:120-134).  Per block
+// the layer is E (ny values, south to north), W (ny), N (nx, west to east), S (nx),
+// starting at base[b]; out holds 4 planes of nghost values.  One thread per ghost
+// cell; grid.y strides over blocks.
+template <typename T, int RECON>
+__global__ void k_ghost_layer(ParamsT<T> P, const T* __restrict__ U, double t, const int64_t* __restrict__ base,
+                              double* __restrict__ out, int64_t nghost) {
+  const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
+  for (int b = blockIdx.y; b < P.nblocks; b += gridDim.y) {
+    const E2DBlock* B = P.blocks + b;
+    const int nx = B->nx, ny = B->ny, len = 2 * (nx + ny);
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < len; g += gridDim.x * blockDim.x) {
+      int side, k;
+      if (g < ny) { side = E2D_E; k = g; }
+      else if (g < 2 * ny) { side = E2D_W; k = g - ny; }
+      else if (g < 2 * ny + nx) { side = E2D_N; k = g - 2 * ny; }
+      else { side = E2D_S; k = g - 2 * ny - nx; }
+      T q[4], r[4];
+      ghost_cons(P, B, side, k, U, t, q);
+      to_recon<RECON>(q, G, r);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) out[v * nghost + base[b] + g] = (double)r[v];
+    }
+  }
+}
+
+// maxlen: the longest layer of one block, 2 (nx + ny)
+template <typename T>
+cudaError_t launch_ghost_layer(const ParamsT<T>& P, const T* U, double t, const int64_t* base, double* out,
+                               int64_t nghost, int maxlen, cudaStream_t st) {
+  if (nghost <= 0) return cudaSuccess;
+  const dim3 grid((maxlen + 255) / 256, P.nblocks < 65535 ? P.nblocks : 65535);
+  if (P.recon == E2D_RECON_PRIMITIVE)
+    k_ghost_layer<T, E2D_RECON_PRIMITIVE><<<grid, 256, 0, st>>>(P, U, t, base, out, nghost);
+  else
+    k_ghost_layer<T, E2D_RECON_CONSERVATIVE><<<grid, 256, 0, st>>>(P, U, t, base, out, nghost);
+  return cudaGetLastError();
+}
+
 #define E2D_INSTANTIATE_STAGE_LAUNCHERS(T)                                                                       \
   template cudaError_t launch_reconstruct<T>(const ParamsT<T>&, const TileSet&, KernelChoice, const T*,          \
                                              const InstanceState*, FaceArraysT<T>, const DebugOutT<T>*,          \
@@ -917,7 +959,9 @@ cudaError_t launch_realizable(const ParamsT<T>& P, const int4* tiles, int n, con
                                         StateBuffersT<T>, const StageProgram&, InstanceState*, RealizState*, T*, \
                                         cudaStream_t);                                                           \
   template cudaError_t launch_dt<T>(const ParamsT<T>&, const int4*, int, const T*, InstanceState*, cudaStream_t); \
-  template cudaError_t launch_realizable<T>(const ParamsT<T>&, const int4*, int, const T*, RealizState*, cudaStream_t);
+  template cudaError_t launch_realizable<T>(const ParamsT<T>&, const int4*, int, const T*, RealizState*, cudaStream_t); \
+  template cudaError_t launch_ghost_layer<T>(const ParamsT<T>&, const T*, double, const int64_t*, double*, int64_t, \
+                                             int, cudaStream_t);
 
 // for units that include this header but call the launchers instantiated elsewhere
 #define E2D_EXTERN_STAGE_LAUNCHERS(T)                                                                           \
@@ -932,6 +976,8 @@ cudaError_t launch_realizable(const ParamsT<T>& P, const int4* tiles, int n, con
   extern template cudaError_t launch_dt<T>(const ParamsT<T>&, const int4*, int, const T*, InstanceState*,        \
                                            cudaStream_t);                                                        \
   extern template cudaError_t launch_realizable<T>(const ParamsT<T>&, const int4*, int, const T*, RealizState*,  \
-                                                   cudaStream_t);
+                                                   cudaStream_t);                                                \
+  extern template cudaError_t launch_ghost_layer<T>(const ParamsT<T>&, const T*, double, const int64_t*, double*, \
+                                                    int64_t, int, cudaStream_t);
 
 }  // namespace e2d

@@ -174,6 +174,25 @@ class Problem:
             res.append(np.ascontiguousarray(soa[:, B.cell_offset:B.cell_offset + n].T.reshape(B.ny, B.nx, 4)))
         return res
 
+    @property
+    def nghost(self) -> int:
+        """Cells in the ghost layers of all blocks, 2 (nx + ny) per block."""
+        return sum(2 * (self.blocks[b].nx + self.blocks[b].ny) for b in range(self.nblocks))
+
+    def split_ghosts(self, planes: np.ndarray) -> List[dict]:
+        """Per block {"E": (ny, 4), "W": (ny, 4), "N": (nx, 4), "S": (nx, 4)} from a
+        4-plane ghost-layer array (blocks in table order, sides E, W, N, S)."""
+        planes = np.asarray(planes).reshape(4, self.nghost)
+        res, o = [], 0
+        for b in range(self.nblocks):
+            B = self.blocks[b]
+            d = {}
+            for side, n in (("E", B.ny), ("W", B.ny), ("N", B.nx), ("S", B.nx)):
+                d[side] = np.ascontiguousarray(planes[:, o:o + n].T)
+                o += n
+            res.append(d)
+        return res
+
     def vface_block(self, planes: np.ndarray, b: int) -> np.ndarray:
         """(ny, nx+1, 4) view of a 4-plane vertical-face array for block b."""
         B = self.blocks[b]

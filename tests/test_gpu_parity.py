@@ -42,6 +42,23 @@ def test_residual_intermediates_vs_oracle(name):
         assert _eq(P.from_soa(dudt)[b], z[f"ops{int(z['blk_ids'][b])}_dUdt"])
 
 
+@pytest.mark.parametrize("name", OPS_CASES)
+def test_ghost_layer_vs_reference(name):
+    """e2d_ghost_layer (halo fill, boundary conditions, conversion) equals the
+    reference's reconstruction-block ghosts and the oracle's layer."""
+    from test_oracle_golden import ghost_pairs
+
+    z = G.load(name)
+    P, S = _solver(z)
+    U = P.to_soa(list(z["ops_state"]))
+    S.set_state(U)
+    t = float(z["ops_t"]) if "ops_t" in z.files else 0.0
+    layer = S.ghost_layer(t)
+    assert _eq(layer, Oracle(P).ghost_layer(U, t=t))
+    for key, mine, ref in ghost_pairs(P, z, layer):
+        assert _eq(mine, ref), f"{key}: max diff {np.max(np.abs(mine - ref))}"
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_steps_vs_reference(name):
     """Per-step: dt equal, state fingerprint equal to the reference's."""

@@ -44,6 +44,27 @@ def test_operator_intermediates(name):
             assert np.array_equal(mine, ref), f"block {b} {key}: max diff {np.max(np.abs(mine - ref))}"
 
 
+def ghost_pairs(P, z, layer):
+    """(mine, reference) ghost arrays per block side; the reference records the
+    reconstruction block's ghosts as (ny, 1, 4) / (1, nx, 4)."""
+    for b, sides in enumerate(P.split_ghosts(layer)):
+        p = f"ops{int(z['blk_ids'][b])}_"
+        for side, mine in sides.items():
+            yield f"block {b} ghost{side}", mine, z[p + "ghost" + side].reshape(-1, 4)
+
+
+@pytest.mark.parametrize("name", OPS_CASES)
+def test_ghost_layer(name):
+    """Halo fill + boundary conditions + conversion to the reconstruction variables."""
+    z = G.load(name)
+    P = G.problem(z)
+    t = float(z["ops_t"]) if "ops_t" in z.files else 0.0
+    layer = Oracle(P).ghost_layer(P.to_soa(list(z["ops_state"])), t=t)
+    for key, mine, ref in ghost_pairs(P, z, layer):
+        assert mine.shape == ref.shape, key
+        assert np.array_equal(mine, ref), f"{key}: max diff {np.max(np.abs(mine - ref))}"
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_steps_bitwise(name):
     z = G.load(name)
