@@ -536,7 +536,8 @@ def main():
     import torch
 
     from pyhype_gb300 import _native
-    from pyhype_gb300.roofline import BYTES_PER_CELL_STAGE_FP64, kernel_flops
+    from pyhype_gb300.roofline import (BYTES_PER_CELL_STAGE_FP64, FP64_INST_PER_CELL, FP64_INST_PER_SM_CLOCK,
+                                       kernel_flops)
 
     torch.cuda.set_device(local)
     solver, cfg = make_solver(args.n)
@@ -691,6 +692,17 @@ def main():
             dmr = {"error": str(exc)}
 
     clocks = clk.summary()
+    # FP64 issue view of the dominant kernel: arithmetic FP64 instructions per second
+    # against the pipe's issue limit at the sampled SM clock
+    fp64_issue = None
+    if names[dom] in FP64_INST_PER_CELL and clocks.get("sm_mhz"):
+        nsm = torch.cuda.get_device_properties(0).multi_processor_count
+        ipeak = FP64_INST_PER_SM_CLOCK * nsm * clocks["sm_mhz"] * 1e6
+        iach = FP64_INST_PER_CELL[names[dom]] * P.ncell / (kms[dom] * 1e-3)
+        fp64_issue = {"achieved_ginst_s": iach / 1e9, "peak_ginst_s": ipeak / 1e9, "frac": iach / ipeak,
+                      "inst_per_cell": FP64_INST_PER_CELL[names[dom]],
+                      "source": "DADD+DMUL+DFMA per cell counted by ncu; peak 2 per SM per clock at the "
+                                "sampled SM clock"}
     line = {
         "metric": METRIC,
         "value": value,
@@ -718,6 +730,7 @@ def main():
             "kernel_ms": {n: float(x) for n, x in zip(names, kms)},
             "kernel_share": {n: float(s / share.sum()) for n, s in zip(names, share)},
             "flops_per_launch": flops,
+            "fp64_issue": fp64_issue,
             "hbm": {"achieved_gbs": hbm_achieved, "peak_gbs": hbm_peak,
                     "frac": hbm_achieved / hbm_peak, "bytes_per_cell_stage": BYTES_PER_CELL_STAGE_FP64,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"},

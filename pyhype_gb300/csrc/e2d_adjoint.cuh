@@ -95,7 +95,7 @@ __device__ __forceinline__ void limiter_forward(T w0, T we, T ea, T so, T no, T 
       davg = (w0 + hot[s]) - w0;
     }
     const bool pos = is_pos(davg), neg = is_neg(davg);
-    const T q = (pos ? dmax : dmin) / ((pos || neg) ? davg : T(1));
+    const T q = qdiv(pos ? dmax : dmin, (pos || neg) ? davg : T(1));
     const T sl = (pos || neg) ? q : T(1);
     const T p = psi<LIM>(sl);
     if (s == 0 || vlt(p, ph)) {
@@ -377,8 +377,8 @@ __global__ void __launch_bounds__(TX * VTY, 4) k_reconstruct_vjp(ParamsT<T> P, c
       const T lsl = lph * psi_deriv<LIM>(tr.sl);
       T ld = T(0), lden = T(0);
       if (tr.sign != 0) {
-        ld = lsl / tr.davg;
-        lden = -lsl * tr.sl / tr.davg;
+        ld = qdiv(lsl, tr.davg);
+        lden = qdiv(-lsl * tr.sl, tr.davg);
       }
       // davg = (w0 + hot) - w0 carries hot through with derivative 1
 #pragma unroll
@@ -628,7 +628,7 @@ __global__ void k_side_pressure_grad(ParamsT<T> P, int b, int side, const T* __r
   bool vert;
   side_cell_face<T>(B, side, k, c, f, vert);
   const T len = vert ? P.geo.vface[E2D_F_L][f] : P.geo.hface[E2D_F_L][f];
-  const T rho = U[c], u = U[P.ncell + c] / rho, v = U[2 * P.ncell + c] / rho;
+  const T rho = U[c], u = qdiv(U[P.ncell + c], rho), v = qdiv(U[2 * P.ncell + c], rho);
   const T g = T(coef) * len * P.gas[1];
   lam[c] += g * T(0.5) * (u * u + v * v);
   lam[P.ncell + c] -= g * u;

@@ -18,16 +18,16 @@ __device__ __forceinline__ T sgn(T x) { return x > T(0) ? T(1) : (x < T(0) ? T(-
 template <typename T>
 __device__ __forceinline__ void cons_to_prim_vjp(const T* U, const Gas<T>& G, const T* lW, T* lU) {
   const T rho = U[0];
-  const T u = U[1] / rho, v = U[2] / rho;
+  const T u = qdiv(U[1], rho), v = qdiv(U[2], rho);
   // p = gm1 * (E - rho * 0.5 * (u*u + v*v))
   const T lp = lW[3];
   T lu = lW[1] - lp * G.gm1 * rho * u;
   T lv = lW[2] - lp * G.gm1 * rho * v;
   T lrho = lW[0] - lp * G.gm1 * T(0.5) * (u * u + v * v);
   // u = rhou / rho, v = rhov / rho
-  lU[1] += lu / rho;
-  lU[2] += lv / rho;
-  lU[0] += lrho - (lu * u + lv * v) / rho;
+  lU[1] += qdiv(lu, rho);
+  lU[2] += qdiv(lv, rho);
+  lU[0] += lrho - qdiv(lu * u + lv * v, rho);
   lU[3] += lp * G.gm1;
 }
 
@@ -49,7 +49,7 @@ __device__ __forceinline__ T psi_deriv(T s) {
   if (LIM == E2D_LIM_BARTH_JESPERSEN) return (s < T(1)) ? T(1) : T(0);  // min(1, s)
   if (LIM == E2D_LIM_VAN_LEER) {  // (|s| + s)/(s + 1), with d|s|/ds = 0 at s = 0
     const T d = s + T(1);
-    return ((sgn(s) + T(1)) - (fabs(s) + s) / d) / d;
+    return ((sgn(s) + T(1)) - qdiv(fabs(s) + s, d)) / d;
   }
   if (vlt(sizeof(T) == 4 ? T(SLOPE_CAP_FP32) : T(SLOPE_CAP_FP64), s)) return T(0);  // capped: constant
   if (LIM == E2D_LIM_VAN_ALBADA) {  // (s^2 + s)/(s^2 + 1)
@@ -76,8 +76,8 @@ __device__ void roe_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* l
   const bool tp_pos = is_pos(tp0), tm_pos = is_pos(tm0);
   const T tp = tp_pos ? tp0 : T(1e-8), tm = tm_pos ? tm0 : T(1e-8);
   const bool cm = vlt(T(fabs(Lm0)), tp), cp = vlt(T(fabs(Lp0)), tm);
-  const T Lm = cm ? T(0.5) * ((Lm0 * Lm0) / tp + tp) : Lm0;
-  const T Lp = cp ? T(0.5) * ((Lp0 * Lp0) / tm + tm) : Lp0;
+  const T Lm = cm ? T(0.5) * (qdiv(Lm0 * Lm0, tp) + tp) : Lm0;
+  const T Lp = cp ? T(0.5) * (qdiv(Lp0 * Lp0, tm) + tm) : Lp0;
   const T Ek = T(0.5) * (Q1 * Q1 + Q2 * Q2);
   const T H = G.gm * Q3 / Q0 + Ek;
   const T ua = Q1 * aQ;
@@ -126,12 +126,12 @@ __device__ void roe_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* l
   // Harten
   T lLm0 = lLm, lLp0 = lLp, ltp = T(0), ltm = T(0);
   if (cm) {
-    lLm0 = lLm * (Lm0 / tp);
-    ltp = lLm * T(0.5) * (T(1) - (Lm0 * Lm0) / (tp * tp));
+    lLm0 = lLm * qdiv(Lm0, tp);
+    ltp = lLm * T(0.5) * (T(1) - qdiv(Lm0 * Lm0, tp * tp));
   }
   if (cp) {
-    lLp0 = lLp * (Lp0 / tm);
-    ltm = lLp * T(0.5) * (T(1) - (Lp0 * Lp0) / (tm * tm));
+    lLp0 = lLp * qdiv(Lp0, tm);
+    ltm = lLp * T(0.5) * (T(1) - qdiv(Lp0 * Lp0, tm * tm));
   }
   if (!tp_pos) ltp = T(0);
   if (!tm_pos) ltm = T(0);
@@ -142,12 +142,12 @@ __device__ void roe_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* l
   T lR1 = lslowR + lfastR, lL1 = lslowL + lfastL;
   const T laR = lfastR - lslowR, laL = lfastL - lslowL;
   // sound speeds a = sqrt(g p / rho)
-  T lR0 = -laR * G.g * R[3] / (T(2) * aR * R[0] * R[0]);
-  T lR3 = laR * G.g / (T(2) * aR * R[0]);
-  T lL0 = -laL * G.g * L[3] / (T(2) * aL * L[0] * L[0]);
-  T lL3 = laL * G.g / (T(2) * aL * L[0]);
-  lQ3 += laQ * G.g / (T(2) * aQ * Q0);
-  lQ0 += -laQ * G.g * Q3 / (T(2) * aQ * Q0 * Q0);
+  T lR0 = qdiv(-laR * G.g * R[3], T(2) * aR * R[0] * R[0]);
+  T lR3 = qdiv(laR * G.g, T(2) * aR * R[0]);
+  T lL0 = qdiv(-laL * G.g * L[3], T(2) * aL * L[0] * L[0]);
+  T lL3 = qdiv(laL * G.g, T(2) * aL * L[0]);
+  lQ3 += qdiv(laQ * G.g, T(2) * aQ * Q0);
+  lQ0 += qdiv(-laQ * G.g * Q3, T(2) * aQ * Q0 * Q0);
   // Roe averages
   const T linv = lQ1 * n1 + lQ2 * n2 + lQ3 * n3;
   lL1 += lQ1 * inv * sqL;
@@ -157,8 +157,8 @@ __device__ void roe_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* l
   lR3 += lQ3 * inv * sqR;
   T lsqL = (lQ1 * L[1] + lQ2 * L[2] + lQ3 * L[3]) * inv - inv * inv * linv;
   T lsqR = (lQ1 * R[1] + lQ2 * R[2] + lQ3 * R[3]) * inv - inv * inv * linv;
-  lL0 += lQ0 * R[0] / (T(2) * Q0) + lsqL / (T(2) * sqL);
-  lR0 += lQ0 * L[0] / (T(2) * Q0) + lsqR / (T(2) * sqR);
+  lL0 += qdiv(lQ0 * R[0], T(2) * Q0) + qdiv(lsqL, T(2) * sqL);
+  lR0 += qdiv(lQ0 * L[0], T(2) * Q0) + qdiv(lsqR, T(2) * sqR);
   // dW = R - L
   lR0 += ld0; lR1 += ld1; lR2 += ld2; lR3 += ld3;
   lL0 -= ld0; lL1 -= ld1; lL2 -= ld2; lL3 -= ld3;

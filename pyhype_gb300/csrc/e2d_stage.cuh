@@ -234,7 +234,7 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
       // slope dmax/davg (davg > 0), dmin/davg (davg < 0), 1 (davg == 0), with a single
       // division so lanes of different signs share one division sequence
       const bool pos = is_pos(davg), neg = is_neg(davg);
-      const T q = (pos ? dmax : dmin) / ((pos || neg) ? davg : T(1));
+      const T q = qdiv(pos ? dmax : dmin, (pos || neg) ? davg : T(1));
       const T sl = (pos || neg) ? q : T(1);
       const T p = psi<LIM>(sl);
       ph = (s == 0) ? p : vmin(ph, p);
@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_qp(ParamsT<T> P, const 
           davg = (w0 + hot) - w0;
         }
         const bool pos = is_pos(davg), neg = is_neg(davg);
-        const T qs = (pos ? dmax : dmin) / ((pos || neg) ? davg : T(1));
+        const T qs = qdiv(pos ? dmax : dmin, (pos || neg) ? davg : T(1));
         const T sl = (pos || neg) ? qs : T(1);
         const T p = psi<LIM>(sl);
         ph = (s == 0 && q == 0) ? p : vmin(ph, p);
@@ -608,7 +608,7 @@ __device__ __forceinline__ void update_tile(const ParamsT<T>& P, const int4 tl, 
     for (int v = 0; v < 4; ++v) {
       const T IW = F.vI[v * P.nvface + fW], IE = F.vI[v * P.nvface + fE];
       const T IS = F.hI[v * P.nhface + fS], IN = F.hI[v * P.nhface + fN];
-      k[v] = T(0.5) * (IW - IE + IS - IN) / A;
+      k[v] = qdiv(T(0.5) * (IW - IE + IS - IN), A);
     }
     if (dudt_out) {
 #pragma unroll

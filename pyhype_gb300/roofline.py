@@ -36,6 +36,16 @@ DIV_PER_CELL_RECONSTRUCT = 40
 DIV_PER_FACE_ROE = 6
 SQRT_PER_FACE_ROE = 6
 
+# FP64 arithmetic instructions (DADD + DMUL + DFMA, per thread) per cell of each FP64
+# stage kernel on the same dominant path, counted by ncu
+# (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum over one launch of
+# 2 097 152 cells).  With multiply-add contraction off, the DFMAs are those of the
+# division and square-root sequences.  The flux kernel's count is per cell (2 faces).
+FP64_INST_PER_CELL = {"reconstruct": 728, "flux": 444, "update": 66}
+# The FP64 pipe issues at most 2 thread-instructions per SM per clock on GB300 (the
+# peak that ncu's FP64 pipe utilisation is relative to).
+FP64_INST_PER_SM_CLOCK = 2
+
 # Algorithmic HBM bytes per cell-stage of the whole stage (state reads/writes and
 # geometry of the cell and its two owned faces), FP64, RK4 low-storage average:
 # U_s 32 + U^n 32 + accumulator read+write 64 + U_{s+1} 32 + geometry 64 (A, 1/A and
