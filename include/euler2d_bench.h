@@ -39,6 +39,11 @@ E2D_API int e2d_set_kernel_choice(E2DHandle h, int32_t kernel, int32_t variant, 
    variant, persistent}.  Graphs captured before are dropped.                    */
 E2D_API int e2d_autotune(E2DHandle h, int32_t reps, int32_t* chosen);
 
+/* The FP32 form's division routine applied elementwise: q[i] = a[i] / b[i] for n
+   values in caller device buffers, on the default stream (synchronised).  For
+   testing the routine against IEEE division.                                   */
+E2D_API int e2d_check_div32(const float* a_dev, const float* b_dev, float* q_dev, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,15 +49,15 @@ __device__ __forceinline__ T psi_deriv(T s) {
   if (LIM == E2D_LIM_BARTH_JESPERSEN) return (s < T(1)) ? T(1) : T(0);  // min(1, s)
   if (LIM == E2D_LIM_VAN_LEER) {  // (|s| + s)/(s + 1), with d|s|/ds = 0 at s = 0
     const T d = s + T(1);
-    return ((sgn(s) + T(1)) - qdiv(fabs(s) + s, d)) / d;
+    return pdiv((sgn(s) + T(1)) - qdiv(fabs(s) + s, d), d);
   }
   if (vlt(sizeof(T) == 4 ? T(SLOPE_CAP_FP32) : T(SLOPE_CAP_FP64), s)) return T(0);  // capped: constant
   if (LIM == E2D_LIM_VAN_ALBADA) {  // (s^2 + s)/(s^2 + 1)
     const T d = s * s + T(1);
-    return ((T(1) + T(2) * s - s * s) / d) / d;
+    return pdiv(pdiv(T(1) + T(2) * s - s * s, d), d);
   }
   const T d = s * s + s + T(2);  // Venkatakrishnan (s^2 + 2s)/(s^2 + s + 2)
-  return ((T(4) + T(4) * s - s * s) / d) / d;
+  return pdiv(pdiv(T(4) + T(4) * s - s * s, d), d);
 }
 
 // F = roe_flux(WL, WR): lamWL += (dF/dWL)^T lamF, lamWR += (dF/dWR)^T lamF
@@ -65,11 +65,11 @@ template <typename T>
 __device__ void roe_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* lF, T* lL, T* lR) {
   // ---- forward (same expressions as roe_flux) ----
   const T sqL = sqrt(L[0]), sqR = sqrt(R[0]);
-  const T inv = T(1) / (sqL + sqR);
+  const T inv = pdiv(T(1), sqL + sqR);
   const T Q0 = sqrt(L[0] * R[0]);
   const T n1 = L[1] * sqL + R[1] * sqR, n2 = L[2] * sqL + R[2] * sqR, n3 = L[3] * sqL + R[3] * sqR;
   const T Q1 = n1 * inv, Q2 = n2 * inv, Q3 = n3 * inv;
-  const T aR = sqrt(G.g * R[3] / R[0]), aL = sqrt(G.g * L[3] / L[0]), aQ = sqrt(G.g * Q3 / Q0);
+  const T aR = sqrt(pdiv(G.g * R[3], R[0])), aL = sqrt(pdiv(G.g * L[3], L[0])), aQ = sqrt(pdiv(G.g * Q3, Q0));
   const T Lm0 = Q1 - aQ, Lp0 = Q1 + aQ;
   const T slowR = R[1] - aR, fastR = R[1] + aR, slowL = L[1] - aL, fastL = L[1] + aL;
   const T tp0 = T(2) * (slowR - slowL), tm0 = T(2) * (fastR - fastL);
@@ -79,9 +79,9 @@ __device__ void roe_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* l
   const T Lm = cm ? T(0.5) * (qdiv(Lm0 * Lm0, tp) + tp) : Lm0;
   const T Lp = cp ? T(0.5) * (qdiv(Lp0 * Lp0, tm) + tm) : Lp0;
   const T Ek = T(0.5) * (Q1 * Q1 + Q2 * Q2);
-  const T H = G.gm * Q3 / Q0 + Ek;
+  const T H = pdiv(G.gm * Q3, Q0) + Ek;
   const T ua = Q1 * aQ;
-  const T ia = T(1) / aQ;
+  const T ia = pdiv(T(1), aQ);
   const T one_a2 = ia * ia;
   const T h = T(0.5) * one_a2;
   const T r2a = T(0.5) * Q0 * ia;
@@ -118,8 +118,8 @@ __device__ void roe_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* l
   // ua = Q1*aQ ; H = gm*Q3/Q0 + Ek ; Ek = 0.5*(Q1^2 + Q2^2)
   lQ1 += aQ * lua;
   laQ += Q1 * lua;
-  T lQ3 = G.gm / Q0 * lH;
-  lQ0 += -G.gm * Q3 / (Q0 * Q0) * lH;
+  T lQ3 = pdiv(G.gm, Q0) * lH;
+  lQ0 += pdiv(-G.gm * Q3, Q0 * Q0) * lH;
   lEk += lH;
   lQ1 += Q1 * lEk;
   lQ2 += Q2 * lEk;

@@ -4,6 +4,7 @@
 #include <cstdio>
 
 #include "../../include/euler2d_bench.h"
+#include "e2d_device.cuh"
 
 namespace {
 
@@ -28,7 +29,21 @@ __global__ void k_fp64_chain(double* out, int iters, double seed) {
   if (s == 12345.678) out[blockIdx.x] = s;  // keeps the chains live, never true in practice
 }
 
+__global__ void k_div32(const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ q,
+                        int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    q[i] = e2d::div32(a[i], b[i]);
+}
+
 }  // namespace
+
+extern "C" int e2d_check_div32(const float* a, const float* b, float* q, int64_t n) {
+  if (!a || !b || !q || n < 0) return E2D_ERR_INVALID;
+  if (n == 0) return 0;
+  k_div32<<<1024, 256>>>(a, b, q, n);
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return E2D_ERR_CUDA;
+  return 0;
+}
 
 extern "C" int e2d_bench_fp64_peak(int32_t op, double* tflops) {
   if (!tflops || op < 0 || op > 2) return E2D_ERR_INVALID;

@@ -689,9 +689,9 @@ __global__ void __launch_bounds__(TX * TY) k_dt(ParamsT<T> P, const int4* __rest
     load_cell(U, P.ncell, c, q);
     const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
     cons_to_prim(q, G, w);
-    const T a = sqrt(P.gas[0] * w[3] / w[0]);
-    const T tx_ = P.geo.cell[E2D_G_CFL_DX][c] / (fabs(w[1]) + a);
-    const T ty_ = P.geo.cell[E2D_G_CFL_DY][c] / (fabs(w[2]) + a);
+    const T a = sqrt(pdiv(P.gas[0] * w[3], w[0]));
+    const T tx_ = pdiv(P.geo.cell[E2D_G_CFL_DX][c], fabs(w[1]) + a);
+    const T ty_ = pdiv(P.geo.cell[E2D_G_CFL_DY][c], fabs(w[2]) + a);
     m = double(vmin(tx_, ty_));  // the reduction itself is FP64 on every path
   }
   unsigned long long bits = (unsigned long long)__double_as_longlong(m);

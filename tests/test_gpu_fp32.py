@@ -59,3 +59,44 @@ def test_fp32_residual_close_to_fp64():
     d32 = S32.residual()
     scale = np.max(np.abs(d64), axis=1, keepdims=True)
     assert np.max(np.abs(d32 - d64) / scale) < 1e-3
+
+
+def _floats(rng, n, emin, emax):
+    """Random float32 values with random sign, exponent uniform in [emin, emax] and
+    random mantissa bits."""
+    e = rng.integers(emin, emax + 1, n, dtype=np.int64)
+    m = rng.integers(0, 1 << 23, n, dtype=np.int64)
+    s = rng.integers(0, 2, n, dtype=np.int64) << 31
+    return ((s | ((e + 127) << 23) | m).astype(np.uint32)).view(np.float32)
+
+
+def test_div32_matches_ieee_division():
+    """The FP32 form's division (reciprocal seed, one Newton step, residual correction;
+    IEEE division outside |a|, |b| in 2^-60..2^61) against numpy's IEEE float32
+    division: the same value for every sampled pair, zero quotients up to sign."""
+    import ctypes
+
+    import torch
+
+    from pyhype_gb300 import _native
+
+    L = _native.load()
+    L.e2d_check_div32.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
+    rng = np.random.default_rng(7)
+    n = 1 << 21
+    cases = {
+        "fast path": (_floats(rng, n, -60, 60), _floats(rng, n, -60, 60)),
+        "fast path, small divisors": (_floats(rng, n, -60, 60), _floats(rng, n, -60, -40)),
+        "fallback operands": (_floats(rng, n, -126, 127), _floats(rng, n, -126, 127)),
+        "zero numerators": (np.where(rng.random(n) < 0.3, np.float32(0), _floats(rng, n, -30, 30)).astype(np.float32),
+                            _floats(rng, n, -30, 30)),
+    }
+    for name, (a, b) in cases.items():
+        ad, bd = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+        qd = torch.empty_like(ad)
+        assert L.e2d_check_div32(ad.data_ptr(), bd.data_ptr(), qd.data_ptr(), n) == 0
+        q = qd.cpu().numpy()
+        with np.errstate(all="ignore"):
+            ref = a / b
+        same = (q.view(np.uint32) == ref.view(np.uint32)) | ((q == 0) & (ref == 0)) | (np.isnan(q) & np.isnan(ref))
+        assert same.all(), f"{name}: {int((~same).sum())} of {n} differ, e.g. {a[~same][:3]} / {b[~same][:3]}"
