@@ -231,20 +231,27 @@ __global__ void __launch_bounds__(TX * VTY, 4) k_reconstruct_vjp(ParamsT<T> P, c
   const double t = I->t;
   const int nx = B->nx, ny = B->ny;
   const int i0 = tl.y, j0 = tl.z;
-  // stencil tile in reconstruction variables, ghosts formed as in the forward kernel
+  // stencil tile in reconstruction variables, ghosts formed as in the forward kernel;
+  // a tile whose halo lies inside the block takes a uniform path without them
+  const bool edge = i0 == 0 || j0 == 0 || i0 + VTY >= ny || j0 + TX >= nx;
   for (int p = threadIdx.x; p < (VTY + 2) * (TX + 2); p += TX * VTY) {
     const int ly = p / (TX + 2), lx = p - ly * (TX + 2);
     const int gi = i0 + ly - 1, gj = j0 + lx - 1;
-    const bool in_i = gi >= 0 && gi < ny, in_j = gj >= 0 && gj < nx;
     T q[4], r[4] = {T(0), T(0), T(0), T(0)};
-    bool ok = true;
-    if (in_i && in_j) load_cell(U, P.ncell, cell_at(B, gi, gj), q);
-    else if (in_i && gj == -1) ghost_cons(P, B, E2D_W, gi, U, t, q);
-    else if (in_i && gj == nx) ghost_cons(P, B, E2D_E, gi, U, t, q);
-    else if (in_j && gi == -1) ghost_cons(P, B, E2D_S, gj, U, t, q);
-    else if (in_j && gi == ny) ghost_cons(P, B, E2D_N, gj, U, t, q);
-    else ok = false;
-    if (ok) to_recon<RECON>(q, G, r);
+    if (!edge) {
+      load_cell(U, P.ncell, cell_at(B, gi, gj), q);
+      to_recon<RECON>(q, G, r);
+    } else {
+      const bool in_i = gi >= 0 && gi < ny, in_j = gj >= 0 && gj < nx;
+      bool ok = true;
+      if (in_i && in_j) load_cell(U, P.ncell, cell_at(B, gi, gj), q);
+      else if (in_i && gj == -1) ghost_cons(P, B, E2D_W, gi, U, t, q);
+      else if (in_i && gj == nx) ghost_cons(P, B, E2D_E, gi, U, t, q);
+      else if (in_j && gi == -1) ghost_cons(P, B, E2D_S, gj, U, t, q);
+      else if (in_j && gi == ny) ghost_cons(P, B, E2D_N, gj, U, t, q);
+      else ok = false;
+      if (ok) to_recon<RECON>(q, G, r);
+    }
     sW[0][ly][lx] = r[0];
     sW[1][ly][lx] = r[1];
     sW[2][ly][lx] = r[2];
@@ -323,7 +330,7 @@ __global__ void __launch_bounds__(TX * VTY, 4) k_reconstruct_vjp(ParamsT<T> P, c
     else load_face(F.hR, P.nhface, fS, lw);
     face_state_vjp<RECON>(q, rot, fc, fs, G, lw, lq);
     const bool at = side == E2D_E ? j == nx - 1 : side == E2D_W ? j == 0 : side == E2D_N ? i == ny - 1 : i == 0;
-    if (at) {
+    if (edge && at) {
       const int k = vert ? i : j;
       const double *gd, *fd;
       const int kind = side_kind_at(B, side, k, t, gd, fd);
@@ -411,7 +418,7 @@ __global__ void __launch_bounds__(TX * VTY, 4) k_reconstruct_vjp(ParamsT<T> P, c
 
   // Phase D: outside states that are the ghost's own value (inter-block and copy
   // sides) pass their adjoint to the ghost's slot
-  {
+  if (edge) {
     const int side_of[4] = {E2D_W, E2D_E, E2D_S, E2D_N};
     const int slot_of[4] = {ST_W, ST_E, ST_S, ST_N};
     const bool at[4] = {j == 0, j == nx - 1, i == 0, i == ny - 1};

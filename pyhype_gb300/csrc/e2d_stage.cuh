@@ -160,19 +160,28 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
   const double t = I->t;
   const int nx = B->nx, ny = B->ny;
   const int i0 = tl.y, j0 = tl.z;
+  // A tile whose halo lies inside the block needs no ghost cell and owns no block-
+  // boundary face.  The test is uniform over the CTA, so interior tiles branch past
+  // the ghost and boundary code instead of issuing it under predicates.
+  const bool edge = i0 == 0 || j0 == 0 || i0 + RTY >= ny || j0 + TX >= nx;
   for (int p = threadIdx.x; p < (RTY + 2) * (TX + 2); p += TX * RTY) {
     const int ly = p / (TX + 2), lx = p - ly * (TX + 2);
     const int gi = i0 + ly - 1, gj = j0 + lx - 1;
-    const bool in_i = gi >= 0 && gi < ny, in_j = gj >= 0 && gj < nx;
     T q[4], r[4] = {T(0), T(0), T(0), T(0)};
-    bool ok = true;
-    if (in_i && in_j) load_cell(U, P.ncell, cell_at(B, gi, gj), q);
-    else if (in_i && gj == -1) ghost_cons(P, B, E2D_W, gi, U, t, q);
-    else if (in_i && gj == nx) ghost_cons(P, B, E2D_E, gi, U, t, q);
-    else if (in_j && gi == -1) ghost_cons(P, B, E2D_S, gj, U, t, q);
-    else if (in_j && gi == ny) ghost_cons(P, B, E2D_N, gj, U, t, q);
-    else ok = false;
-    if (ok) to_recon<RECON>(q, G, r);
+    if (!edge) {
+      load_cell(U, P.ncell, cell_at(B, gi, gj), q);
+      to_recon<RECON>(q, G, r);
+    } else {
+      const bool in_i = gi >= 0 && gi < ny, in_j = gj >= 0 && gj < nx;
+      bool ok = true;
+      if (in_i && in_j) load_cell(U, P.ncell, cell_at(B, gi, gj), q);
+      else if (in_i && gj == -1) ghost_cons(P, B, E2D_W, gi, U, t, q);
+      else if (in_i && gj == nx) ghost_cons(P, B, E2D_E, gi, U, t, q);
+      else if (in_j && gi == -1) ghost_cons(P, B, E2D_S, gj, U, t, q);
+      else if (in_j && gi == ny) ghost_cons(P, B, E2D_N, gj, U, t, q);
+      else ok = false;
+      if (ok) to_recon<RECON>(q, G, r);
+    }
     sW[0][ly][lx] = r[0];
     sW[1][ly][lx] = r[1];
     sW[2][ly][lx] = r[2];
@@ -281,6 +290,7 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
     store4(F.hR, P.nhface, fS, w);
   }
   // outside states of block-boundary faces
+  if (!edge) return;
   if (j == 0) {
     const T gr[4] = {sW[0][ty + 1][tx], sW[1][ty + 1][tx], sW[2][ty + 1][tx], sW[3][ty + 1][tx]};
     T o[4], w[4];
@@ -358,19 +368,25 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_qp(ParamsT<T> P, const 
   const double t = I->t;
   const int nx = B->nx, ny = B->ny;
   const int i0 = tl.y, j0 = tl.z;
+  const bool edge = i0 == 0 || j0 == 0 || i0 + TY >= ny || j0 + TX >= nx;  // as in reconstruct_tile
   for (int p = threadIdx.x; p < (TY + 2) * (TX + 2); p += TX * TY) {
     const int ly = p / (TX + 2), lx = p - ly * (TX + 2);
     const int gi = i0 + ly - 1, gj = j0 + lx - 1;
-    const bool in_i = gi >= 0 && gi < ny, in_j = gj >= 0 && gj < nx;
     T q[4], r[4] = {T(0), T(0), T(0), T(0)};
-    bool ok = true;
-    if (in_i && in_j) load_cell(U, P.ncell, cell_at(B, gi, gj), q);
-    else if (in_i && gj == -1) ghost_cons(P, B, E2D_W, gi, U, t, q);
-    else if (in_i && gj == nx) ghost_cons(P, B, E2D_E, gi, U, t, q);
-    else if (in_j && gi == -1) ghost_cons(P, B, E2D_S, gj, U, t, q);
-    else if (in_j && gi == ny) ghost_cons(P, B, E2D_N, gj, U, t, q);
-    else ok = false;
-    if (ok) to_recon<RECON>(q, G, r);
+    if (!edge) {
+      load_cell(U, P.ncell, cell_at(B, gi, gj), q);
+      to_recon<RECON>(q, G, r);
+    } else {
+      const bool in_i = gi >= 0 && gi < ny, in_j = gj >= 0 && gj < nx;
+      bool ok = true;
+      if (in_i && in_j) load_cell(U, P.ncell, cell_at(B, gi, gj), q);
+      else if (in_i && gj == -1) ghost_cons(P, B, E2D_W, gi, U, t, q);
+      else if (in_i && gj == nx) ghost_cons(P, B, E2D_E, gi, U, t, q);
+      else if (in_j && gi == -1) ghost_cons(P, B, E2D_S, gj, U, t, q);
+      else if (in_j && gi == ny) ghost_cons(P, B, E2D_N, gj, U, t, q);
+      else ok = false;
+      if (ok) to_recon<RECON>(q, G, r);
+    }
     sW[0][ly][lx] = r[0];
     sW[1][ly][lx] = r[1];
     sW[2][ly][lx] = r[2];
@@ -459,7 +475,7 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_qp(ParamsT<T> P, const 
       }
       // the outside state of a block-boundary face, for this point
       const bool at = s == E2D_E ? j == nx - 1 : s == E2D_W ? j == 0 : s == E2D_N ? i == ny - 1 : i == 0;
-      if (at) {
+      if (edge && at) {
         T gr[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v)
