@@ -95,9 +95,8 @@ __device__ __forceinline__ void limiter_forward(T w0, T we, T ea, T so, T no, T 
       davg = (w0 + hot[s]) - w0;
     }
     const bool pos = is_pos(davg), neg = is_neg(davg);
-    const T q = qdiv(pos ? dmax : dmin, (pos || neg) ? davg : T(1));
-    const T sl = (pos || neg) ? q : T(1);
-    const T p = psi<LIM>(sl);
+    const T sl = (pos || neg) ? qdiv(pos ? dmax : dmin, davg) : T(1);
+    const T p = psi_s<LIM>(sl);
     if (s == 0 || vlt(p, ph)) {
       ph = p;
       sel = s;

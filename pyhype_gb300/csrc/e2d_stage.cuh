@@ -241,11 +241,11 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
         davg = (w0 + hot[s]) - w0;
       }
       // slope dmax/davg (davg > 0), dmin/davg (davg < 0), 1 (davg == 0), with a single
-      // division so lanes of different signs share one division sequence
+      // division so lanes of different signs share one division sequence; a zero davg
+      // divides nothing
       const bool pos = is_pos(davg), neg = is_neg(davg);
-      const T q = qdiv(pos ? dmax : dmin, (pos || neg) ? davg : T(1));
-      const T sl = (pos || neg) ? q : T(1);
-      const T p = psi<LIM>(sl);
+      const T sl = (pos || neg) ? qdiv(pos ? dmax : dmin, davg) : T(1);
+      const T p = psi_s<LIM>(sl);
       ph = (s == 0) ? p : vmin(ph, p);
     }
     ph = is_neg(ph) ? T(0) : ph;
@@ -434,9 +434,8 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_qp(ParamsT<T> P, const 
           davg = (w0 + hot) - w0;
         }
         const bool pos = is_pos(davg), neg = is_neg(davg);
-        const T qs = qdiv(pos ? dmax : dmin, (pos || neg) ? davg : T(1));
-        const T sl = (pos || neg) ? qs : T(1);
-        const T p = psi<LIM>(sl);
+        const T sl = (pos || neg) ? qdiv(pos ? dmax : dmin, davg) : T(1);
+        const T p = psi_s<LIM>(sl);
         ph = (s == 0 && q == 0) ? p : vmin(ph, p);
       }
     phs[v] = is_neg(ph) ? T(0) : ph;
