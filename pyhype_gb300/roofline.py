@@ -41,7 +41,7 @@ SQRT_PER_FACE_ROE = 6
 # (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum over one launch of
 # 2 097 152 cells).  With multiply-add contraction off, the DFMAs are those of the
 # division and square-root sequences.  The flux kernel's count is per cell (2 faces).
-FP64_INST_PER_CELL = {"reconstruct": 738, "flux": 444, "update": 67}
+FP64_INST_PER_CELL = {"reconstruct": 712, "flux": 444, "update": 67}
 # The FP64 pipe issues at most 2 thread-instructions per SM per clock on GB300 (the
 # peak that ncu's FP64 pipe utilisation is relative to).
 FP64_INST_PER_SM_CLOCK = 2
