@@ -28,8 +28,9 @@ E2D_API int e2d_bench_kernels(E2DHandle h, int32_t steps, double* ms, int64_t* l
 /* Kernel-variant selection.  Every variant computes the same values; they differ in
    tile height, register/occupancy target and grid shape (one CTA per tile, or a
    persistent grid of resident CTAs striding over the tile table).
-   kernel: 0 = reconstruct (variants 0..4: tile height x min CTAs per SM of (8,2),
-   (8,1), (4,2), (4,4), (16,1)), 1 = flux (variants 0..2: min CTAs per SM 4, 1, 6),
+   kernel: 0 = reconstruct (variants 0..5: tile height x min CTAs per SM of (8,2),
+   (8,1), (4,2), (4,4), (16,1), and (4,8) in the FP32 form, where the FP64 path
+   runs variant 0), 1 = flux (variants 0..2: min CTAs per SM 4, 1, 6),
    2 = update (variant 0).                                                       */
 E2D_API int e2d_set_kernel_choice(E2DHandle h, int32_t kernel, int32_t variant, int32_t persistent);
 /* Autotuner: times every variant and grid shape of the reconstruct and flux kernels

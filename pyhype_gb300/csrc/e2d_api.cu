@@ -397,9 +397,10 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
 
   h->prec = cfg->precision;
   if (h->prec == E2D_FP32) {
-    // FP32 defaults measured on GB300 (2x4x1024^2): 4-row reconstruction tiles at 4
-    // CTAs/SM and the persistent flux grid at 6 CTAs/SM
-    h->kr = KernelChoice{3, false};
+    // FP32 defaults measured on GB300: 4-row reconstruction tiles at 8 CTAs/SM (the
+    // autotuner's choice on the 512-instance ensemble) and the persistent flux grid at
+    // 6 CTAs/SM (2x4x1024^2)
+    h->kr = KernelChoice{5, false};
     h->kf = KernelChoice{2, true};
   }
   if (int e = (h->prec == E2D_FP32 ? upload_geometry<float>(h, geo) : upload_geometry<double>(h, geo)))

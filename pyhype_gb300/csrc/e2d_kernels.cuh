@@ -129,7 +129,7 @@ struct KernelChoice {
   int variant;
   bool persistent;
 };
-constexpr int N_RECON_VARIANTS = 5;  // (tile height, min CTAs/SM): (8,2) (8,1) (4,2) (4,4) (16,1)
+constexpr int N_RECON_VARIANTS = 6;  // (tile height, min CTAs/SM): (8,2) (8,1) (4,2) (4,4) (16,1), (4,8) FP32 only
 constexpr int N_FLUX_VARIANTS = 3;   // min CTAs/SM: 4, 1, 6
 
 // launchers, instantiated for double (e2d_fp64.cu) and float (e2d_fp32.cu)

@@ -786,6 +786,11 @@ static cudaError_t recon_variant(const ParamsT<T>& P, const int4* const* tiles_b
     case 2: return recon_launch<T, LIM, RECON, false, 4, 2>(P, tiles_by_rty[0], n_by_rty[0], persistent, U, inst, F, none, st);
     case 3: return recon_launch<T, LIM, RECON, false, 4, 4>(P, tiles_by_rty[0], n_by_rty[0], persistent, U, inst, F, none, st);
     case 4: return recon_launch<T, LIM, RECON, false, 16, 1>(P, tiles_by_rty[2], n_by_rty[2], persistent, U, inst, F, none, st);
+    case 5:  // FP32 only (64 registers, 8 CTAs of 128 threads per SM); FP64 would spill
+      if constexpr (sizeof(T) == 4)
+        return recon_launch<T, LIM, RECON, false, 4, 8>(P, tiles_by_rty[0], n_by_rty[0], persistent, U, inst, F, none, st);
+      else
+        return recon_launch<T, LIM, RECON, false, 8, 2>(P, tiles_by_rty[1], n_by_rty[1], persistent, U, inst, F, none, st);
     default: return recon_launch<T, LIM, RECON, false, 8, 2>(P, tiles_by_rty[1], n_by_rty[1], persistent, U, inst, F, none, st);
   }
 }
