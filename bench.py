@@ -266,6 +266,7 @@ def ensemble_section(stream, full: bool = False, autotune: bool = True):
 
     E32 = EnsembleSolver(inst, precision=1, problem=P)
     E32.device.set_stream(stream.cuda_stream)
+    T0 = {"fp32": E32.device.totals()}
     if autotune:
         out["fp32_autotune"] = E32.device.autotune(reps=2)
     halted["fp32"].update(E32.run(w))
@@ -274,6 +275,7 @@ def ensemble_section(stream, full: bool = False, autotune: bool = True):
                            "steps": k32, "ms_per_step": ms32 / k32}
     E64 = EnsembleSolver(inst, precision=0, problem=P)
     E64.device.set_stream(stream.cuda_stream)
+    T0["fp64"] = E64.device.totals()
     halted["fp64"].update(E64.run(w))
     ms64 = timed(E64, k64, "fp64")
     out["fp64_batched"] = {"value": cells * stages * k64 / (ms64 * 1e-3), "unit": "cell-stage updates/s",
@@ -286,6 +288,15 @@ def ensemble_section(stream, full: bool = False, autotune: bool = True):
           for k, (x, y) in enumerate(zip(a, b)) if k not in bad]
     out["fp32_l1_density_rel_vs_fp64"] = {"after_steps": w + k32, "mean": float(np.mean(l1)), "max": float(np.max(l1)),
                                            "median": float(np.median(l1)), "instances": len(l1)}
+    # conservation (single reflecting blocks conserve mass and energy up to rounding):
+    # relative drift of each instance's FP64 totals over the run, largest over instances
+    keep = [k for k in range(len(inst)) if k not in bad]
+    drift = {}
+    for key, E in (("fp32", E32), ("fp64", E64)):
+        T1 = E.device.totals()
+        d = np.abs(T1[keep] - T0[key][keep]) / np.abs(T0[key][keep])
+        drift[key] = {"mass_max": float(d[:, 0].max()), "energy_max": float(d[:, 3].max())}
+    out["conservation_drift"] = dict(drift, after_steps=w + k32)
     out["halted_unrealizable"] = {"fp32": sorted(halted["fp32"]), "fp64": sorted(halted["fp64"]),
                                   "note": "the reference scheme reaches NaN on these instances (checked in the CPU "
                                           "oracle for instance 265); they are excluded from the L1 statistics"}
@@ -436,6 +447,7 @@ def dmr_section(stream):
     out = {"workload": "double-Mach reflection, 5 blocks x 400x500 cells, HLLL/Venkatakrishnan, primitive "
                        "reconstruction, SSP-RK2, CFL 0.4, t_final 0.2"}
     states = {}
+    totals = {}
     for prec in ("fp64", "fp32"):
         cfg, gen = double_mach()
         sim = Euler2D(cfg, gen, precision=prec)
@@ -453,9 +465,14 @@ def dmr_section(stream):
         out[prec] = {"value": cells * 2 * sim.num_time_step / (ms * 1e-3), "unit": "cell-stage updates/s",
                      "steps": sim.num_time_step, "seconds": ms * 1e-3, "t_final_reached": sim.t >= sim.t_final}
         states[prec] = np.concatenate([b.state.data[:, :, 0].ravel() for b in sim.blocks])
+        totals[prec] = sim.device.totals()[0]
         sim.device.close()
     a, b = states["fp64"], states["fp32"]
     out["fp32_l1_density_rel_vs_fp64"] = float(np.sum(np.abs(b - a)) / np.sum(np.abs(a)))
+    # inflow and outflow sides: the totals are not conserved; FP32 against FP64 at t_final
+    out["fp32_totals_rel_vs_fp64"] = {
+        "mass": float(abs(totals["fp32"][0] - totals["fp64"][0]) / abs(totals["fp64"][0])),
+        "energy": float(abs(totals["fp32"][3] - totals["fp64"][3]) / abs(totals["fp64"][3]))}
     out["fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
     return out
 
@@ -650,9 +667,20 @@ def main():
         S64b = _native.DeviceSolver(P, tableau=solver._time_integrator.tableau())
         S64b.set_stream(stream.cuda_stream)
         S64b.set_state(P.to_soa([b.state.data for b in solver.blocks]))
+        tot0 = S64b.totals()[0]
         S64b.run(0.0, t_final, max_steps=args.warmup + args.steps)
         U64 = S64b.get_state()
         l1 = float(np.sum(np.abs(U32[0] - U64[0])) / np.sum(np.abs(U64[0])))
+        tot64, tot32 = S64b.totals()[0], S32.totals()[0]
+        conservation = {
+            "totals_rel_vs_fp64": {"mass": float(abs(tot32[0] - tot64[0]) / abs(tot64[0])),
+                                   "energy": float(abs(tot32[3] - tot64[3]) / abs(tot64[3]))},
+            "drift_fp64": {"mass": float((tot64[0] - tot0[0]) / abs(tot0[0])),
+                           "energy": float((tot64[3] - tot0[3]) / abs(tot0[3]))},
+            "drift_fp32": {"mass": float((tot32[0] - tot0[0]) / abs(tot0[0])),
+                           "energy": float((tot32[3] - tot0[3]) / abs(tot0[3]))},
+            "note": "FP64 sums of A*U; the 2x4 layout is not conservative across blocks (the reference's "
+                    "inter-block faces), so the drift includes the scheme's own"}
         # per-kernel timing advances the FP32 state further: after the comparison
         k32 = np.zeros(5)
         c32 = np.zeros(5, dtype=np.int64)
@@ -660,6 +688,7 @@ def main():
         fp32 = {"value": ws * P.ncell * stages * args.steps / (ms32 * 1e-3), "unit": "cell-stage updates/s",
                 "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": ms / ms32,
                 "l1_density_rel_vs_fp64": l1, "l1_after_steps": args.warmup + args.steps,
+                "conservation": conservation,
                 "kernel_ms": {n: float(x) for n, x in zip(names, k32)}}
         S32.close()
         S64b.close()

@@ -242,6 +242,11 @@ E2D_API int e2d_check_realizable(E2DHandle h, E2DRealizability* out);
 /* Solver time and steps taken of every instance (batched problems advance each
    instance with its own CFL dt); arrays of E2DConfig.ninstances entries.        */
 E2D_API int e2d_instance_times(E2DHandle h, double* t_out, int32_t* steps_out);
+/* Conserved totals of the current state: totals[4 q + v] = sum over the cells of
+   instance q of A * U_v (mass, x and y momentum, energy), accumulated in FP64 on
+   either path in a fixed order (reproducible run to run).  No counterpart in the
+   reference; the FP32 form's conservation drift is stated against these.        */
+E2D_API int e2d_totals(E2DHandle h, double* totals);
 
 /* ---- per-operator entry points (parity testing) ---------------------------------- */
 /* dUdt of the current state (FiniteVolumeMethod.dUdt, pyhype/fvm/base.py:108-139)

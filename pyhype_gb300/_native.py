@@ -30,7 +30,7 @@ EXPORTS = (
     "e2d_abi_version", "e2d_last_error", "e2d_create", "e2d_destroy", "e2d_set_stream", "e2d_num_cells",
     "e2d_set_state", "e2d_get_state", "e2d_set_state_device", "e2d_get_state_device", "e2d_set_tableau",
     "e2d_compute_dt", "e2d_step", "e2d_run", "e2d_check_realizable", "e2d_residual", "e2d_instance_times",
-    "e2d_residual_vjp", "e2d_adjoint_forward", "e2d_adjoint_backward", "e2d_ghost_layer",
+    "e2d_residual_vjp", "e2d_adjoint_forward", "e2d_adjoint_backward", "e2d_ghost_layer", "e2d_totals",
 )
 
 
@@ -82,6 +82,7 @@ def load(path: Optional[str] = None):
     L.e2d_residual.argtypes = [vp, ctypes.c_double, vp, vp]
     L.e2d_residual_vjp.argtypes = [vp, ctypes.c_double, vp, vp]
     L.e2d_ghost_layer.argtypes = [vp, ctypes.c_double, vp]
+    L.e2d_totals.argtypes = [vp, vp]
     L.e2d_adjoint_forward.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, vp, vp, vp,
                                       ctypes.POINTER(ctypes.c_double)]
     L.e2d_adjoint_backward.argtypes = [vp, vp]
@@ -214,6 +215,14 @@ class DeviceSolver:
         out = dudt.cpu().numpy()
         if debug:
             return out, {k: v.cpu().numpy() for k, v in dbg_t.items()}
+        return out
+
+    def totals(self) -> np.ndarray:
+        """Conserved totals (sum of A * U per variable) of every instance, FP64,
+        shape (ninstances, 4)."""
+        n = max(1, int(self.problem.cfg.ninstances))
+        out = np.zeros((n, 4))
+        _check(self.L.e2d_totals(self.h, out.ctypes.data))
         return out
 
     def ghost_layer(self, t: float = 0.0) -> np.ndarray:

@@ -602,6 +602,31 @@ static int launch_dt_path(E2DHandle h) {
 }
 
 template <typename T>
+static int totals_path(E2DHandle h, double* totals) {
+  PathT<T>& p = path<T>(h);
+  const int nt = h->ncell_tiles;
+  std::vector<double> part(4 * (size_t)nt);
+  std::vector<int4> tl(nt);
+  double* dpart = nullptr;
+  CK(cudaMalloc(&dpart, sizeof(double) * part.size()));
+  cudaError_t e = launch_totals<T>(p.P, h->cell_tiles, nt, p.S.buf[0], dpart, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(part.data(), dpart, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(tl.data(), h->cell_tiles, sizeof(int4) * nt, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(dpart);
+  CK(e);
+  const size_t ninst = h->hinst.size();
+  for (size_t q = 0; q < 4 * ninst; ++q) totals[q] = 0.0;
+  for (int k = 0; k < nt; ++k) {  // tile order: reproducible
+    const int q = h->hblocks[tl[k].x].instance;
+    for (int v = 0; v < 4; ++v) totals[4 * q + v] += part[4 * (size_t)k + v];
+  }
+  return 0;
+}
+
+template <typename T>
 static int ghost_layer_path(E2DHandle h, double t, double* out) {
   PathT<T>& p = path<T>(h);
   std::vector<int64_t> base(h->hblocks.size());
@@ -699,6 +724,11 @@ int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* d) {
   CK(launch_end_step(h->inst, ninst, h->real, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return 0;
+}
+
+int e2d_totals(E2DHandle h, double* totals) {
+  if (!h || !totals) return fail(E2D_ERR_INVALID, "null argument");
+  return E2D_DISPATCH(h, totals_path, totals);
 }
 
 int e2d_ghost_layer(E2DHandle h, double t, double* ghosts_dev) {

@@ -151,6 +151,9 @@ template <typename T>
 cudaError_t launch_realizable(const ParamsT<T>& P, const int4* cell_tiles, int ntiles, const T* U,
                               RealizState* real, cudaStream_t st);
 template <typename T>
+cudaError_t launch_totals(const ParamsT<T>& P, const int4* tiles, int n, const T* U, double* partial,
+                          cudaStream_t st);
+template <typename T>
 cudaError_t launch_ghost_layer(const ParamsT<T>& P, const T* U, double t, const int64_t* base, double* out,
                                int64_t nghost, int maxlen, cudaStream_t st);
 cudaError_t launch_begin_step(InstanceState* inst, int ninst, double cfl, int use_min, cudaStream_t st);

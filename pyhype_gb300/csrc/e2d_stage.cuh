@@ -927,6 +927,47 @@ cudaError_t launch_realizable(const ParamsT<T>& P, const int4* tiles, int n, con
   return cudaGetLastError();
 }
 
+// Conserved totals: per 8-row cell tile, the sum over its cells of A * U_v for the
+// four conserved variables, accumulated in FP64 whatever the path's precision (cell
+// values and areas promoted), in a fixed order (a shared-memory tree over the tile's
+// 256 cells), into partial[tile][4].  The caller sums the partials of each instance in
+// tile order, so the totals are reproducible run to run.
+template <typename T>
+__global__ void __launch_bounds__(TX * TY) k_totals(ParamsT<T> P, const int4* __restrict__ tiles,
+                                                    const T* __restrict__ U, double* __restrict__ partial) {
+  __shared__ double red[4][TX * TY];
+  const int4 tl = tiles[blockIdx.x];
+  const E2DBlock* B = P.blocks + tl.x;
+  const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
+  const int i = tl.y + ty, j = tl.z + tx;
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  if (i < B->ny && j < B->nx) {
+    const int64_t c = cell_at(B, i, j);
+    const double A = (double)P.geo.cell[E2D_G_A][c];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = A * (double)U[k * P.ncell + c];
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) red[k][threadIdx.x] = v[k];
+  __syncthreads();
+  for (int w = TX * TY / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) partial[4 * (int64_t)blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
+}
+
+template <typename T>
+cudaError_t launch_totals(const ParamsT<T>& P, const int4* tiles, int n, const T* U, double* partial,
+                          cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_totals<T><<<n, TX * TY, 0, st>>>(P, tiles, U, partial);
+  return cudaGetLastError();
+}
+
 // Ghost layer of every block in the reconstruction variables: the values that
 // Blocks.apply_boundary_condition leaves in the ghost blocks and that
 // ReconstructionBlock.from_block converts (pyhype/blocks/base.py:448-471,
@@ -981,7 +1022,8 @@ cudaError_t launch_ghost_layer(const ParamsT<T>& P, const T* U, double t, const 
   template cudaError_t launch_dt<T>(const ParamsT<T>&, const int4*, int, const T*, InstanceState*, cudaStream_t); \
   template cudaError_t launch_realizable<T>(const ParamsT<T>&, const int4*, int, const T*, RealizState*, cudaStream_t); \
   template cudaError_t launch_ghost_layer<T>(const ParamsT<T>&, const T*, double, const int64_t*, double*, int64_t, \
-                                             int, cudaStream_t);
+                                             int, cudaStream_t);                                                 \
+  template cudaError_t launch_totals<T>(const ParamsT<T>&, const int4*, int, const T*, double*, cudaStream_t);
 
 // for units that include this header but call the launchers instantiated elsewhere
 #define E2D_EXTERN_STAGE_LAUNCHERS(T)                                                                           \
@@ -998,6 +1040,7 @@ cudaError_t launch_ghost_layer(const ParamsT<T>& P, const T* U, double t, const 
   extern template cudaError_t launch_realizable<T>(const ParamsT<T>&, const int4*, int, const T*, RealizState*,  \
                                                    cudaStream_t);                                                \
   extern template cudaError_t launch_ghost_layer<T>(const ParamsT<T>&, const T*, double, const int64_t*, double*, \
-                                                    int64_t, int, cudaStream_t);
+                                                    int64_t, int, cudaStream_t);                                 \
+  extern template cudaError_t launch_totals<T>(const ParamsT<T>&, const int4*, int, const T*, double*, cudaStream_t);
 
 }  // namespace e2d
