@@ -294,7 +294,8 @@ def ensemble_section(stream, full: bool = False, autotune: bool = True):
     drift = {}
     for key, E in (("fp32", E32), ("fp64", E64)):
         T1 = E.device.totals()
-        d = np.abs(T1[keep] - T0[key][keep]) / np.abs(T0[key][keep])
+        with np.errstate(divide="ignore", invalid="ignore"):  # momentum totals are 0
+            d = np.abs(T1[keep] - T0[key][keep]) / np.abs(T0[key][keep])
         drift[key] = {"mass_max": float(d[:, 0].max()), "energy_max": float(d[:, 3].max())}
     out["conservation_drift"] = dict(drift, after_steps=w + k32)
     out["halted_unrealizable"] = {"fp32": sorted(halted["fp32"]), "fp64": sorted(halted["fp64"]),
