@@ -68,3 +68,62 @@ def test_no_device_fails_loudly():
     z = G.load("ops_explosion_cons")
     with pytest.raises(E2DError):
         DeviceSolver(G.problem(z))
+
+
+def _copy(obj):
+    dup = type(obj)()
+    ctypes.memmove(ctypes.addressof(dup), ctypes.addressof(obj), ctypes.sizeof(obj))
+    return dup
+
+
+def _mutations():
+    def cfg(field, value):
+        return lambda c, b, g: setattr(c, field, value)
+
+    def blk(i, field, value, idx=None):
+        def f(c, b, g):
+            if idx is None:
+                setattr(b[i], field, value)
+            else:
+                getattr(b[i], field)[idx] = value
+        return f
+
+    def no_plane(c, b, g):
+        g.cell[0] = None
+
+    return [
+        ("nblocks", cfg("nblocks", 0), "nblocks must be >= 1"),
+        ("precision", cfg("precision", 7), "unknown precision"),
+        ("flux code", cfg("flux", 9), "unknown flux/limiter/reconstruction code"),
+        ("quadrature points", cfg("nqp", 4), "nqp must be 1, 2 or 3"),
+        ("block size", blk(0, "nx", 1), "block 0: nx, ny must be >= 2"),
+        ("instance id", blk(0, "instance", 5), "block 0: bad instance id"),
+        ("offset", blk(1, "cell_offset", -1), "block 1: negative offset"),
+        ("side kind", blk(0, "side_kind", 99, 0), "block 0 side 0: bad kind"),
+        ("neighbour index", blk(0, "neighbor", 42, 0), "neighbour 42 out of range"),
+        ("neighbour size", blk(1, "ny", 39), "neighbour size mismatch"),
+        ("geometry", no_plane, "geometry cell plane 0 missing"),
+    ]
+
+
+@pytest.mark.parametrize("name,mutate,message", _mutations(), ids=[m[0] for m in _mutations()])
+def test_create_validates_the_problem_before_touching_a_device(name, mutate, message):
+    """e2d_create checks the configuration, block table and geometry on the host and
+    returns E2D_ERR_INVALID with a message, before any device call (so this runs
+    without a GPU)."""
+    import _golden as G
+    from pyhype_gb300 import _native
+
+    z = G.load("m2x4_40")
+    P = G.problem(z)
+    assert P.cfg.nblocks == 8
+    c = _copy(P.cfg)
+    b = (type(P.blocks[0]) * P.cfg.nblocks)()
+    ctypes.memmove(b, P.blocks, ctypes.sizeof(b))
+    g = _copy(P.geometry)
+    mutate(c, b, g)
+    L = _native.load()
+    h = ctypes.c_void_p()
+    code = L.e2d_create(ctypes.addressof(c), ctypes.addressof(b), ctypes.addressof(g), ctypes.byref(h))
+    assert code == -1 and not h.value
+    assert message in L.e2d_last_error().decode()
