@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=1024, help="cells per block side")
+    ap.add_argument("--n", "--cells-per-side", dest="n", type=int, default=1024, help="cells per block side")
     ap.add_argument("--cpu-steps", type=int, default=1, help="RK4 steps in the CPU-baseline sample")
     ap.add_argument("--skip-cpu-baseline", action="store_true", help="omit the CPU baseline (profiling runs)")
     ap.add_argument("--skip-ensemble", action="store_true", help="omit the batched-ensemble section")
