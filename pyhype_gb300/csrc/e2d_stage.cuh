@@ -28,6 +28,7 @@
 
 #include "e2d_device.cuh"
 #include "e2d_kernels.cuh"
+#include "e2d_slope_pick.cuh"
 
 namespace e2d {
 
@@ -225,28 +226,46 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
     const T dmin = vmin(vmin(vmin(vmin(w0, we), ea), so), no) - w0;
     T hot[4];
     T ph = T(0);
+    if constexpr (sizeof(T) == 8) {
+      // FP64: psi only at the faces that decide the minimum (e2d_slope_pick.cuh); all
+      // four when the pick cannot rule a face out.  Same expressions, same phi.
+      double davg[4];
 #pragma unroll
-    for (int s = 0; s < 4; ++s) {
-      hot[s] = gx * hx[s] + gy * hy[s];
-      T davg;
-      if constexpr (sizeof(T) == 4) {
+      for (int s = 0; s < 4; ++s) {
+        hot[s] = gx * hx[s] + gy * hy[s];
+        davg[s] = (w0 + hot[s]) - w0;
+      }
+      const SlopePick k = pick_slopes<LIM>(dmax, dmin, davg);
+      if (k.ok) {
+        ph = psi_s<LIM>(k.ga ? qdiv(k.na, k.da) : T(1));
+        if (k.second) ph = vmin(ph, psi_s<LIM>(k.gb ? qdiv(k.nb, k.db) : T(1)));
+      } else {
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          const bool pos = is_pos(davg[s]), neg = is_neg(davg[s]);
+          const T p = psi_s<LIM>((pos || neg) ? qdiv(pos ? dmax : dmin, davg[s]) : T(1));
+          ph = (s == 0) ? p : vmin(ph, p);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        hot[s] = gx * hx[s] + gy * hy[s];
         // FP64's round trip (w0 + hot) - w0 is hot itself unless |hot| is below half
         // an FP64 ulp of w0, where it is zero and the slope takes its davg == 0
         // branch (psi(1)).  In FP32 the same round trip would zero every |hot| below
         // 2^-25 |w0| and switch branches where the FP64 path does not, so the FP32 form
         // applies the FP64 threshold, 2^-53 times the power of two of w0.
         const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
-        davg = (fabs(hot[s]) < half_ulp64) ? T(0) : hot[s];
-      } else {
-        davg = (w0 + hot[s]) - w0;
+        const T davg = (fabs(hot[s]) < half_ulp64) ? T(0) : hot[s];
+        // slope dmax/davg (davg > 0), dmin/davg (davg < 0), 1 (davg == 0), with a single
+        // division so lanes of different signs share one division sequence; a zero davg
+        // divides nothing
+        const bool pos = is_pos(davg), neg = is_neg(davg);
+        const T sl = (pos || neg) ? qdiv(pos ? dmax : dmin, davg) : T(1);
+        const T p = psi_s<LIM>(sl);
+        ph = (s == 0) ? p : vmin(ph, p);
       }
-      // slope dmax/davg (davg > 0), dmin/davg (davg < 0), 1 (davg == 0), with a single
-      // division so lanes of different signs share one division sequence; a zero davg
-      // divides nothing
-      const bool pos = is_pos(davg), neg = is_neg(davg);
-      const T sl = (pos || neg) ? qdiv(pos ? dmax : dmin, davg) : T(1);
-      const T p = psi_s<LIM>(sl);
-      ph = (s == 0) ? p : vmin(ph, p);
     }
     ph = is_neg(ph) ? T(0) : ph;
 #pragma unroll
