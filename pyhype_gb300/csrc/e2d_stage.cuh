@@ -217,8 +217,8 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
     const T so = sW[v][ty][tx + 1];
     const T no = sW[v][ty + 2][tx + 1];
     // interface averages (quad_block.py:181-218) and Green-Gauss (greengauss.py:137-155)
-    const T ie = T(0.5) * (w0 + ea), iw = T(0.5) * (we + w0);
-    const T in = T(0.5) * (w0 + no), is = T(0.5) * (so + w0);
+    const T ie = half(w0 + ea), iw = half(we + w0);
+    const T in = half(w0 + no), is = half(so + w0);
     const T gx = (ie * LcE + iw * (-LcW) + in * LcN + is * (-LcS)) * ia;
     const T gy = (ie * LsE + iw * (-LsW) + in * LsN + is * (-LsS)) * ia;
     // limiter (limiters/base.py:47-221)
@@ -433,8 +433,8 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_qp(ParamsT<T> P, const 
     const T ea = sW[v][ty + 1][tx + 2];
     const T so = sW[v][ty][tx + 1];
     const T no = sW[v][ty + 2][tx + 1];
-    const T ie = T(0.5) * (w0 + ea), iw = T(0.5) * (we + w0);
-    const T in = T(0.5) * (w0 + no), is = T(0.5) * (so + w0);
+    const T ie = half(w0 + ea), iw = half(we + w0);
+    const T in = half(w0 + no), is = half(so + w0);
     const T gx = (ie * LcE + iw * (-LcW) + in * LcN + is * (-LcS)) * ia;
     const T gy = (ie * LsE + iw * (-LsW) + in * LsN + is * (-LsS)) * ia;
     const T dmax = vmax(vmax(vmax(vmax(w0, we), ea), so), no) - w0;
@@ -586,7 +586,7 @@ __device__ __forceinline__ void flux_tile(const ParamsT<T>& P, const int4 tl, co
     if (!cart) unrotate(Fx, P.geo.vface[E2D_F_COS][f], P.geo.vface[E2D_F_SIN][f]);
     if (DBG && dbg.vflux) store4(dbg.vflux, P.nvface, f, Fx);
     const T len = P.geo.vface[E2D_F_L][f];
-    T I[4] = {len * (T(2) * Fx[0]), len * (T(2) * Fx[1]), len * (T(2) * Fx[2]), len * (T(2) * Fx[3])};
+    T I[4] = {len * twice(Fx[0]), len * twice(Fx[1]), len * twice(Fx[2]), len * twice(Fx[3])};
     store4(F.vI, P.nvface, f, I);
   }
   if (j < nx) {
@@ -600,7 +600,7 @@ __device__ __forceinline__ void flux_tile(const ParamsT<T>& P, const int4 tl, co
     else unrotate(Fy, P.geo.hface[E2D_F_COS][f], P.geo.hface[E2D_F_SIN][f]);
     if (DBG && dbg.hflux) store4(dbg.hflux, P.nhface, f, Fy);
     const T len = P.geo.hface[E2D_F_L][f];
-    T I[4] = {len * (T(2) * Fy[0]), len * (T(2) * Fy[1]), len * (T(2) * Fy[2]), len * (T(2) * Fy[3])};
+    T I[4] = {len * twice(Fy[0]), len * twice(Fy[1]), len * twice(Fy[2]), len * twice(Fy[3])};
     store4(F.hI, P.nhface, f, I);
   }
 }
@@ -642,7 +642,7 @@ __device__ __forceinline__ void update_tile(const ParamsT<T>& P, const int4 tl, 
     for (int v = 0; v < 4; ++v) {
       const T IW = F.vI[v * P.nvface + fW], IE = F.vI[v * P.nvface + fE];
       const T IS = F.hI[v * P.nhface + fS], IN = F.hI[v * P.nhface + fN];
-      k[v] = qdiv(T(0.5) * (IW - IE + IS - IN), A);
+      k[v] = qdiv(half(IW - IE + IS - IN), A);
     }
     if (dudt_out) {
 #pragma unroll
