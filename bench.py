@@ -628,6 +628,26 @@ def main():
     names = ["dt", "reconstruct", "flux", "update", "bookkeeping"]
     share = kms * kcnt
     dom = int(np.argmax(share))
+    # inter-block halo: reconstruction over the real tiles against the same number of
+    # tiles with those along inter-block sides (and along any side) made interior
+    halo = None
+    try:
+        L.e2d_bench_halo.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+        hms = np.zeros(3)
+        hn = np.zeros(3, dtype=np.int64)
+        if L.e2d_bench_halo(dev.h, 10, hms.ctypes.data, hn.ctypes.data) != 0:
+            raise RuntimeError(L.e2d_last_error().decode())
+        t, _ = dev.run(t, t_final, max_steps=1)  # face arrays rebuilt by a full step
+        halo = {"reconstruct_ms": float(hms[0]), "inter_block_tiles_made_interior_ms": float(hms[1]),
+                "all_side_tiles_made_interior_ms": float(hms[2]), "tiles": int(hn[0]),
+                "inter_block_side_tiles": int(hn[1]), "side_tiles": int(hn[2]),
+                "inter_block_halo_ms_per_stage": float(hms[0] - hms[1]),
+                "halo_and_bc_ms_per_stage": float(hms[0] - hms[2]),
+                "inter_block_halo_share_of_step": float((hms[0] - hms[1]) * stages / (ms / args.steps)),
+                "note": "ghost cells and boundary face states are formed inside the reconstruction kernel's "
+                        "side tiles; no separate halo pass or copy"}
+    except Exception as exc:
+        halo = {"error": str(exc)}
     peak_fma = ctypes.c_double(0.0)
     peak_add = ctypes.c_double(0.0)
     L.e2d_bench_fp64_peak(0, ctypes.byref(peak_fma))
@@ -759,6 +779,7 @@ def main():
                            f"{peak_add.value:.3f} TFLOP/s",
             "kernel_ms": {n: float(x) for n, x in zip(names, kms)},
             "kernel_share": {n: float(s / share.sum()) for n, s in zip(names, share)},
+            "halo": halo,
             "flops_per_launch": flops,
             "fp64_issue": fp64_issue,
             "hbm": {"achieved_gbs": hbm_achieved, "peak_gbs": hbm_peak,

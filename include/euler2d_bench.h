@@ -25,6 +25,17 @@ E2D_API int e2d_bench_fp64_peak(int32_t op, double* tflops);
 #define E2D_BENCH_NK 5
 E2D_API int e2d_bench_kernels(E2DHandle h, int32_t steps, double* ms, int64_t* launches);
 
+/* Cost of the halo: the reconstruction kernel (8-row tiles, default variant) forms
+   ghost cells (inter-block neighbours and boundary conditions) and block-boundary
+   face states on the fly in the tiles along block sides.  ms[0] receives the average
+   duration of `reps` launches over the real tile table; ms[1] the same number of
+   tiles with every tile touching an inter-block side replaced by an interior tile;
+   ms[2] with every tile touching any block side replaced.  ntiles[0..2] = all tiles,
+   tiles touching an inter-block side, tiles touching any side.  ms[0] - ms[1] is the
+   inter-block halo cost of one stage.  Face arrays are stale after the call until
+   the next reconstruction.                                                      */
+E2D_API int e2d_bench_halo(E2DHandle h, int32_t reps, double* ms, int64_t* ntiles);
+
 /* Kernel-variant selection.  Every variant computes the same values; they differ in
    tile height, register/occupancy target and grid shape (one CTA per tile, or a
    persistent grid of resident CTAs striding over the tile table).

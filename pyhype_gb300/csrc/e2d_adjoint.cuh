@@ -59,8 +59,8 @@ struct LimiterTrace {
 template <typename T>
 __device__ __forceinline__ void green_gauss(T w0, T we, T ea, T so, T no, T LcE, T LsE, T LcW, T LsW, T LcN, T LsN,
                                             T LcS, T LsS, T ia, T& gx, T& gy) {
-  const T ie = T(0.5) * (w0 + ea), iw = T(0.5) * (we + w0);
-  const T in = T(0.5) * (w0 + no), is = T(0.5) * (so + w0);
+  const T ie = half(w0 + ea), iw = half(we + w0);
+  const T in = half(w0 + no), is = half(so + w0);
   gx = (ie * LcE + iw * (-LcW) + in * LcN + is * (-LcS)) * ia;
   gy = (ie * LsE + iw * (-LsW) + in * LsN + is * (-LsS)) * ia;
 }
@@ -84,25 +84,57 @@ __device__ __forceinline__ void limiter_forward(T w0, T we, T ea, T so, T no, T 
   const T dmax = mx - w0, dmin = mn - w0;
   int sel = 0, ssign = 0;
   T ssl = T(0), sdavg = T(0);
+  T dv[4];
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     hot[s] = gx * hx[s] + gy * hy[s];
-    T davg;
     if constexpr (sizeof(T) == 4) {
       const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
-      davg = (fabs(hot[s]) < half_ulp64) ? T(0) : hot[s];
+      dv[s] = (fabs(hot[s]) < half_ulp64) ? T(0) : hot[s];
     } else {
-      davg = (w0 + hot[s]) - w0;
+      dv[s] = (w0 + hot[s]) - w0;
     }
-    const bool pos = is_pos(davg), neg = is_neg(davg);
-    const T sl = (pos || neg) ? qdiv(pos ? dmax : dmin, davg) : T(1);
-    const T p = psi_s<LIM>(sl);
-    if (s == 0 || vlt(p, ph)) {
-      ph = p;
-      sel = s;
-      ssl = sl;
-      sdavg = davg;
-      ssign = pos ? 1 : (neg ? -1 : 0);
+  }
+  bool done = false;
+  if constexpr (sizeof(T) == 8) {
+    // FP64: psi only at the faces that decide phi, as the reconstruction kernel does;
+    // the selected face is the first whose psi equals phi, as in the loop below.
+    // Barth-Jespersen at phi == 1 (every face with s >= 1 gives 1: the first face is
+    // selected) takes the loop.
+    const SlopePick k = pick_slopes<LIM>(dmax, dmin, dv);
+    if (k.ok) {
+      T sl = k.ga ? qdiv(k.na, k.da) : T(1);
+      T p = psi_s<LIM>(sl);
+      int f = k.fa;
+      T d = k.da;
+      if (k.second) {
+        const T slb = k.gb ? qdiv(k.nb, k.db) : T(1);
+        const T pb = psi_s<LIM>(slb);
+        if (vlt(pb, p) || (!vlt(p, pb) && k.fb < k.fa)) {
+          p = pb; sl = slb; f = k.fb; d = k.db;
+        }
+      }
+      if (!(LIM == E2D_LIM_BARTH_JESPERSEN && p == T(1))) {
+        done = true;
+        ph = p; sel = f; ssl = sl; sdavg = d;
+        ssign = is_pos(d) ? 1 : (is_neg(d) ? -1 : 0);
+      }
+    }
+  }
+  if (!done) {
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const T davg = dv[s];
+      const bool pos = is_pos(davg), neg = is_neg(davg);
+      const T sl = (pos || neg) ? qdiv(pos ? dmax : dmin, davg) : T(1);
+      const T p = psi_s<LIM>(sl);
+      if (s == 0 || vlt(p, ph)) {
+        ph = p;
+        sel = s;
+        ssl = sl;
+        sdavg = davg;
+        ssign = pos ? 1 : (neg ? -1 : 0);
+      }
     }
   }
   const bool clipped = is_neg(ph);
@@ -140,12 +172,12 @@ __global__ void __launch_bounds__(TX * TY) k_flux_vjp(ParamsT<T> P, const int4* 
   if (i < ny) {
     const int64_t f = vf_at(B, i, j);
     T lF[4];
-    const T len2 = T(2) * P.geo.vface[E2D_F_L][f];
+    const T len2 = twice(P.geo.vface[E2D_F_L][f]);
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       T li = T(0);
-      if (j < nx) { const int64_t c = cell_at(B, i, j); li += T(0.5) * lk[v * P.ncell + c] * ia[c]; }
-      if (j > 0) { const int64_t c = cell_at(B, i, j - 1); li -= T(0.5) * lk[v * P.ncell + c] * ia[c]; }
+      if (j < nx) { const int64_t c = cell_at(B, i, j); li += half(lk[v * P.ncell + c]) * ia[c]; }
+      if (j > 0) { const int64_t c = cell_at(B, i, j - 1); li -= half(lk[v * P.ncell + c]) * ia[c]; }
       lF[v] = len2 * li;
     }
     if (!cart) rotate(lF, P.geo.vface[E2D_F_COS][f], P.geo.vface[E2D_F_SIN][f]);  // transpose of unrotate
@@ -162,12 +194,12 @@ __global__ void __launch_bounds__(TX * TY) k_flux_vjp(ParamsT<T> P, const int4* 
   if (j < nx) {
     const int64_t f = hf_at(B, i, j);
     T lF[4];
-    const T len2 = T(2) * P.geo.hface[E2D_F_L][f];
+    const T len2 = twice(P.geo.hface[E2D_F_L][f]);
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       T li = T(0);
-      if (i < ny) { const int64_t c = cell_at(B, i, j); li += T(0.5) * lk[v * P.ncell + c] * ia[c]; }
-      if (i > 0) { const int64_t c = cell_at(B, i - 1, j); li -= T(0.5) * lk[v * P.ncell + c] * ia[c]; }
+      if (i < ny) { const int64_t c = cell_at(B, i, j); li += half(lk[v * P.ncell + c]) * ia[c]; }
+      if (i > 0) { const int64_t c = cell_at(B, i - 1, j); li -= half(lk[v * P.ncell + c]) * ia[c]; }
       lF[v] = len2 * li;
     }
     if (cart) rotate90(lF);  // transpose of unrotate90
@@ -402,12 +434,12 @@ __global__ void __launch_bounds__(TX * VTY, 4) k_reconstruct_vjp(ParamsT<T> P, c
     }
     const T lie = (lgx * LcE + lgy * LsE) * ia, liw = -(lgx * LcW + lgy * LsW) * ia;
     const T lin = (lgx * LcN + lgy * LsN) * ia, lis = -(lgx * LcS + lgy * LsS) * ia;
-    lw0 += T(0.5) * (lie + liw + lin + lis);
+    lw0 += half(lie + liw + lin + lis);
     lst[0] += lw0;
-    lst[1] += T(0.5) * liw;
-    lst[2] += T(0.5) * lie;
-    lst[3] += T(0.5) * lis;
-    lst[4] += T(0.5) * lin;
+    lst[1] += half(liw);
+    lst[2] += half(lie);
+    lst[3] += half(lis);
+    lst[4] += half(lin);
     st[(ST_SELF * 4 + v) * P.ncell + c] = lst[0];
     st[(ST_W * 4 + v) * P.ncell + c] = lst[1];
     st[(ST_E * 4 + v) * P.ncell + c] = lst[2];
@@ -636,7 +668,7 @@ __global__ void k_side_pressure_grad(ParamsT<T> P, int b, int side, const T* __r
   const T len = vert ? P.geo.vface[E2D_F_L][f] : P.geo.hface[E2D_F_L][f];
   const T rho = U[c], u = qdiv(U[P.ncell + c], rho), v = qdiv(U[2 * P.ncell + c], rho);
   const T g = T(coef) * len * P.gas[1];
-  lam[c] += g * T(0.5) * (u * u + v * v);
+  lam[c] += half(g) * (u * u + v * v);
   lam[P.ncell + c] -= g * u;
   lam[2 * P.ncell + c] -= g * v;
   lam[3 * P.ncell + c] += g;

@@ -268,6 +268,79 @@ static int bench_kernels_t(E2DHandle h, int32_t steps, double* ms, int64_t* laun
 }
 
 
+// Cost of forming ghost cells and block-boundary face states inside the
+// reconstruction kernel: the 8-row reconstruction launch over the real tile table,
+// against launches of the same number of tiles in which the tiles touching an
+// inter-block side (ms[1]) or any block side (ms[2]) are replaced by interior tiles.
+// The replacement launches recompute interior tiles twice (same values written twice)
+// and leave the replaced faces stale until the next reconstruction, which every
+// stage runs before it reads face arrays.
+template <typename T>
+static int bench_halo_t(E2DHandle h, int32_t reps, double* ms, int64_t* ntiles) {
+  PathT<T>& p = path<T>(h);
+  const int n = h->ts.ncell[1];
+  std::vector<int4> all(n);
+  CK(cudaMemcpy(all.data(), h->ts.cell[1], sizeof(int4) * n, cudaMemcpyDeviceToHost));
+  std::vector<int4> interior;
+  std::vector<char> nb_edge(n, 0), edge(n, 0);
+  for (int k = 0; k < n; ++k) {
+    const int4 t = all[k];
+    const E2DBlock& B = h->hblocks[t.x];
+    const bool touch[4] = {t.z + TX >= B.nx, t.z == 0, t.y + 8 >= B.ny, t.y == 0};  // E, W, N, S
+    for (int s = 0; s < 4; ++s) {
+      if (!touch[s]) continue;
+      edge[k] = 1;
+      if (B.side_kind[s] == E2D_SIDE_NEIGHBOR) nb_edge[k] = 1;
+    }
+    if (!edge[k]) interior.push_back(t);
+  }
+  if (interior.empty()) return fail(E2D_ERR_UNSUPPORTED, "e2d_bench_halo: the problem has no interior tiles");
+  std::vector<int4> lists[3] = {all, all, all};
+  int64_t counts[3] = {n, 0, 0};
+  size_t r1 = 0, r2 = 0;
+  for (int k = 0; k < n; ++k) {
+    if (nb_edge[k]) { lists[1][k] = interior[r1++ % interior.size()]; ++counts[1]; }
+    if (edge[k]) { lists[2][k] = interior[r2++ % interior.size()]; ++counts[2]; }
+  }
+  int4* d = nullptr;
+  CK(cudaMalloc(&d, sizeof(int4) * n));
+  // every instance active while timing (a finished run leaves them inactive, and an
+  // inactive instance's tiles return at once); the instance table is put back after
+  const int ninst = (int)h->hinst.size();
+  std::vector<InstanceState> saved(ninst);
+  CK(cudaMemcpyAsync(saved.data(), h->inst, sizeof(InstanceState) * ninst, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  CK(launch_set_time(h->inst, ninst, saved[0].t, 0.0, h->stream));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int err = 0;
+  for (int v = 0; v < 3 && !err; ++v) {
+    TileSet ts = h->ts;
+    ts.cell[1] = d;
+    cudaError_t ce = cudaMemcpyAsync(d, lists[v].data(), sizeof(int4) * n, cudaMemcpyHostToDevice, h->stream);
+    for (int r = -1; r < reps && ce == cudaSuccess; ++r) {  // r = -1 warms up
+      if (r == 0) ce = cudaEventRecord(e0, h->stream);
+      if (ce == cudaSuccess)
+        ce = launch_reconstruct<T>(p.P, ts, KernelChoice{0, false}, p.S.buf[0], h->inst, p.F, nullptr, h->stream);
+    }
+    float t = 0.f;
+    if (ce == cudaSuccess) ce = cudaEventRecord(e1, h->stream);
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+    if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, e0, e1);
+    if (ce != cudaSuccess) err = fail(E2D_ERR_CUDA, "e2d_bench_halo: %s", cudaGetErrorString(ce));
+    ms[v] = t / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  CK(cudaMemcpyAsync(h->inst, saved.data(), sizeof(InstanceState) * ninst, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (ntiles)
+    for (int v = 0; v < 3; ++v) ntiles[v] = counts[v];
+  return err;
+}
+
 // Times `reps` launches of one kernel class under the handle's current choice.
 template <typename T>
 static int time_kernel(E2DHandle h, int which, int reps, float* ms) {
@@ -855,6 +928,12 @@ int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps, int
 int e2d_bench_kernels(E2DHandle h, int32_t steps, double* ms, int64_t* launches) {
   if (!h || !ms || steps < 1) return fail(E2D_ERR_INVALID, "bad argument");
   return E2D_DISPATCH(h, bench_kernels_t, steps, ms, launches);
+}
+
+int e2d_bench_halo(E2DHandle h, int32_t reps, double* ms, int64_t* ntiles) {
+  if (!h || !ms || reps < 1) return fail(E2D_ERR_INVALID, "bad argument");
+  if (h->cfg.nqp > 1) return fail(E2D_ERR_UNSUPPORTED, "e2d_bench_halo: one-point face rule only");
+  return E2D_DISPATCH(h, bench_halo_t, reps, ms, ntiles);
 }
 
 int e2d_set_kernel_choice(E2DHandle h, int32_t kernel, int32_t variant, int32_t persistent) {

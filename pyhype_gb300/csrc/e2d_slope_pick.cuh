@@ -62,6 +62,9 @@ struct SlopePick {
   bool ga, gb;    // false: that slope is exactly 1 (davg == 0), not na/da
   bool second;    // phi = min(psi(na/da), psi(nb/db)); else phi = psi(na/da)
   bool ok;        // false: evaluate all four faces
+  int fa, fb;     // their faces (0..3 = E, W, N, S): the first face whose psi equals
+                  // phi is fa, or with `second` the one of fa, fb whose psi is smaller
+                  // (the lower index when both are equal)
 };
 
 namespace slope_pick_detail {
@@ -238,6 +241,8 @@ E2D_HD SlopePick pick_slopes(double dmax, double dmin, const double (&den)[4]) {
     if (k == ib) p.db = den[k];
   }
   p.second = use_a && use_b;
+  p.fa = i1;
+  p.fb = ib;
   p.ga = nonzero(p.da);
   p.gb = nonzero(p.db);
   p.na = signbit_of(p.da) ? dmin : dmax;

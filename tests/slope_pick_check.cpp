@@ -1,6 +1,7 @@
 // Host check of pick_slopes (pyhype_gb300/csrc/e2d_slope_pick.cuh): for random and
 // adversarial cells, phi from psi at the picked faces equals phi from all four faces,
-// bit for bit, for all four limiters.  The approximate reciprocal of the device is
+// bit for bit, and the picked face is the first face whose psi is phi (the selection
+// the adjoint differentiates), for all four limiters.  The approximate reciprocal of the device is
 // replaced by the correctly rounded one perturbed by up to +-2 ulp at random, which is
 // wider than the device instruction's stated 1 ulp.
 //
@@ -16,11 +17,17 @@
 
 static std::mt19937_64 g_rng;
 
+// Like the device instruction, the stand-in is a function of its input: the
+// perturbation (-2..+2 ulp) is drawn from a hash of the input bits and a per-run salt.
+static uint32_t g_salt = 0;
 static float perturbed_rcp(float x) {
   float y = 1.0f / x;
-  uint32_t u;
+  uint32_t u, xb;
   std::memcpy(&u, &y, sizeof u);
-  u += (int)(g_rng() % 5) - 2;
+  std::memcpy(&xb, &x, sizeof xb);
+  uint32_t hsh = (xb ^ g_salt) * 0x9e3779b1u;
+  hsh ^= hsh >> 15;
+  u += (int)(hsh % 5) - 2;
   std::memcpy(&y, &u, sizeof y);
   return y;
 }
@@ -72,12 +79,16 @@ static double psi_s(double s) {
   return psi<LIM>(s);
 }
 
+// phi over all four faces, and the first face whose psi is phi (the selection the
+// adjoint differentiates)
 template <int LIM>
-static double phi_all(double dmax, double dmin, const double (&davg)[4]) {
+static double phi_all(double dmax, double dmin, const double (&davg)[4], int& sel) {
   double ph = 0.0;
+  sel = 0;
   for (int s = 0; s < 4; ++s) {
     const bool pos = is_pos(davg[s]), neg = is_neg(davg[s]);
     const double p = psi_s<LIM>((pos || neg) ? (pos ? dmax : dmin) / davg[s] : 1.0);
+    if (s > 0 && okey(p) < okey(ph)) sel = s;
     ph = (s == 0) ? p : vmin(ph, p);
   }
   return ph;
@@ -93,7 +104,8 @@ static void check_cell(double w0, const double (&nb)[4], const double (&hot)[4],
   const double dmin = vmin(vmin(vmin(vmin(w0, nb[0]), nb[1]), nb[2]), nb[3]) - w0;
   double davg[4];
   for (int s = 0; s < 4; ++s) davg[s] = (w0 + hot[s]) - w0;
-  const double ref = phi_all<LIM>(dmax, dmin, davg);
+  int sel_ref;
+  const double ref = phi_all<LIM>(dmax, dmin, davg, sel_ref);
   const e2d::SlopePick k = e2d::pick_slopes<LIM>(dmax, dmin, davg);
   ++c.cases;
   if (!k.ok) {
@@ -101,9 +113,17 @@ static void check_cell(double w0, const double (&nb)[4], const double (&hot)[4],
     return;
   }
   double ph = psi_s<LIM>(k.ga ? k.na / k.da : 1.0);
+  int sel = k.fa;
+  if (LIM == 1 && bits(ph) == bits(1.0)) sel = 0;  // Barth-Jespersen's plateau: every face gives 1
   if (k.second) {
     ++c.second;
-    ph = vmin(ph, psi_s<LIM>(k.gb ? k.nb / k.db : 1.0));
+    const double pb = psi_s<LIM>(k.gb ? k.nb / k.db : 1.0);
+    if (okey(pb) < okey(ph) || (bits(pb) == bits(ph) && k.fb < k.fa)) sel = k.fb;
+    ph = vmin(ph, pb);
+  }
+  if (!std::isnan(ref) && sel != sel_ref) {
+    if (c.mismatches < 5) std::fprintf(stderr, "LIM %d face %d, all faces %d\n", LIM, sel, sel_ref);
+    ++c.mismatches;
   }
   if (bits(ph) != bits(ref) && !(std::isnan(ph) && std::isnan(ref))) {
     if (c.mismatches < 5)
@@ -189,6 +209,7 @@ static void make_cell(int kind, double& w0, double (&nb)[4], double (&hot)[4]) {
 template <int LIM>
 static Counts run(long n) {
   Counts c;
+  g_salt = (uint32_t)g_rng();
   for (long i = 0; i < n; ++i) {
     double w0, nb[4], hot[4];
     make_cell((int)(i % 7), w0, nb, hot);
