@@ -15,7 +15,9 @@ k_reconstruct, per cell (4 variables):
   limited face states       4 x (mul + add)                         =  8 / var
                                                           -> 82 x 4 = 328
   4 face states to primitive (2 div + 7)                              =  36
-  total 364 flops, 40 of them divisions
+  total 364 flops, 40 of them divisions (the reference's operation count; the
+  kernel evaluates the slope and psi only at the faces that decide phi, about 4 of
+  the 16 per cell, and gets the same phi)
 k_flux, per face (Roe):
   Roe average 18 (1 div, 3 sqrt), 3 sound speeds 9 (3 div, 3 sqrt), speeds 6,
   Harten 4, H/ua/1/a/r2a/h 13 (2 div), dW 4, Lp dW 8, |L| 4, Rc 22,
@@ -37,11 +39,11 @@ DIV_PER_FACE_ROE = 6
 SQRT_PER_FACE_ROE = 6
 
 # FP64 arithmetic instructions (DADD + DMUL + DFMA, per thread) per cell of each FP64
-# stage kernel on the same dominant path, counted by ncu
+# stage kernel, counted by ncu on the seeded benchmark state
 # (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum over one launch of
 # 2 097 152 cells).  With multiply-add contraction off, the DFMAs are those of the
 # division and square-root sequences.  The flux kernel's count is per cell (2 faces).
-FP64_INST_PER_CELL = {"reconstruct": 712, "flux": 444, "update": 67}
+FP64_INST_PER_CELL = {"reconstruct": 432, "flux": 407, "update": 63}
 # The FP64 pipe issues at most 2 thread-instructions per SM per clock on GB300 (the
 # peak that ncu's FP64 pipe utilisation is relative to).
 FP64_INST_PER_SM_CLOCK = 2
