@@ -36,6 +36,12 @@ E2D_API int e2d_bench_kernels(E2DHandle h, int32_t steps, double* ms, int64_t* l
    the next reconstruction.                                                      */
 E2D_API int e2d_bench_halo(E2DHandle h, int32_t reps, double* ms, int64_t* ntiles);
 
+/* Tile loads of the reconstruction kernel: enable != 0 (the default) stages interior
+   tiles (halo inside the block) with one TMA box load per tile where the block's
+   layout allows it, 0 stages every tile with plain loads.  Both compute the same
+   values.                                                                       */
+E2D_API int e2d_bench_set_tma(E2DHandle h, int32_t enable);
+
 /* Kernel-variant selection.  Every variant computes the same values; they differ in
    tile height, register/occupancy target and grid shape (one CTA per tile, or a
    persistent grid of resident CTAs striding over the tile table).

@@ -174,7 +174,7 @@ int forward_step(E2DSolver* h, T* stage_out, T* face_out) {
       in = Y;
       F = face_slot<T>(h, face_out + (size_t)s * face_set_size(h));
     }
-    CK(launch_reconstruct<T>(p.P, h->ts, h->kr, in, h->inst, F, nullptr, h->stream));
+    CK(launch_reconstruct<T>(p.P, h->ts, h->kr, in, h->inst, F, nullptr, h->stream, h->tma_for(in)));
     CK(launch_flux<T>(p.P, h->ts, h->kf, h->inst, F, nullptr, h->stream));
     CK(launch_update<T>(p.P, h->ts, h->ku, F, p.S, h->prog[s], h->inst, h->real, nullptr, h->stream));
   }
@@ -293,7 +293,8 @@ int residual_vjp_t(E2DSolver* h, double t, const double* lam_dev, double* out_de
   const T* lk = from_caller(h, lam_dev, io);
   T* out = sizeof(T) == 8 ? reinterpret_cast<T*>(out_dev) : io + n;
   CK(cudaMemsetAsync(out, 0, sizeof(T) * n, h->stream));
-  CK(launch_reconstruct<T>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, nullptr, h->stream));
+  CK(launch_reconstruct<T>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, nullptr, h->stream,
+                           h->tma_for(p.S.buf[0])));
   AdjProgramT<T> none{};
   if (int e = residual_vjp<T>(h, p.S.buf[0], p.F, lk, out, none)) return e;
   if (sizeof(T) == 4)

@@ -12,6 +12,10 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
+
+#include <mutex>
+
 #include "e2d_solver.cuh"
 #include "../../include/euler2d_bench.h"
 
@@ -100,6 +104,81 @@ static int build_program(E2DSolver* h, int S, const double* a) {
   return 0;
 }
 
+// ---- TMA tensor maps ----------------------------------------------------------------
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime (no link
+// against libcuda); null when the driver does not offer it, and then every tile takes
+// plain loads.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// Tensor maps of one state buffer for the reconstruction kernel's interior tiles, at
+// the three tile heights: per block a 3-D map (x = column, y = row, z = the 4 planes)
+// whose box is the tile, its one-cell halo and the alignment columns.  A block whose
+// row stride, plane stride or base is not a multiple of 16 bytes gets ok = 0.
+template <typename T>
+static int build_tma_t(E2DSolver* h, const T* base) {
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return 0;
+  const int nb = (int)h->hblocks.size();
+  const int heights[3] = {4, 8, 16};
+  E2DSolver::TmaEntry entry{base, {}};
+  std::vector<CUtensorMap> maps(nb);
+  std::vector<int> ok(nb);
+  for (int r = 0; r < 3; ++r) {
+    for (int b = 0; b < nb; ++b) {
+      const E2DBlock& B = h->hblocks[b];
+      const uint64_t row = (uint64_t)B.nx * sizeof(T), plane = (uint64_t)h->ncell * sizeof(T);
+      const T* addr = base + B.cell_offset;
+      bool good = row % 16 == 0 && plane % 16 == 0 && (reinterpret_cast<uintptr_t>(addr) % 16) == 0 &&
+                  B.nx > TX && B.ny > heights[r];
+      std::memset(&maps[b], 0, sizeof(CUtensorMap));
+      if (good) {
+        const cuuint64_t dims[3] = {(cuuint64_t)B.nx, (cuuint64_t)B.ny, 4};
+        const cuuint64_t strides[2] = {row, plane};
+        const cuuint32_t box[3] = {(cuuint32_t)TileCols<T>::TXW, (cuuint32_t)(heights[r] + 2), 4};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        const CUresult cr = enc(&maps[b], sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                                3, const_cast<T*>(addr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        good = cr == CUDA_SUCCESS;
+        if (!good) std::memset(&maps[b], 0, sizeof(CUtensorMap));
+      }
+      ok[b] = good ? 1 : 0;
+    }
+    CUtensorMap* dmaps = nullptr;
+    int* dok = nullptr;
+    if (int e = h->alloc(&dmaps, nb)) return e;
+    if (int e = h->alloc(&dok, nb)) return e;
+    CK(cudaMemcpy(dmaps, maps.data(), sizeof(CUtensorMap) * nb, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dok, ok.data(), sizeof(int) * nb, cudaMemcpyHostToDevice));
+    entry.set.by_rty[r] = TmaTiles{dmaps, dok, h->tma_timeouts};
+  }
+  h->tma_reg.push_back(entry);
+  return 0;
+}
+
+// Bounded TMA waits that ran out since the last check (the kernel drops those tiles).
+static int check_tma(E2DSolver* h) {
+  if (!h->tma_timeouts) return 0;
+  unsigned long long n = 0;
+  CK(cudaMemcpyAsync(&n, h->tma_timeouts, sizeof n, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (!n) return 0;
+  CK(cudaMemsetAsync(h->tma_timeouts, 0, sizeof n, h->stream));
+  return fail(E2D_ERR_CUDA, "%llu TMA tile load(s) did not arrive within the wait bound", n);
+}
+
 template <typename T>
 static int ensure_buffers_t(E2DSolver* h) {
   PathT<T>& p = path<T>(h);
@@ -107,6 +186,7 @@ static int ensure_buffers_t(E2DSolver* h) {
   for (int b = h->nbuf; b < need; ++b) {
     if (int e = h->alloc(&p.S.buf[b], 4 * (size_t)h->ncell)) return e;
     if (b > 0) CK(cudaMemsetAsync(p.S.buf[b], 0, sizeof(T) * 4 * h->ncell, h->stream));
+    if (int e = build_tma_t<T>(h, p.S.buf[b])) return e;
   }
   if (need > h->nbuf) h->nbuf = need;
   h->drop_graphs();
@@ -234,7 +314,7 @@ static int bench_kernels_t(E2DHandle h, int32_t steps, double* ms, int64_t* laun
     for (int s = 0; s < h->nstages; ++s) {
       const T* in = p.S.buf[h->stage_input[s]];
       CK(rec(1));
-      CK(launch_reconstruct<T>(p.P, h->ts, h->kr, in, h->inst, p.F, nullptr, h->stream));
+      CK(launch_reconstruct<T>(p.P, h->ts, h->kr, in, h->inst, p.F, nullptr, h->stream, h->tma_for(in)));
       CK(fin());
       CK(rec(2));
       CK(launch_flux<T>(p.P, h->ts, h->kf, h->inst, p.F, nullptr, h->stream));
@@ -322,7 +402,8 @@ static int bench_halo_t(E2DHandle h, int32_t reps, double* ms, int64_t* ntiles) 
     for (int r = -1; r < reps && ce == cudaSuccess; ++r) {  // r = -1 warms up
       if (r == 0) ce = cudaEventRecord(e0, h->stream);
       if (ce == cudaSuccess)
-        ce = launch_reconstruct<T>(p.P, ts, KernelChoice{0, false}, p.S.buf[0], h->inst, p.F, nullptr, h->stream);
+        ce = launch_reconstruct<T>(p.P, ts, KernelChoice{0, false}, p.S.buf[0], h->inst, p.F, nullptr, h->stream,
+                                   h->tma_for(p.S.buf[0]));
     }
     float t = 0.f;
     if (ce == cudaSuccess) ce = cudaEventRecord(e1, h->stream);
@@ -351,7 +432,8 @@ static int time_kernel(E2DHandle h, int which, int reps, float* ms) {
   CK(cudaEventCreate(&e1));
   for (int r = -1; r < reps; ++r) {  // r = -1 warms up
     if (r == 0) CK(cudaEventRecord(e0, h->stream));
-    if (which == 0) CK(launch_reconstruct<T>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, nullptr, h->stream));
+    if (which == 0)
+      CK(launch_reconstruct<T>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, nullptr, h->stream, h->tma_for(p.S.buf[0])));
     else if (which == 1) CK(launch_flux<T>(p.P, h->ts, h->kf, h->inst, p.F, nullptr, h->stream));
     else CK(launch_update<T>(p.P, h->ts, h->ku, p.F, p.S, none, h->inst, h->real, nullptr, h->stream));
   }
@@ -542,6 +624,9 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
     return bail(fail(E2D_ERR_CUDA, "instance copy: %s", cudaGetErrorString(ce)));
   if (int e = h->alloc(&h->real, 1)) return bail(e);
   k_reset_real<<<1, 1, 0, h->stream>>>(h->real);
+  if (int e = h->alloc(&h->tma_timeouts, 1)) return bail(e);
+  if ((ce = cudaMemsetAsync(h->tma_timeouts, 0, sizeof(unsigned long long), h->stream)) != cudaSuccess)
+    return bail(fail(E2D_ERR_CUDA, "counter init: %s", cudaGetErrorString(ce)));
 
   if (int e = E2D_DISPATCH(h, init_path)) return bail(e);
 
@@ -642,7 +727,7 @@ static int enqueue_stages(E2DHandle h, T* dudt_out, const DebugOutT<T>* dbg) {
   PathT<T>& p = path<T>(h);
   for (int s = 0; s < h->nstages; ++s) {
     const T* in = p.S.buf[h->stage_input[s]];
-    CK(launch_reconstruct<T>(p.P, h->ts, h->kr, in, h->inst, p.F, dbg, h->stream));
+    CK(launch_reconstruct<T>(p.P, h->ts, h->kr, in, h->inst, p.F, dbg, h->stream, h->tma_for(in)));
     CK(launch_flux<T>(p.P, h->ts, h->kf, h->inst, p.F, dbg, h->stream));
     CK(launch_update<T>(p.P, h->ts, h->ku, p.F, p.S, h->prog[s], h->inst, h->real, dudt_out,
                         h->stream));
@@ -750,7 +835,7 @@ int e2d_step(E2DHandle h, double dt, double t) {
     return e;
   CK(launch_end_step(h->inst, ninst, h->real, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  return 0;
+  return check_tma(h);
 }
 
 int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* d) {
@@ -767,7 +852,8 @@ int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* d) {
     PathT<float>& p = h->pf;
     if (!p.dudt_tmp)
       if (int e = h->alloc(&p.dudt_tmp, 4 * (size_t)h->ncell)) return e;
-    CK(launch_reconstruct<float>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, nullptr, h->stream));
+    CK(launch_reconstruct<float>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, nullptr, h->stream,
+                                 h->tma_for(p.S.buf[0])));
     CK(launch_flux<float>(p.P, h->ts, h->kf, h->inst, p.F, nullptr, h->stream));
     CK(launch_update<float>(p.P, h->ts, h->ku, p.F, p.S, none, h->inst, h->real, p.dudt_tmp,
                             h->stream));
@@ -782,7 +868,8 @@ int e2d_residual(E2DHandle h, double t, double* dudt_dev, const E2DDebug* d) {
       dbg.vflux = d->vflux; dbg.hflux = d->hflux;
       pdb = &dbg;
     }
-    CK(launch_reconstruct<double>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, pdb, h->stream));
+    CK(launch_reconstruct<double>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, pdb, h->stream,
+                                  h->tma_for(p.S.buf[0])));
     CK(launch_flux<double>(p.P, h->ts, h->kf, h->inst, p.F, pdb, h->stream));
     CK(launch_update<double>(p.P, h->ts, h->ku, p.F, p.S, none, h->inst, h->real, dudt_dev,
                              h->stream));
@@ -910,6 +997,7 @@ int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps, int
   }
   *t_inout = h->hinst[0].t;
   if (steps_done) *steps_done = h->hinst[0].steps;
+  if (int e = check_tma(h)) return e;
   RealizState r;
   CK(cudaMemcpyAsync(&r, h->real, sizeof r, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -928,6 +1016,13 @@ int e2d_run(E2DHandle h, double* t_inout, double t_final, int32_t max_steps, int
 int e2d_bench_kernels(E2DHandle h, int32_t steps, double* ms, int64_t* launches) {
   if (!h || !ms || steps < 1) return fail(E2D_ERR_INVALID, "bad argument");
   return E2D_DISPATCH(h, bench_kernels_t, steps, ms, launches);
+}
+
+int e2d_bench_set_tma(E2DHandle h, int32_t enable) {
+  if (!h) return fail(E2D_ERR_INVALID, "null handle");
+  h->tma_on = enable != 0;
+  h->drop_graphs();
+  return 0;
 }
 
 int e2d_bench_halo(E2DHandle h, int32_t reps, double* ms, int64_t* ntiles) {

@@ -2,6 +2,7 @@
 // kernels (e2d_stage.cuh, instantiated by e2d_fp64.cu and e2d_fp32.cu).  Internal.
 #pragma once
 #include <cstdint>
+#include <cuda.h>  // CUtensorMap
 #include <cuda_runtime.h>
 
 #include "../../include/euler2d.h"
@@ -124,6 +125,32 @@ struct TileSet {
   const int4* face;
   int nface;
 };
+// Tensor-memory-access (TMA) tile loads of one state buffer for the reconstruction
+// kernel's interior tiles (tiles whose one-cell halo lies inside their block), at one
+// tile height: one tensor map per block over its 4 planes (box: the tile and its halo,
+// widened on both sides so that its first column is 16-byte aligned).  ok[b] = 0 where
+// block b cannot use one (row stride, plane stride or base not 16-byte aligned); those
+// blocks, edge tiles and maps == nullptr take plain loads.  timeouts counts bounded
+// barrier waits that ran out (the kernel then drops that tile and reports through it).
+struct TmaTiles {
+  const CUtensorMap* maps;
+  const int* ok;
+  unsigned long long* timeouts;
+};
+// Columns of a staged tile: the box starts XO = 16 / sizeof(T) columns left of the tile
+// (its first column is then 16-byte aligned: j0 is a multiple of 32) and is TXW columns
+// wide; column j0 - 1 + lx of the block sits at shared-memory column C0 + lx.
+template <typename T>
+struct TileCols {
+  static constexpr int XO = 16 / (int)sizeof(T);
+  static constexpr int TXW = TX + 2 * XO;
+  static constexpr int C0 = XO - 1;
+};
+// the three tile heights (4, 8, 16) of one state buffer
+struct TmaSet {
+  TmaTiles by_rty[3];
+};
+
 // Kernel variant chosen by the autotuner (0 = default) and persistent-grid flag.
 struct KernelChoice {
   int variant;
@@ -136,7 +163,7 @@ constexpr int N_FLUX_VARIANTS = 3;   // min CTAs/SM: 4, 1, 6
 template <typename T>
 cudaError_t launch_reconstruct(const ParamsT<T>& P, const TileSet& ts, KernelChoice kc, const T* U,
                                const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>* dbg,
-                               cudaStream_t st);
+                               cudaStream_t st, const TmaSet* tma = nullptr);
 template <typename T>
 cudaError_t launch_flux(const ParamsT<T>& P, const TileSet& ts, KernelChoice kc, const InstanceState* inst,
                         FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st);

@@ -75,6 +75,21 @@ struct E2DSolver {
   std::vector<std::pair<int, cudaGraphExec_t>> graphs;
   int64_t ncell = 0, nvface = 0, nhface = 0;
   E2DAdjoint* adj = nullptr;
+  // TMA tensor maps of each state buffer (interior reconstruction tiles), the device
+  // counter of bounded TMA waits that ran out, and the switch between TMA and plain loads
+  struct TmaEntry {
+    const void* base;
+    e2d::TmaSet set;
+  };
+  std::vector<TmaEntry> tma_reg;
+  unsigned long long* tma_timeouts = nullptr;
+  bool tma_on = true;
+  const e2d::TmaSet* tma_for(const void* buf) const {
+    if (!tma_on) return nullptr;
+    for (const auto& e : tma_reg)
+      if (e.base == buf) return &e.set;
+    return nullptr;
+  }
 
   void drop_graphs() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);

@@ -146,14 +146,56 @@ __device__ __forceinline__ void outside_state(const ParamsT<T>& P, const E2DBloc
 }
 
 // --------------------------------------------------------------------------------------
+// TMA tile loads (cp.async.bulk.tensor) completed on a shared-memory mbarrier
+// --------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Bounded wait for the barrier phase `parity`; false when the bound ran out.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  const unsigned a = smem_u32(bar);
+  for (int it = 0; it < (1 << 22); ++it) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// One thread: expect `bytes` on the barrier and load the 3-D box at (x, y, z) of the
+// tensor map into shared memory.  The fence orders the CTA's earlier generic accesses
+// of that shared memory (the previous tile) before the asynchronous write.
+__device__ __forceinline__ void tma_load_box(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                             unsigned long long* bar, unsigned bytes) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"((unsigned long long)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// --------------------------------------------------------------------------------------
 // K1: reconstruction
 // --------------------------------------------------------------------------------------
+
 // One tile of cells: the body of k_reconstruct.  Returns early (uniformly per CTA)
 // for an inactive instance; the caller synchronises before sW is refilled.
 template <typename T, int LIM, int RECON, bool DBG, int RTY>
 __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4 tl, const T* __restrict__ U,
                                                  const InstanceState* __restrict__ inst, const FaceArraysT<T>& F,
-                                                 const DebugOutT<T>& dbg, T (&sW)[4][RTY + 2][TX + 2]) {
+                                                 const DebugOutT<T>& dbg,
+                                                 T (&sW)[4][RTY + 2][TileCols<T>::TXW], const TmaTiles& tma,
+                                                 unsigned long long* bar, unsigned& phase, bool& tma_live) {
+  constexpr int C0 = TileCols<T>::C0;
   const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
   const E2DBlock* B = P.blocks + tl.x;
   const InstanceState* I = inst + B->instance;
@@ -165,7 +207,33 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
   // boundary face.  The test is uniform over the CTA, so interior tiles branch past
   // the ghost and boundary code instead of issuing it under predicates.
   const bool edge = i0 == 0 || j0 == 0 || i0 + RTY >= ny || j0 + TX >= nx;
+  // Interior tiles of blocks with a tensor map arrive by one TMA box load (the tile, its
+  // halo and the alignment columns, 4 planes); the test is uniform over the CTA.
+  if (!edge && tma_live && tma.maps != nullptr && tma.ok[tl.x]) {
+    if (threadIdx.x == 0)
+      tma_load_box(&sW[0][0][0], &tma.maps[tl.x], j0 - TileCols<T>::XO, i0 - 1, 0, bar, (unsigned)sizeof(sW));
+    const bool arrived = __syncthreads_and(mbar_wait(bar, phase));
+    phase ^= 1u;
+    if (!arrived) {  // a wait ran out: report it, wait once more for the copy in flight, drop the tile
+      if (threadIdx.x == 0) atomicAdd(tma.timeouts, 1ULL);
+      mbar_wait(bar, phase ^ 1u);
+      tma_live = false;
+      return;
+    }
+    if (RECON == E2D_RECON_PRIMITIVE) {  // conversion in place, one thread per staged cell
+      for (int p = threadIdx.x; p < (RTY + 2) * (TX + 2); p += TX * RTY) {
+        const int ly = p / (TX + 2), lx = p - ly * (TX + 2);
+        T q[4] = {sW[0][ly][C0 + lx], sW[1][ly][C0 + lx], sW[2][ly][C0 + lx], sW[3][ly][C0 + lx]}, r[4];
+        to_recon<RECON>(q, G, r);
+        sW[0][ly][C0 + lx] = r[0];
+        sW[1][ly][C0 + lx] = r[1];
+        sW[2][ly][C0 + lx] = r[2];
+        sW[3][ly][C0 + lx] = r[3];
+      }
+    }
+  } else
   for (int p = threadIdx.x; p < (RTY + 2) * (TX + 2); p += TX * RTY) {
+
     const int ly = p / (TX + 2), lx = p - ly * (TX + 2);
     const int gi = i0 + ly - 1, gj = j0 + lx - 1;
     T q[4], r[4] = {T(0), T(0), T(0), T(0)};
@@ -183,10 +251,10 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
       else ok = false;
       if (ok) to_recon<RECON>(q, G, r);
     }
-    sW[0][ly][lx] = r[0];
-    sW[1][ly][lx] = r[1];
-    sW[2][ly][lx] = r[2];
-    sW[3][ly][lx] = r[3];
+    sW[0][ly][C0 + lx] = r[0];
+    sW[1][ly][C0 + lx] = r[1];
+    sW[2][ly][C0 + lx] = r[2];
+    sW[3][ly][C0 + lx] = r[3];
   }
   __syncthreads();
 
@@ -211,11 +279,11 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
   T face[4][4];  // [side][var] limited face states, reconstruction variables
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
-    const T w0 = sW[v][ty + 1][tx + 1];
-    const T we = sW[v][ty + 1][tx];
-    const T ea = sW[v][ty + 1][tx + 2];
-    const T so = sW[v][ty][tx + 1];
-    const T no = sW[v][ty + 2][tx + 1];
+    const T w0 = sW[v][ty + 1][C0 + tx + 1];
+    const T we = sW[v][ty + 1][C0 + tx];
+    const T ea = sW[v][ty + 1][C0 + tx + 2];
+    const T so = sW[v][ty][C0 + tx + 1];
+    const T no = sW[v][ty + 2][C0 + tx + 1];
     // interface averages (quad_block.py:181-218) and Green-Gauss (greengauss.py:137-155)
     const T ie = half(w0 + ea), iw = half(we + w0);
     const T in = half(w0 + no), is = half(so + w0);
@@ -311,7 +379,7 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
   // outside states of block-boundary faces
   if (!edge) return;
   if (j == 0) {
-    const T gr[4] = {sW[0][ty + 1][tx], sW[1][ty + 1][tx], sW[2][ty + 1][tx], sW[3][ty + 1][tx]};
+    const T gr[4] = {sW[0][ty + 1][C0 + tx], sW[1][ty + 1][C0 + tx], sW[2][ty + 1][C0 + tx], sW[3][ty + 1][C0 + tx]};
     T o[4], w[4];
     outside_state(P, B, E2D_W, i, t, gr, face[E2D_W], o);
     if (!cart) rotate(o, P.geo.vface[E2D_F_COS][fW], P.geo.vface[E2D_F_SIN][fW]);
@@ -319,7 +387,8 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
     store4(F.vL, P.nvface, fW, w);
   }
   if (j == nx - 1) {
-    const T gr[4] = {sW[0][ty + 1][tx + 2], sW[1][ty + 1][tx + 2], sW[2][ty + 1][tx + 2], sW[3][ty + 1][tx + 2]};
+    const T gr[4] = {sW[0][ty + 1][C0 + tx + 2], sW[1][ty + 1][C0 + tx + 2], sW[2][ty + 1][C0 + tx + 2],
+                      sW[3][ty + 1][C0 + tx + 2]};
     T o[4], w[4];
     outside_state(P, B, E2D_E, i, t, gr, face[E2D_E], o);
     if (!cart) rotate(o, P.geo.vface[E2D_F_COS][fE], P.geo.vface[E2D_F_SIN][fE]);
@@ -327,7 +396,7 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
     store4(F.vR, P.nvface, fE, w);
   }
   if (i == 0) {
-    const T gr[4] = {sW[0][ty][tx + 1], sW[1][ty][tx + 1], sW[2][ty][tx + 1], sW[3][ty][tx + 1]};
+    const T gr[4] = {sW[0][ty][C0 + tx + 1], sW[1][ty][C0 + tx + 1], sW[2][ty][C0 + tx + 1], sW[3][ty][C0 + tx + 1]};
     T o[4], w[4];
     outside_state(P, B, E2D_S, j, t, gr, face[E2D_S], o);
     if (cart) rotate90(o);
@@ -336,7 +405,8 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
     store4(F.hL, P.nhface, fS, w);
   }
   if (i == ny - 1) {
-    const T gr[4] = {sW[0][ty + 2][tx + 1], sW[1][ty + 2][tx + 1], sW[2][ty + 2][tx + 1], sW[3][ty + 2][tx + 1]};
+    const T gr[4] = {sW[0][ty + 2][C0 + tx + 1], sW[1][ty + 2][C0 + tx + 1], sW[2][ty + 2][C0 + tx + 1],
+                      sW[3][ty + 2][C0 + tx + 1]};
     T o[4], w[4];
     outside_state(P, B, E2D_N, j, t, gr, face[E2D_N], o);
     if (cart) rotate90(o);
@@ -353,13 +423,20 @@ template <typename T, int LIM, int RECON, bool DBG, int RTY, int MINB, bool PERS
 __global__ void __launch_bounds__(TX * RTY, MINB) k_reconstruct(ParamsT<T> P, const int4* __restrict__ tiles,
                                                                 int ntiles, const T* __restrict__ U,
                                                                 const InstanceState* __restrict__ inst,
-                                                                FaceArraysT<T> F, DebugOutT<T> dbg) {
-  __shared__ T sW[4][RTY + 2][TX + 2];
+                                                                FaceArraysT<T> F, DebugOutT<T> dbg, TmaTiles tma) {
+  __shared__ __align__(128) T sW[4][RTY + 2][TileCols<T>::TXW];
+  __shared__ __align__(8) unsigned long long bar;
+  unsigned phase = 0;
+  bool tma_live = tma.maps != nullptr;
+  if (tma_live) {
+    if (threadIdx.x == 0) mbar_init(&bar);
+    __syncthreads();
+  }
   if constexpr (!PERSIST) {
-    reconstruct_tile<T, LIM, RECON, DBG, RTY>(P, tiles[blockIdx.x], U, inst, F, dbg, sW);
+    reconstruct_tile<T, LIM, RECON, DBG, RTY>(P, tiles[blockIdx.x], U, inst, F, dbg, sW, tma, &bar, phase, tma_live);
   } else {
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-      reconstruct_tile<T, LIM, RECON, DBG, RTY>(P, tiles[tile], U, inst, F, dbg, sW);
+      reconstruct_tile<T, LIM, RECON, DBG, RTY>(P, tiles[tile], U, inst, F, dbg, sW, tma, &bar, phase, tma_live);
       __syncthreads();  // the next tile refills sW
     }
   }
@@ -783,12 +860,14 @@ static int persistent_grid(K kern, int threads, int n) {
 
 template <typename T, int LIM, int RECON, bool DBG, int RTY, int MINB>
 static cudaError_t recon_launch(const ParamsT<T>& P, const int4* tiles, int n, bool persistent, const T* U,
-                                const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>& dbg, cudaStream_t st) {
+                                const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>& dbg, cudaStream_t st,
+                                const TmaSet* tset) {
+  const TmaTiles tma = tset ? tset->by_rty[RTY == 4 ? 0 : (RTY == 8 ? 1 : 2)] : TmaTiles{nullptr, nullptr, nullptr};
   if (persistent) {
     auto kern = k_reconstruct<T, LIM, RECON, DBG, RTY, MINB, true>;
-    kern<<<persistent_grid(kern, TX * RTY, n), TX * RTY, 0, st>>>(P, tiles, n, U, inst, F, dbg);
+    kern<<<persistent_grid(kern, TX * RTY, n), TX * RTY, 0, st>>>(P, tiles, n, U, inst, F, dbg, tma);
   } else {
-    k_reconstruct<T, LIM, RECON, DBG, RTY, MINB, false><<<n, TX * RTY, 0, st>>>(P, tiles, n, U, inst, F, dbg);
+    k_reconstruct<T, LIM, RECON, DBG, RTY, MINB, false><<<n, TX * RTY, 0, st>>>(P, tiles, n, U, inst, F, dbg, tma);
   }
   return cudaGetLastError();
 }
@@ -796,31 +875,31 @@ static cudaError_t recon_launch(const ParamsT<T>& P, const int4* tiles, int n, b
 template <typename T, int LIM, int RECON>
 static cudaError_t recon_variant(const ParamsT<T>& P, const int4* const* tiles_by_rty, const int* n_by_rty,
                                  int variant, bool persistent, const T* U, const InstanceState* inst, FaceArraysT<T> F,
-                                 const DebugOutT<T>* dbg, cudaStream_t st) {
+                                 const DebugOutT<T>* dbg, cudaStream_t st, const TmaSet* tma) {
   if (dbg)  // the per-operator outputs are built for the default variant only
-    return recon_launch<T, LIM, RECON, true, 8, 1>(P, tiles_by_rty[1], n_by_rty[1], false, U, inst, F, *dbg, st);
+    return recon_launch<T, LIM, RECON, true, 8, 1>(P, tiles_by_rty[1], n_by_rty[1], false, U, inst, F, *dbg, st, tma);
   const DebugOutT<T> none{};
   switch (variant) {
-    case 1: return recon_launch<T, LIM, RECON, false, 8, 1>(P, tiles_by_rty[1], n_by_rty[1], persistent, U, inst, F, none, st);
-    case 2: return recon_launch<T, LIM, RECON, false, 4, 2>(P, tiles_by_rty[0], n_by_rty[0], persistent, U, inst, F, none, st);
-    case 3: return recon_launch<T, LIM, RECON, false, 4, 4>(P, tiles_by_rty[0], n_by_rty[0], persistent, U, inst, F, none, st);
-    case 4: return recon_launch<T, LIM, RECON, false, 16, 1>(P, tiles_by_rty[2], n_by_rty[2], persistent, U, inst, F, none, st);
+    case 1: return recon_launch<T, LIM, RECON, false, 8, 1>(P, tiles_by_rty[1], n_by_rty[1], persistent, U, inst, F, none, st, tma);
+    case 2: return recon_launch<T, LIM, RECON, false, 4, 2>(P, tiles_by_rty[0], n_by_rty[0], persistent, U, inst, F, none, st, tma);
+    case 3: return recon_launch<T, LIM, RECON, false, 4, 4>(P, tiles_by_rty[0], n_by_rty[0], persistent, U, inst, F, none, st, tma);
+    case 4: return recon_launch<T, LIM, RECON, false, 16, 1>(P, tiles_by_rty[2], n_by_rty[2], persistent, U, inst, F, none, st, tma);
     case 5:  // FP32 only (64 registers, 8 CTAs of 128 threads per SM); FP64 would spill
       if constexpr (sizeof(T) == 4)
-        return recon_launch<T, LIM, RECON, false, 4, 8>(P, tiles_by_rty[0], n_by_rty[0], persistent, U, inst, F, none, st);
+        return recon_launch<T, LIM, RECON, false, 4, 8>(P, tiles_by_rty[0], n_by_rty[0], persistent, U, inst, F, none, st, tma);
       else
-        return recon_launch<T, LIM, RECON, false, 8, 2>(P, tiles_by_rty[1], n_by_rty[1], persistent, U, inst, F, none, st);
-    default: return recon_launch<T, LIM, RECON, false, 8, 2>(P, tiles_by_rty[1], n_by_rty[1], persistent, U, inst, F, none, st);
+        return recon_launch<T, LIM, RECON, false, 8, 2>(P, tiles_by_rty[1], n_by_rty[1], persistent, U, inst, F, none, st, tma);
+    default: return recon_launch<T, LIM, RECON, false, 8, 2>(P, tiles_by_rty[1], n_by_rty[1], persistent, U, inst, F, none, st, tma);
   }
 }
 
 template <typename T, int LIM>
 static cudaError_t recon_lim(const ParamsT<T>& P, const int4* const* tiles, const int* n, int variant, bool persistent,
                              const T* U, const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>* dbg,
-                             cudaStream_t st) {
+                             cudaStream_t st, const TmaSet* tma) {
   if (P.recon == E2D_RECON_PRIMITIVE)
-    return recon_variant<T, LIM, E2D_RECON_PRIMITIVE>(P, tiles, n, variant, persistent, U, inst, F, dbg, st);
-  return recon_variant<T, LIM, E2D_RECON_CONSERVATIVE>(P, tiles, n, variant, persistent, U, inst, F, dbg, st);
+    return recon_variant<T, LIM, E2D_RECON_PRIMITIVE>(P, tiles, n, variant, persistent, U, inst, F, dbg, st, tma);
+  return recon_variant<T, LIM, E2D_RECON_CONSERVATIVE>(P, tiles, n, variant, persistent, U, inst, F, dbg, st, tma);
 }
 
 template <typename T, int LIM, int RECON>
@@ -842,7 +921,8 @@ static cudaError_t recon_qp_lim(const ParamsT<T>& P, const TileSet& ts, const T*
 
 template <typename T>
 cudaError_t launch_reconstruct(const ParamsT<T>& P, const TileSet& ts, KernelChoice kc, const T* U,
-                               const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st) {
+                               const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>* dbg, cudaStream_t st,
+                               const TmaSet* tma) {
   const int4* tiles[3] = {ts.cell[0], ts.cell[1], ts.cell[2]};
   if (ts.ncell[1] <= 0) return cudaSuccess;
   if (P.nqp > 1) {  // several face quadrature points: one kernel form, no per-operator outputs
@@ -855,13 +935,13 @@ cudaError_t launch_reconstruct(const ParamsT<T>& P, const TileSet& ts, KernelCho
   }
   switch (P.limiter) {
     case E2D_LIM_BARTH_JESPERSEN:
-      return recon_lim<T, E2D_LIM_BARTH_JESPERSEN>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st);
+      return recon_lim<T, E2D_LIM_BARTH_JESPERSEN>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st, tma);
     case E2D_LIM_VAN_ALBADA:
-      return recon_lim<T, E2D_LIM_VAN_ALBADA>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st);
+      return recon_lim<T, E2D_LIM_VAN_ALBADA>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st, tma);
     case E2D_LIM_VAN_LEER:
-      return recon_lim<T, E2D_LIM_VAN_LEER>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st);
+      return recon_lim<T, E2D_LIM_VAN_LEER>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st, tma);
     default:
-      return recon_lim<T, E2D_LIM_VENKATAKRISHNAN>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st);
+      return recon_lim<T, E2D_LIM_VENKATAKRISHNAN>(P, tiles, ts.ncell, kc.variant, kc.persistent, U, inst, F, dbg, st, tma);
   }
 }
 
@@ -1032,7 +1112,7 @@ cudaError_t launch_ghost_layer(const ParamsT<T>& P, const T* U, double t, const 
 #define E2D_INSTANTIATE_STAGE_LAUNCHERS(T)                                                                       \
   template cudaError_t launch_reconstruct<T>(const ParamsT<T>&, const TileSet&, KernelChoice, const T*,          \
                                              const InstanceState*, FaceArraysT<T>, const DebugOutT<T>*,          \
-                                             cudaStream_t);                                                      \
+                                             cudaStream_t, const TmaSet*);                                       \
   template cudaError_t launch_flux<T>(const ParamsT<T>&, const TileSet&, KernelChoice, const InstanceState*,     \
                                       FaceArraysT<T>, const DebugOutT<T>*, cudaStream_t);                        \
   template cudaError_t launch_update<T>(const ParamsT<T>&, const TileSet&, KernelChoice, FaceArraysT<T>,         \
@@ -1048,7 +1128,7 @@ cudaError_t launch_ghost_layer(const ParamsT<T>& P, const T* U, double t, const 
 #define E2D_EXTERN_STAGE_LAUNCHERS(T)                                                                           \
   extern template cudaError_t launch_reconstruct<T>(const ParamsT<T>&, const TileSet&, KernelChoice, const T*,   \
                                                     const InstanceState*, FaceArraysT<T>, const DebugOutT<T>*,   \
-                                                    cudaStream_t);                                               \
+                                                    cudaStream_t, const TmaSet*);                                \
   extern template cudaError_t launch_flux<T>(const ParamsT<T>&, const TileSet&, KernelChoice, const InstanceState*, \
                                              FaceArraysT<T>, const DebugOutT<T>*, cudaStream_t);                 \
   extern template cudaError_t launch_update<T>(const ParamsT<T>&, const TileSet&, KernelChoice, FaceArraysT<T>,  \
