@@ -774,6 +774,9 @@ def main():
         "roofline": {
             "bound": "fp64", "kernel": names[dom], "achieved": achieved, "peak": peak_fma.value,
             "unit": "TFLOP/s", "frac": achieved / peak_fma.value if peak_fma.value else None,
+            # the parity build may not contract a*b+c, so every algorithmic flop takes at
+            # least one FP64 instruction: against the unfused (DADD) rate
+            "frac_unfused": achieved / peak_add.value if peak_add.value else None,
             "traffic": traffic,
             "peak_source": "measured in-run: DFMA chains over all SMs (2 flops per DFMA); DADD rate "
                            f"{peak_add.value:.3f} TFLOP/s",
