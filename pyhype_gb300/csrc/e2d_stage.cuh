@@ -7,19 +7,21 @@
 // table maps CTAs to (block, tile) pairs):
 //
 //   k_reconstruct  per cell: reconstruction-type state of the cell and its four
-//                  neighbours (ghost cells formed on the fly at block edges), interface
-//                  averages, Green-Gauss gradient, limiter, limited face states; each
-//                  face state is rotated into its face frame, converted to primitive
-//                  and written to the face-indexed L/R arrays, block-boundary cells
-//                  also write the outside state of their boundary face.
+//                  neighbours (an interior tile arrives by one TMA box load, edge tiles
+//                  by plain loads with ghost cells formed on the fly), interface
+//                  averages, Green-Gauss gradient, limiter (in FP64 psi only at the
+//                  faces that decide phi, e2d_slope_pick.cuh), limited face states;
+//                  each face state is rotated into its face frame, converted to
+//                  primitive and written to the face-indexed L/R arrays, block-boundary
+//                  cells also write the outside state of their boundary face.
 //   k_flux         per face, exactly once: Riemann flux of (L, R), rotated back,
 //                  times 2*L (one-point rule, weight 2).
 //   k_update       per cell: dUdt = 0.5*(((I_W - I_E) + I_S) - I_N)/A and the RK stage
 //                  program (every partial Butcher sum this stage contributes to);
 //                  on the last stage also the positivity check.
 //
-// GB300's FP64 pipe is the binding resource of this scheme in FP64 (about 1000 FP64
-// pipe operations per cell-stage against ~250 bytes of HBM traffic), so the split
+// GB300's FP64 pipe is the binding resource of this scheme in FP64 (about 900 FP64
+// instructions per cell-stage against ~250 bytes of HBM traffic), so the split
 // avoids every recomputation a fused halo-tile kernel would do (gradients and
 // limiter of the halo ring, fluxes of tile-edge faces); the extra face-array traffic
 // costs HBM bandwidth that is otherwise idle.
