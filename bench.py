@@ -301,6 +301,28 @@ def ensemble_section(stream, full: bool = False, autotune: bool = True):
     out["halted_unrealizable"] = {"fp32": sorted(halted["fp32"]), "fp64": sorted(halted["fp64"]),
                                   "note": "the reference scheme reaches NaN on these instances (checked in the CPU "
                                           "oracle for instance 265); they are excluded from the L1 statistics"}
+    if full:
+        # the FP64 scheme's own sensitivity to round-off: the same run from an initial
+        # state whose densities and energies are one ulp larger
+        from pyhype_gb300.batch import ensemble_state
+
+        E64p = EnsembleSolver(inst, precision=0, problem=P)
+        E64p.device.set_stream(stream.cuda_stream)
+        U = ensemble_state(P, inst)
+        U[0] = np.nextafter(U[0], np.inf)
+        U[3] = np.nextafter(U[3], np.inf)
+        E64p.device.set_state(U)
+        bad_p = set(E64p.run(w)) | set(E64p.run(k32))
+        c = E64p.states()
+        l1p = [float(np.sum(np.abs(y[:, :, 0] - x[:, :, 0])) / np.sum(np.abs(x[:, :, 0])))
+               for k, (x, y) in enumerate(zip(a, c)) if k not in bad | bad_p]
+        out["fp64_one_ulp_initial_change_l1_density"] = {
+            "after_steps": w + k32, "mean": float(np.mean(l1p)), "max": float(np.max(l1p)),
+            "median": float(np.median(l1p)),
+            "note": "FP64 run from densities and energies one ulp larger, against the FP64 run: the scheme's "
+                    "own round-off sensitivity (the reference limiter switches psi between 0.75 and ~1 on "
+                    "round-off-sized face differences)"}
+        E64p.device.close()
     # FP64 instances one after another (each its own device problem)
     nseq = 512 if full else 16
     seq_ms, seq_cells = 0.0, 0
