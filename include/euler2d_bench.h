@@ -57,6 +57,13 @@ E2D_API int e2d_set_kernel_choice(E2DHandle h, int32_t kernel, int32_t variant, 
    variant, persistent}.  Graphs captured before are dropped.                    */
 E2D_API int e2d_autotune(E2DHandle h, int32_t reps, int32_t* chosen);
 
+/* The bounded barrier wait of the reconstruction kernel's TMA tile staging, on its
+   own: one warp waits on a shared-memory barrier phase for at most `limit` polls.
+   complete != 0 completes the phase (*arrived = 1); complete == 0 announces a
+   transfer that never comes, and the wait must run out and return (*arrived = 0)
+   instead of spinning, leaving the context usable.                              */
+E2D_API int e2d_check_wait_bound(int32_t complete, int32_t limit, int32_t* arrived);
+
 /* The FP32 form's division routine applied elementwise: q[i] = a[i] / b[i] for n
    values in caller device buffers, on the default stream (synchronised).  For
    testing the routine against IEEE division.                                   */

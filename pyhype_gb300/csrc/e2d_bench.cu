@@ -5,6 +5,7 @@
 
 #include "../../include/euler2d_bench.h"
 #include "e2d_device.cuh"
+#include "e2d_tma.cuh"
 
 namespace {
 
@@ -35,7 +36,43 @@ __global__ void k_div32(const float* __restrict__ a, const float* __restrict__ b
     q[i] = e2d::div32(a[i], b[i]);
 }
 
+// One warp waits on a shared-memory barrier phase with the reconstruction kernel's
+// bounded wait.  complete != 0: thread 0 arrives (the phase completes); else thread 0
+// announces 16 bytes of transfer that no copy delivers, so the phase cannot complete
+// and the wait runs out after `limit` polls.  out[0] = 1 if the phase was seen
+// complete, out[1] = 1 once the kernel got past the wait.
+__global__ void k_wait_bound(int complete, int limit, int* out) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) e2d::mbar_init(&bar);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned a = e2d::smem_u32(&bar);
+    if (complete) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+    else asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], 16;" ::"r"(a) : "memory");
+  }
+  const bool arrived = __syncthreads_and(e2d::mbar_wait(&bar, 0u, limit));
+  if (threadIdx.x == 0) {
+    out[0] = arrived ? 1 : 0;
+    out[1] = 1;
+  }
+}
+
 }  // namespace
+
+extern "C" int e2d_check_wait_bound(int32_t complete, int32_t limit, int32_t* arrived) {
+  if (!arrived || limit < 1) return E2D_ERR_INVALID;
+  int* d = nullptr;
+  if (cudaMalloc(&d, 2 * sizeof(int)) != cudaSuccess) return E2D_ERR_NOMEM;
+  int h[2] = {0, 0};
+  cudaMemset(d, 0, 2 * sizeof(int));
+  k_wait_bound<<<1, 32>>>(complete, limit, d);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess || h[1] != 1) return E2D_ERR_CUDA;
+  *arrived = h[0];
+  return 0;
+}
 
 extern "C" int e2d_check_div32(const float* a, const float* b, float* q, int64_t n) {
   if (!a || !b || !q || n < 0) return E2D_ERR_INVALID;

@@ -31,6 +31,7 @@
 #include "e2d_device.cuh"
 #include "e2d_kernels.cuh"
 #include "e2d_slope_pick.cuh"
+#include "e2d_tma.cuh"
 
 namespace e2d {
 
@@ -145,44 +146,6 @@ __device__ __forceinline__ void outside_state(const ParamsT<T>& P, const E2DBloc
       reflect(o, c, s);
     }
   }
-}
-
-// --------------------------------------------------------------------------------------
-// TMA tile loads (cp.async.bulk.tensor) completed on a shared-memory mbarrier
-// --------------------------------------------------------------------------------------
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-// Bounded wait for the barrier phase `parity`; false when the bound ran out.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
-  const unsigned a = smem_u32(bar);
-  for (int it = 0; it < (1 << 22); ++it) {
-    unsigned done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
-// One thread: expect `bytes` on the barrier and load the 3-D box at (x, y, z) of the
-// tensor map into shared memory.  The fence orders the CTA's earlier generic accesses
-// of that shared memory (the previous tile) before the asynchronous write.
-__device__ __forceinline__ void tma_load_box(void* dst, const CUtensorMap* map, int x, int y, int z,
-                                             unsigned long long* bar, unsigned bytes) {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-      ::"r"(smem_u32(dst)), "l"((unsigned long long)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-      : "memory");
 }
 
 // --------------------------------------------------------------------------------------
