@@ -62,9 +62,9 @@ struct SlopePick {
   bool ga, gb;    // false: that slope is exactly 1 (davg == 0), not na/da
   bool second;    // phi = min(psi(na/da), psi(nb/db)); else phi = psi(na/da)
   bool ok;        // false: evaluate all four faces
-  int fa, fb;     // their faces (0..3 = E, W, N, S): the first face whose psi equals
-                  // phi is fa, or with `second` the one of fa, fb whose psi is smaller
-                  // (the lower index when both are equal)
+  int fa, fb;     // their indices in den: the first candidate whose psi equals phi is
+                  // fa, or with `second` the one of fa, fb whose psi is smaller (the
+                  // lower index when both are equal)
 };
 
 namespace slope_pick_detail {
@@ -161,10 +161,12 @@ E2D_HD bool same_slope(uint64_t n0, uint64_t d0, uint64_t n1, uint64_t d1) {
 
 // LIM: E2D_LIM_* of euler2d.h (0 Venkatakrishnan, 1 Barth-Jespersen, 2 van Albada,
 // 3 van Leer).  dmax >= 0, dmin <= 0: the cell's stencil extremes minus its value;
-// den: davg of the E, W, N, S faces.  A face's slope is dmax/davg (davg > 0),
-// dmin/davg (davg < 0) or exactly 1 (davg == 0).
-template <int LIM>
-E2D_HD SlopePick pick_slopes(double dmax, double dmin, const double (&den)[4]) {
+// den: davg of the N candidate points in the limiter's order (the E, W, N, S faces;
+// with several face quadrature points, every point of E, then of W, N, S).  A slope
+// is dmax/davg (davg > 0), dmin/davg (davg < 0) or exactly 1 (davg == 0).  fa, fb
+// index den.
+template <int LIM, int N = 4>
+E2D_HD SlopePick pick_slopes(double dmax, double dmin, const double (&den)[N]) {
   using namespace slope_pick_detail;
   const uint64_t amax = abs_bits(dmax), amin = abs_bits(dmin);
   // per face: |numerator| and |denominator| bits (1, 1 for davg == 0) and the estimate
@@ -175,10 +177,10 @@ E2D_HD SlopePick pick_slopes(double dmax, double dmin, const double (&den)[4]) {
     n = gen ? (pos ? amax : amin) : kOneBits;
     d = gen ? b : kOneBits;
   };
-  float se[4];
+  float se[N];
   bool ok = true, zpos = false, zneg = false;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < N; ++k) {
     uint64_t n, d;
     operands(k, n, d);
     bool okk;
@@ -196,7 +198,7 @@ E2D_HD SlopePick pick_slopes(double dmax, double dmin, const double (&den)[4]) {
   float smin = se[0], smax = se[0];
   int ia = 0, ib = 0;
 #pragma unroll
-  for (int k = 1; k < 4; ++k) {
+  for (int k = 1; k < N; ++k) {
     if (se[k] < smin) { smin = se[k]; ia = k; }
     if (se[k] > smax) { smax = se[k]; ib = k; }
   }
@@ -217,7 +219,7 @@ E2D_HD SlopePick pick_slopes(double dmax, double dmin, const double (&den)[4]) {
   if (LIM == 3 && smin > kFallingLimit) ok = false;
   uint64_t nA = 0, dA = 0, nB = 0, dB = 0;  // operands of the two ends
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {  // unrolled selects: no indexed access to den
+  for (int k = 0; k < N; ++k) {  // unrolled selects: no indexed access to den
     uint64_t n, d;
     operands(k, n, d);
     if (k == ia) { nA = n; dA = d; }
@@ -225,7 +227,7 @@ E2D_HD SlopePick pick_slopes(double dmax, double dmin, const double (&den)[4]) {
   }
   const float lo = smin * (1.0f + kTau), hi = smax * (1.0f - kTau);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < N; ++k) {
     uint64_t n, d;
     operands(k, n, d);
     if (use_a && k != ia && se[k] <= lo && !same_slope(n, d, nA, dA)) ok = false;
@@ -236,7 +238,7 @@ E2D_HD SlopePick pick_slopes(double dmax, double dmin, const double (&den)[4]) {
   const int i1 = use_a ? ia : ib;
   p.da = den[0]; p.db = den[0];
 #pragma unroll
-  for (int k = 1; k < 4; ++k) {
+  for (int k = 1; k < N; ++k) {
     if (k == i1) p.da = den[k];
     if (k == ib) p.db = den[k];
   }

@@ -482,23 +482,38 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_qp(ParamsT<T> P, const 
     const T dmax = vmax(vmax(vmax(vmax(w0, we), ea), so), no) - w0;
     const T dmin = vmin(vmin(vmin(vmin(w0, we), ea), so), no) - w0;
     T ph = T(0);
+    T dv[4 * NQP];  // davg of every point, E points first, then W, N, S
 #pragma unroll
     for (int s = 0; s < 4; ++s)
 #pragma unroll
       for (int q = 0; q < NQP; ++q) {
         const T hot = gx * P.geo.qp[q][s][c] + gy * P.geo.qp[q][4 + s][c];
-        T davg;
         if constexpr (sizeof(T) == 4) {
           const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
-          davg = (fabs(hot) < half_ulp64) ? T(0) : hot;
+          dv[s * NQP + q] = (fabs(hot) < half_ulp64) ? T(0) : hot;
         } else {
-          davg = (w0 + hot) - w0;
+          dv[s * NQP + q] = (w0 + hot) - w0;
         }
+      }
+    bool done = false;
+    if constexpr (sizeof(T) == 8) {  // psi only at the points that decide phi, as k_reconstruct does
+      const SlopePick k = pick_slopes<LIM, 4 * NQP>(dmax, dmin, dv);
+      if (k.ok) {
+        ph = psi_s<LIM>(k.ga ? qdiv(k.na, k.da) : T(1));
+        if (k.second) ph = vmin(ph, psi_s<LIM>(k.gb ? qdiv(k.nb, k.db) : T(1)));
+        done = true;
+      }
+    }
+    if (!done) {
+#pragma unroll
+      for (int m = 0; m < 4 * NQP; ++m) {
+        const T davg = dv[m];
         const bool pos = is_pos(davg), neg = is_neg(davg);
         const T sl = (pos || neg) ? qdiv(pos ? dmax : dmin, davg) : T(1);
         const T p = psi_s<LIM>(sl);
-        ph = (s == 0 && q == 0) ? p : vmin(ph, p);
+        ph = (m == 0) ? p : vmin(ph, p);
       }
+    }
     phs[v] = is_neg(ph) ? T(0) : ph;
     gxs[v] = gx;
     gys[v] = gy;

@@ -6,7 +6,8 @@
 // wider than the device instruction's stated 1 ulp.
 //
 // Build: g++ -O2 -std=c++17 -ffp-contract=off slope_pick_check.cpp
-// Run:   ./a.out <cases per limiter> <seed>     prints one line per limiter:
+// Run:   ./a.out <cases per limiter> <seed>     prints two lines per limiter, four
+//        candidates ("<lim> cases=...") and 8 or 12 ("<lim>+ cases=..."):
 //        "<lim> cases=<n> mismatches=<m> fallback=<f> second=<s>"
 #include <cmath>
 #include <cstdint>
@@ -81,11 +82,11 @@ static double psi_s(double s) {
 
 // phi over all four faces, and the first face whose psi is phi (the selection the
 // adjoint differentiates)
-template <int LIM>
-static double phi_all(double dmax, double dmin, const double (&davg)[4], int& sel) {
+template <int LIM, int N>
+static double phi_all(double dmax, double dmin, const double (&davg)[N], int& sel) {
   double ph = 0.0;
   sel = 0;
-  for (int s = 0; s < 4; ++s) {
+  for (int s = 0; s < N; ++s) {
     const bool pos = is_pos(davg[s]), neg = is_neg(davg[s]);
     const double p = psi_s<LIM>((pos || neg) ? (pos ? dmax : dmin) / davg[s] : 1.0);
     if (s > 0 && okey(p) < okey(ph)) sel = s;
@@ -98,15 +99,15 @@ struct Counts {
   long cases = 0, mismatches = 0, fallback = 0, second = 0;
 };
 
-template <int LIM>
-static void check_cell(double w0, const double (&nb)[4], const double (&hot)[4], Counts& c) {
+template <int LIM, int N>
+static void check_cell(double w0, const double (&nb)[4], const double (&hot)[N], Counts& c) {
   const double dmax = vmax(vmax(vmax(vmax(w0, nb[0]), nb[1]), nb[2]), nb[3]) - w0;
   const double dmin = vmin(vmin(vmin(vmin(w0, nb[0]), nb[1]), nb[2]), nb[3]) - w0;
-  double davg[4];
-  for (int s = 0; s < 4; ++s) davg[s] = (w0 + hot[s]) - w0;
+  double davg[N];
+  for (int s = 0; s < N; ++s) davg[s] = (w0 + hot[s]) - w0;
   int sel_ref;
-  const double ref = phi_all<LIM>(dmax, dmin, davg, sel_ref);
-  const e2d::SlopePick k = e2d::pick_slopes<LIM>(dmax, dmin, davg);
+  const double ref = phi_all<LIM, N>(dmax, dmin, davg, sel_ref);
+  const e2d::SlopePick k = e2d::pick_slopes<LIM, N>(dmax, dmin, davg);
   ++c.cases;
   if (!k.ok) {
     ++c.fallback;
@@ -127,8 +128,8 @@ static void check_cell(double w0, const double (&nb)[4], const double (&hot)[4],
   }
   if (bits(ph) != bits(ref) && !(std::isnan(ph) && std::isnan(ref))) {
     if (c.mismatches < 5)
-      std::fprintf(stderr, "LIM %d mismatch: w0=%a nb=%a %a %a %a hot=%a %a %a %a phi=%a ref=%a\n", LIM, w0, nb[0],
-                   nb[1], nb[2], nb[3], hot[0], hot[1], hot[2], hot[3], ph, ref);
+      std::fprintf(stderr, "LIM %d N %d mismatch: w0=%a nb=%a %a %a %a hot0=%a phi=%a ref=%a\n", LIM, N, w0, nb[0],
+                   nb[1], nb[2], nb[3], hot[0], ph, ref);
     ++c.mismatches;
   }
 }
@@ -206,14 +207,34 @@ static void make_cell(int kind, double& w0, double (&nb)[4], double (&hot)[4]) {
   }
 }
 
-template <int LIM>
+// N > 4 candidates (several face quadrature points): the cell's four face terms,
+// then more made from them: exact copies, one-ulp neighbours, relative 1e-6 and
+// 1e-4 changes, sign flips and unrelated values
+template <int N>
+static void extend(const double (&h4)[4], double (&hot)[N]) {
+  for (int s = 0; s < 4; ++s) hot[s] = h4[s];
+  for (int s = 4; s < N; ++s) {
+    const double b = h4[g_rng() % 4];
+    switch (g_rng() % 6) {
+      case 0: hot[s] = b; break;
+      case 1: hot[s] = ulps(b, (long)(g_rng() % 5) - 2); break;
+      case 2: hot[s] = b * (1 + 1e-6 * sgn()); break;
+      case 3: hot[s] = b * (1 + 1e-4 * sgn()); break;
+      case 4: hot[s] = -b; break;
+      default: hot[s] = b * unif(-3, 3);
+    }
+  }
+}
+
+template <int LIM, int N>
 static Counts run(long n) {
   Counts c;
   g_salt = (uint32_t)g_rng();
   for (long i = 0; i < n; ++i) {
-    double w0, nb[4], hot[4];
-    make_cell((int)(i % 7), w0, nb, hot);
-    check_cell<LIM>(w0, nb, hot, c);
+    double w0, nb[4], h4[4], hot[N];
+    make_cell((int)(i % 7), w0, nb, h4);
+    extend<N>(h4, hot);
+    check_cell<LIM, N>(w0, nb, hot, c);
   }
   return c;
 }
@@ -221,12 +242,16 @@ static Counts run(long n) {
 int main(int argc, char** argv) {
   const long n = argc > 1 ? std::atol(argv[1]) : 1000000;
   g_rng.seed(argc > 2 ? std::strtoull(argv[2], nullptr, 10) : 1);
-  const Counts c[4] = {run<0>(n), run<1>(n), run<2>(n), run<3>(n)};
+  // the four faces, and 2 and 3 face quadrature points (8 and 12 candidates)
+  const Counts c[4] = {run<0, 4>(n), run<1, 4>(n), run<2, 4>(n), run<3, 4>(n)};
+  const Counts q[4] = {run<0, 12>(n / 2), run<1, 8>(n / 2), run<2, 12>(n / 2), run<3, 8>(n / 2)};
   long bad = 0;
   for (int l = 0; l < 4; ++l) {
     std::printf("%d cases=%ld mismatches=%ld fallback=%ld second=%ld\n", l, c[l].cases, c[l].mismatches,
                 c[l].fallback, c[l].second);
-    bad += c[l].mismatches;
+    std::printf("%d+ cases=%ld mismatches=%ld fallback=%ld second=%ld\n", l, q[l].cases, q[l].mismatches,
+                q[l].fallback, q[l].second);
+    bad += c[l].mismatches + q[l].mismatches;
   }
   return bad ? 1 : 0;
 }

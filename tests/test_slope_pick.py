@@ -1,6 +1,7 @@
 """The FP64 reconstruction kernel evaluates the limiter only at the faces that decide
 phi (pyhype_gb300/csrc/e2d_slope_pick.cuh).  These CPU tests compile the pick for the
-host and check, over millions of random and adversarial cells (linear profiles, exact
+host and check, over millions of random and adversarial cells with four candidates
+(one point per face) and with 8 and 12 (2 and 3 face quadrature points) (linear profiles, exact
 and one-ulp ties, uniform regions, slopes at the limiters' special points and on the
 falling branch, zeros of both signs, subnormals, infinities, NaN), that phi from the
 picked faces equals phi from all four faces bit for bit, for all four limiters.  The
@@ -39,9 +40,9 @@ def _compile(tmp, header_text=None):
 def _run(exe, cases, seed):
     r = subprocess.run([exe, str(cases), str(seed)], capture_output=True, text=True)
     out = {}
-    for line in r.stdout.splitlines():
+    for line in r.stdout.splitlines():  # "<lim> ..." four candidates, "<lim>+ ..." 8 or 12
         lim, rest = line.split(" ", 1)
-        out[int(lim)] = {k: int(v) for k, v in re.findall(r"(\w+)=(\d+)", rest)}
+        out[lim] = {k: int(v) for k, v in re.findall(r"(\w+)=(\d+)", rest)}
     return r.returncode, out
 
 
@@ -49,7 +50,7 @@ def test_pick_equals_all_faces(tmp_path):
     exe = _compile(str(tmp_path))
     for seed in (1, 2):
         rc, out = _run(exe, 1_500_000, seed)
-        assert set(out) == {0, 1, 2, 3}
+        assert set(out) == {"0", "1", "2", "3", "0+", "1+", "2+", "3+"}
         for lim, c in out.items():
             assert c["mismatches"] == 0, (lim, seed, c)
             assert c["fallback"] < 0.3 * c["cases"], (lim, c)  # the pick mostly applies
@@ -74,4 +75,4 @@ def test_harness_detects_weakened_pick(tmp_path, mutation, limiters):
     rc, out = _run(exe, 1_500_000, 5)
     assert rc != 0
     for lim in limiters:
-        assert out[lim]["mismatches"] > 0, (mutation, lim, out[lim])
+        assert out[str(lim)]["mismatches"] > 0, (mutation, lim, out[str(lim)])
