@@ -382,19 +382,19 @@ static int bench_halo_t(E2DHandle h, int32_t reps, double* ms, int64_t* ntiles) 
     if (nb_edge[k]) { lists[1][k] = interior[r1++ % interior.size()]; ++counts[1]; }
     if (edge[k]) { lists[2][k] = interior[r2++ % interior.size()]; ++counts[2]; }
   }
-  int4* d = nullptr;
-  CK(cudaMalloc(&d, sizeof(int4) * n));
   // every instance active while timing (a finished run leaves them inactive, and an
   // inactive instance's tiles return at once); the instance table is put back after
   const int ninst = (int)h->hinst.size();
   std::vector<InstanceState> saved(ninst);
   CK(cudaMemcpyAsync(saved.data(), h->inst, sizeof(InstanceState) * ninst, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  CK(launch_set_time(h->inst, ninst, saved[0].t, 0.0, h->stream));
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  int err = 0;
+  int4* d = nullptr;
+  CK(cudaMalloc(&d, sizeof(int4) * n));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t ce0 = launch_set_time(h->inst, ninst, saved[0].t, 0.0, h->stream);
+  if (ce0 == cudaSuccess) ce0 = cudaEventCreate(&e0);
+  if (ce0 == cudaSuccess) ce0 = cudaEventCreate(&e1);
+  int err = ce0 == cudaSuccess ? 0 : fail(E2D_ERR_CUDA, "e2d_bench_halo: %s", cudaGetErrorString(ce0));
   for (int v = 0; v < 3 && !err; ++v) {
     TileSet ts = h->ts;
     ts.cell[1] = d;
@@ -412,8 +412,8 @@ static int bench_halo_t(E2DHandle h, int32_t reps, double* ms, int64_t* ntiles) 
     if (ce != cudaSuccess) err = fail(E2D_ERR_CUDA, "e2d_bench_halo: %s", cudaGetErrorString(ce));
     ms[v] = t / reps;
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
   cudaFree(d);
   CK(cudaMemcpyAsync(h->inst, saved.data(), sizeof(InstanceState) * ninst, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
