@@ -1,41 +1,37 @@
 """Algorithmic work per launch of each FP64 stage kernel, for the roofline.
 
-Counts are +, -, *, /, sqrt = 1 flop each (min/max/compare/abs/negation = 0), read
-off the kernel code on its dominant path: Roe flux, Venkatakrishnan limiter,
-conservative reconstruction, Cartesian block, interior cell, no Harten correction
-triggered.  Divisions and square roots are listed separately because each costs the
-FP64 pipe several instruction slots (a reciprocal seed plus Newton steps).
+Counts are +, -, *, /, sqrt = 1 flop each (min/max/compare/abs/negation/select = 0) of
+the reference's own operation sequence on the benchmark's path (Roe flux,
+Venkatakrishnan limiter, conservative reconstruction, blocks that take the rotation
+path, as the 2x4 rectangular layout's ULP-skewed blocks do).  They are instrumented,
+not read off by hand: tests/test_flop_count.py runs an FP64 PyTorch restatement of the
+scheme (value-exact against the reference's fixtures, vectorised over whole arrays as
+the reference's numpy code is) under an operation counter and checks these constants.
 
-k_reconstruct, per cell (4 variables):
-  interface averages        4 x (add + mul)                         =  8 / var
-  Green-Gauss gx, gy        2 x (4 mul + 3 add + 1 mul)             = 16 / var
-  dmax, dmin                2 sub                                    =  2 / var
-  per side (4): high-order term 3, davg 2, slope 1 div,
-                Venkatakrishnan 5 + 1 div                           = 48 / var
-  limited face states       4 x (mul + add)                         =  8 / var
-                                                          -> 82 x 4 = 328
-  4 face states to primitive (2 div + 7)                              =  36
-  total 364 flops, 40 of them divisions (the reference's operation count; the
-  kernel evaluates the slope and psi only at the faces that decide phi, about 4 of
-  the 16 per cell, and gets the same phi)
-k_flux, per face (Roe):
-  Roe average 18 (1 div, 3 sqrt), 3 sound speeds 9 (3 div, 3 sqrt), speeds 6,
-  Harten 4, H/ua/1/a/r2a/h 13 (2 div), dW 4, Lp dW 8, |L| 4, Rc 22,
-  F(WL)+F(WR) 26, flux combine 16, 2 L F 8                             = 138
-  (6 divisions, 6 square roots); a cell owns 2 faces
+k_reconstruct, per interior cell: 388 (block-edge cells add the outside states: 156/n
+per cell on an n x n block).  By hand: interface averages 4 x (add + mul) = 8,
+  Green-Gauss gx, gy 2 x (4 mul + 3 add + 1 mul) = 16, dmax/dmin 2, per side (4): high-
+  order term 3, davg 2, slope 1 div, Venkatakrishnan 5 + 1 div = 48, limited face states
+  8 -> 82 per variable x 4 = 328; 4 face states rotated (6) and converted to primitive
+  (2 div + 7) = 60.  40 of them divisions (the kernel evaluates the slope and psi only
+  at the faces that decide phi, about 4 of the 16 per cell, and gets the same phi).
+k_flux, per face: 154.  Roe average 18 (1 div, 3 sqrt), 3 sound speeds 9 (3 div,
+  3 sqrt), speeds 6, Harten 4 + 8 for both corrected speeds (the reference forms them
+  over whole arrays and selects), H/ua/1/a/r2a/h 13 (2 div), dW 4, Lp dW 8, |L| 4,
+  Rc 22, F(WL)+F(WR) 26, flux combine 16, rotation back 6, 2 L F 8; a cell owns 2 faces.
 k_update, per cell-stage: divergence 5 / var = 20, RK4 stage program on average
-  1.75 updates x (1 + 4 x 2)                                           = 35.75
+  1.75 updates x (1 + 4 x 2) = 35.75.
 k_dt, per cell (once per step): conversion 9 (2 div), sound 3 (1 div, 1 sqrt),
-  2 x (add + div)                                                      = 16
+  2 x (add + div) = 16.
 """
 from __future__ import annotations
 
-FLOPS_PER_CELL_RECONSTRUCT = 364
-FLOPS_PER_FACE_ROE = 138
+FLOPS_PER_CELL_RECONSTRUCT = 388
+FLOPS_PER_FACE_ROE = 154
 FLOPS_PER_CELL_UPDATE_RK4 = 35.75
 FLOPS_PER_CELL_DT = 16
 DIV_PER_CELL_RECONSTRUCT = 40
-DIV_PER_FACE_ROE = 6
+DIV_PER_FACE_ROE = 8  # 6, and the 2 of both corrected speeds
 SQRT_PER_FACE_ROE = 6
 
 # FP64 arithmetic instructions (DADD + DMUL + DFMA, per thread) per cell of each FP64
