@@ -58,8 +58,9 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
                     help="arithmetic of the timed multiblock run (fp32: the FP32 form; for profiling)")
     ap.add_argument("--workload", default="multiblock",
-                    choices=["multiblock", "ensemble", "adjoint", "adjoint-study"],
+                    choices=["multiblock", "ensemble", "adjoint", "adjoint-study", "dmr"],
                     help="'ensemble' runs the full 512-instance, 200-step batched comparison instead; "
+                         "'dmr' the double-Mach case with the FP64 scheme's one-ulp sensitivity; "
                          "'adjoint' one recorded forward + reverse pass on an n x n block for --steps steps; "
                          "'adjoint-study' the finite-difference convergence study of the reverse pass")
     return ap.parse_args()
@@ -456,11 +457,13 @@ def adjoint_study(limiters=("Venkatakrishnan", "BarthJespersen"), steps=(100, 20
     return res
 
 
-def dmr_section(stream):
+def dmr_section(stream, sensitivity: bool = False):
     """Mach-10 double-Mach reflection: [0,4] x [0,1] as 5 blocks of 400 x 500 cells
     (dx = dy = 0.002), HLLL/Venkatakrishnan/Green-Gauss, primitive reconstruction,
     SSP-RK2 at CFL 0.4 to t = 0.2, FP64 and FP32 through Euler2D; FP32 L1 density
-    difference at t_final."""
+    difference at t_final.  With ``sensitivity`` also an FP64 run whose initial
+    densities and energies are one ulp larger (the FP64 scheme's own round-off
+    sensitivity beside the FP32 difference)."""
     import numpy as np
     import torch
 
@@ -471,11 +474,16 @@ def dmr_section(stream):
                        "reconstruction, SSP-RK2, CFL 0.4, t_final 0.2"}
     states = {}
     totals = {}
-    for prec in ("fp64", "fp32"):
+    for prec in ("fp64", "fp32") + (("fp64_ulp",) if sensitivity else ()):
         cfg, gen = double_mach()
-        sim = Euler2D(cfg, gen, precision=prec)
+        sim = Euler2D(cfg, gen, precision=prec[:4])
         sim.device.set_stream(stream.cuda_stream)
         sim._pre_process_solve()
+        if prec == "fp64_ulp":
+            U = sim.device.get_state()
+            U[0] = np.nextafter(U[0], np.inf)
+            U[3] = np.nextafter(U[3], np.inf)
+            sim.device.set_state(U)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
@@ -492,6 +500,9 @@ def dmr_section(stream):
         sim.device.close()
     a, b = states["fp64"], states["fp32"]
     out["fp32_l1_density_rel_vs_fp64"] = float(np.sum(np.abs(b - a)) / np.sum(np.abs(a)))
+    if sensitivity:
+        out["fp64_one_ulp_initial_change_l1_density"] = float(np.sum(np.abs(states["fp64_ulp"] - a)) / np.sum(np.abs(a)))
+        out.pop("fp64_ulp", None)
     # inflow and outflow sides: the totals are not conserved; FP32 against FP64 at t_final
     out["fp32_totals_rel_vs_fp64"] = {
         "mass": float(abs(totals["fp32"][0] - totals["fp64"][0]) / abs(totals["fp64"][0])),
@@ -560,6 +571,15 @@ def main():
         torch.cuda.set_device(local)
         if rank == 0:
             adjoint_study()
+        return
+    if args.workload == "dmr":
+        import torch
+
+        torch.cuda.set_device(local)
+        st = torch.cuda.Stream()
+        res = dmr_section(st, sensitivity=True)
+        if rank == 0:
+            print(json.dumps({"metric": "cell-stage updates/s, double-Mach reflection", "dmr": res}), flush=True)
         return
     if args.workload == "ensemble":
         import torch
