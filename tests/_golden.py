@@ -64,7 +64,7 @@ def geometry(z, b: int):
 
     The transcendental functions behind the face angles and areas (numpy arctan,
     arccos, cos, sin) may round differently on another platform; parity with the
-    reference's run is judged on the reference's own geometry."""
+    reference's run is compared on the reference's own geometry."""
     from pyhype_gb300.mesh.quad_mesh import BlockGeometry
 
     p = f"geo{b}_"
