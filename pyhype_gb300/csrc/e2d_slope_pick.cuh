@@ -31,10 +31,11 @@
 //     (same |numerator| and |denominator| bits, both exactly 1, or both exactly 0)
 //     the pick gives up;
 //   * every other face then has an exact slope at least 0.88*TAU (relative) away from
-//     the chosen ones, where psi differs by more than 5e-12 relative (5.6e-12 at the
-//     flat peak, second order; more elsewhere), far above the 7e-16 that the
-//     rounding of two psi evaluations can account for: its computed psi is strictly
-//     larger than the chosen minimum;
+//     the chosen ones, where psi differs by at least 8.8e-14 relative (2.6e-7 on the
+//     rising branch below s = 4, 5.6e-12 at the flat peak, second order, and
+//     0.88*TAU/s >= 8.8e-14 on the falling branch up to s = 1e8), far above the
+//     7e-16 that the rounding of two psi evaluations can account for: its computed
+//     psi is strictly larger than the chosen minimum;
 //   * on the falling branch psi - 1 ~ 1/s, so the difference TAU/s must stay above the
 //     rounding: the pick gives up when it would need psi at a slope above 1e8
 //     (van Leer: when the smallest slope is above 1e8);
