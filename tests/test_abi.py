@@ -127,3 +127,22 @@ def test_create_validates_the_problem_before_touching_a_device(name, mutate, mes
     code = L.e2d_create(ctypes.addressof(c), ctypes.addressof(b), ctypes.addressof(g), ctypes.byref(h))
     assert code == -1 and not h.value
     assert message in L.e2d_last_error().decode()
+
+
+def test_bench_and_check_entry_points_validate_arguments():
+    """The measurement and check entry points reject bad arguments before touching a
+    device: a null handle, a missing output, a wait bound below one poll."""
+    from pyhype_gb300._native import E2D_ERR_INVALID, load
+
+    L = load()
+    L.e2d_bench_halo.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+    L.e2d_bench_set_tma.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    L.e2d_check_wait_bound.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+    L.e2d_set_kernel_choice.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
+    ms = (ctypes.c_double * 3)()
+    assert L.e2d_bench_halo(None, 10, ctypes.addressof(ms), None) == E2D_ERR_INVALID
+    assert L.e2d_bench_set_tma(None, 1) == E2D_ERR_INVALID
+    arrived = ctypes.c_int32(0)
+    assert L.e2d_check_wait_bound(0, 0, ctypes.byref(arrived)) == E2D_ERR_INVALID
+    assert L.e2d_check_wait_bound(0, 10, None) == E2D_ERR_INVALID
+    assert L.e2d_set_kernel_choice(None, 0, 0, 0) == E2D_ERR_INVALID
