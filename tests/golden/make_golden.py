@@ -336,7 +336,7 @@ CASES = {
     "ops_explosion_cons": (dict(nx=24, ny=20), lambda: single_block(0, 10, 0, 10), lambda: ExplosionIC(), 6, "all", 3, None),
     "p100": (dict(nx=100, ny=100), lambda: single_block(0, 10, 0, 10), lambda: ExplosionIC(), 100, (1, 10, 100), None, None),
     "m2x4_40": (dict(nx=40, ny=40), lambda: rect_mesh(2, 4, 10.0, 20.0), lambda: ExplosionIC(), 12, (1, 4, 12), 2, None),
-    "m2x4_150": (dict(nx=150, ny=150), lambda: rect_mesh(2, 4, 10.0, 20.0), lambda: ExplosionIC(), 2, (), None, None),
+    "m2x4_150": (dict(nx=150, ny=150), lambda: rect_mesh(2, 4, 10.0, 20.0), lambda: ExplosionIC(), 10, (), None, None),
     "lim_bj": (dict(nx=20, ny=16, fvm_slope_limiter_type="BarthJespersen"), lambda: single_block(0, 10, 0, 8), lambda: ExplosionIC(**MOVING), 5, "all", 2, None),
     "lim_va": (dict(nx=20, ny=16, fvm_slope_limiter_type="VanAlbada"), lambda: single_block(0, 10, 0, 8), lambda: ExplosionIC(**MOVING), 5, "all", 2, None),
     "lim_vl": (dict(nx=20, ny=16, fvm_slope_limiter_type="VanLeer"), lambda: single_block(0, 10, 0, 8), lambda: ExplosionIC(**MOVING), 5, "all", 2, None),
