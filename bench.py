@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", "--cells-per-side", dest="n", type=int, default=1024, help="cells per block side")
-    ap.add_argument("--cpu-steps", type=int, default=1, help="RK4 steps in the CPU-baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=2, help="timed RK4 steps in the CPU-baseline sample")
     ap.add_argument("--skip-cpu-baseline", action="store_true", help="omit the CPU baseline (profiling runs)")
     ap.add_argument("--skip-ensemble", action="store_true", help="omit the batched-ensemble section")
     ap.add_argument("--skip-adjoint", action="store_true", help="omit the adjoint section")
@@ -211,28 +211,69 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(n: int, steps: int):
-    """The CPU oracle on every host core, one full RK4 step of the workload per sample."""
+def oracle_steps(P, U, warmup: int, steps: int, integrator: str = "RK4"):
+    """The CPU oracle on every host core, run as the reference's loop body: per step the
+    CFL dt, then one RK step advancing the state in place.  ``warmup`` untimed steps,
+    then ``steps`` timed ones.  Returns (seconds, threads, (dt, state) after the first
+    step or None when that step was timed)."""
+    import numpy as np
+
     from oracle.oracle import Oracle, lib
     from pyhype_gb300.time_marching import tableau
 
-    (P, U), cfg = make_solver(n, device_solver=False)
-    threads = os.cpu_count() or 1
-    O = Oracle(P, threads=threads)
-    a = tableau("RK4")
-    dt = float(O.dt(U)[0])
+    O = Oracle(P, threads=os.cpu_count() or 1)
+    a = tableau(integrator) if isinstance(integrator, str) else integrator
+    U = np.array(U, dtype=np.float64, copy=True, order="C").reshape(4, P.ncell)
+    first = None
+    t = 0.0
     t0 = time.perf_counter()
-    for _ in range(steps):
-        U = O.step(U, a, dt, 0.0)
+    for k in range(warmup + steps):
+        if k == warmup:
+            t0 = time.perf_counter()
+        dt = float(O.dt(U)[0])
+        O.step(U, a, dt, t, inplace=True)
+        t += dt
+        if k == 0 and warmup > 0:
+            first = (dt, U.copy())
     el = time.perf_counter() - t0
-    used = lib().oracle_max_threads()
+    return el, int(lib().oracle_max_threads()), first
+
+
+def cpu_baseline(n: int, steps: int):
+    """The CPU oracle on every host core: one untimed step, then ``steps`` timed steps
+    of the workload (the reference arm's loop body).  Also returns the initial state and
+    the oracle's first step for the full-size parity check."""
+    (P, U0), cfg = make_solver(n, device_solver=False)
+    el, used, first = oracle_steps(P, U0, warmup=1, steps=steps)
     return {
         "value": P.ncell * 4 * steps / el,
         "unit": "cell-stage updates/s",
-        "cores": int(used),
+        "cores": used,
         "kind": "port",
-        "sample": f"{steps} RK4 step(s) of the full {P.ncell}-cell workload, {el:.2f} s wall on {used} threads",
-    }
+        "sample": f"{steps} timed RK4 step(s) of the full {P.ncell}-cell workload after 1 untimed step, each the "
+                  f"CFL dt plus one step in place, {el:.2f} s wall on {used} threads",
+    }, U0, first
+
+
+def step_parity(P, U0, tableau_a, dt_ref, U1_ref, t: float = 0.0):
+    """One step of the device FP64 path from U0 against the oracle's step (dt and
+    state, value for value)."""
+    import numpy as np
+
+    from pyhype_gb300._native import DeviceSolver
+
+    S = DeviceSolver(P, tableau=tableau_a)
+    try:
+        S.set_state(U0)
+        dt = float(S.compute_dt()[0])
+        S.step(dt, t)
+        G1 = S.get_state()
+    finally:
+        S.close()
+    diff = np.abs(G1 - U1_ref)
+    return {"dt_equal": dt == dt_ref, "max_abs_diff": float(np.max(diff)),
+            "max_rel_diff": float(np.max(diff / np.maximum(np.abs(U1_ref), 1e-300))),
+            "bitwise": bool(dt == dt_ref and np.array_equal(G1, U1_ref)), "cells": int(P.ncell)}
 
 
 def ensemble_section(stream, full: bool = False, autotune: bool = True):
@@ -474,11 +515,14 @@ def dmr_section(stream, sensitivity: bool = False):
                        "reconstruction, SSP-RK2, CFL 0.4, t_final 0.2"}
     states = {}
     totals = {}
+    start = None
     for prec in ("fp64", "fp32") + (("fp64_ulp",) if sensitivity else ()):
         cfg, gen = double_mach()
         sim = Euler2D(cfg, gen, precision=prec[:4])
         sim.device.set_stream(stream.cuda_stream)
         sim._pre_process_solve()
+        if prec == "fp64":
+            start = (sim.problem, sim.device.get_state(), sim._time_integrator.tableau())
         if prec == "fp64_ulp":
             U = sim.device.get_state()
             U[0] = np.nextafter(U[0], np.inf)
@@ -508,40 +552,31 @@ def dmr_section(stream, sensitivity: bool = False):
         "mass": float(abs(totals["fp32"][0] - totals["fp64"][0]) / abs(totals["fp64"][0])),
         "energy": float(abs(totals["fp32"][3] - totals["fp64"][3]) / abs(totals["fp64"][3]))}
     out["fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    # parity at full size: the first FP64 step on the device against the CPU oracle's
+    P, U0, a = start
+    _, _, first = oracle_steps(P, U0, warmup=1, steps=0, integrator=a)
+    out["parity"] = step_parity(P, U0, a, *first)
     return out
 
 
 def run_reference(args, ws, rank):
     """--impl reference: the reference algorithm's CPU implementation (C restatement,
-    all host threads) on the same workload; rank 0 only."""
+    all host threads) on the same workload, through the same loop body as the CPU
+    baseline of the GPU arm (CFL dt + one RK step in place per step); rank 0 only."""
     if rank != 0:
         return
-    from oracle.oracle import Oracle, lib
-    from pyhype_gb300.time_marching import tableau
-
     (P, U), cfg = make_solver(args.n, device_solver=False)
-    O = Oracle(P, threads=os.cpu_count() or 1)
-    a = tableau("RK4")
-    t = 0.0
-    for _ in range(args.warmup):
-        dt = float(O.dt(U)[0])
-        U = O.step(U, a, dt, t)
-        t += dt
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        dt = float(O.dt(U)[0])
-        U = O.step(U, a, dt, t)
-        t += dt
-    el = time.perf_counter() - t0
+    el, used, _ = oracle_steps(P, U, warmup=args.warmup, steps=args.steps)
     value = P.ncell * 4 * args.steps / el
-    used = int(lib().oracle_max_threads())
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "cell-stage updates/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cells": P.ncell, "l2": "working set > L2"},
+        "config": {"workload": WORKLOAD, "cells": P.ncell, "blocks": 8, "stages_per_step": 4,
+                   "l2": "inputs larger than L2 (state 268 MB)", "parallelism": "host cores"},
         "cpu_baseline": {"value": value, "unit": "cell-stage updates/s", "cores": used, "kind": "port",
-                         "sample": f"every step is one full RK4 step of the workload on {used} host threads"},
+                         "sample": f"every step is the CFL dt plus one full RK4 step of the workload in place, "
+                                   f"on {used} host threads"},
         "e2e": {"value": value, "unit": "cell-stage updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -777,9 +812,11 @@ def main():
             adjoint = {"error": str(exc)}
 
     dmr = None
+    parity = {}
     if not args.skip_dmr and ws == 1:
         try:
             dmr = dmr_section(stream)
+            parity["dmr_ssprk2_step"] = dmr.pop("parity")
         except Exception as exc:
             dmr = {"error": str(exc)}
 
@@ -840,9 +877,17 @@ def main():
     }
     if rank == 0 and ws == 1 and not args.skip_cpu_baseline:
         try:
-            line["cpu_baseline"] = cpu_baseline(args.n, args.cpu_steps)
+            line["cpu_baseline"], U0, first = cpu_baseline(args.n, args.cpu_steps)
+            # full-size parity: the device's first FP64 step from the same seeded state
+            if not np.array_equal(U0, P.to_soa([b.state.data for b in solver.blocks])):
+                raise RuntimeError("CPU and GPU arms start from different states")
+            parity["multiblock_rk4_step"] = step_parity(P, U0, solver._time_integrator.tableau(), *first)
         except Exception as exc:  # the GPU number stands without it
             line["cpu_baseline"] = {"value": None, "error": str(exc)}
+    if parity:
+        line["parity"] = {"bitwise": all(v.get("bitwise", False) for v in parity.values()),
+                          "max_abs_diff": max(v.get("max_abs_diff", float("inf")) for v in parity.values()),
+                          **parity}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -171,7 +171,7 @@ typedef struct {
   const double* qp[E2D_MAX_QP][8];
 } E2DGeometry;
 
-/* Result of the positivity check (pyhype/solvers/Euler2D.py:310-318). */
+/* Result of the positivity check (pyhype/solvers/Euler2D.py:144-152). */
 typedef struct {
   int32_t ok;           /* 1 if every cell has rho > 0 and E > 0              */
   int32_t block;        /* first offending block, -1 if ok                    */
@@ -228,7 +228,7 @@ E2D_API int e2d_compute_dt(E2DHandle h, double* dt_host);
 /* One ExplicitRungeKutta.integrate(dt) including the ghost/BC refresh after every
    stage; t is the solver time at the start of the step (moving BCs).              */
 E2D_API int e2d_step(E2DHandle h, double dt, double t);
-/* The Euler2D._solve loop (pyhype/solvers/Euler2D.py:361-376): dt -> clamp to
+/* The Euler2D._solve loop (pyhype/solvers/Euler2D.py:175-216): dt -> clamp to
    t_final - t -> step -> realizability, until t >= t_final or max_steps.  Time is
    non-dimensional (t_final already multiplied by a_inf).  *t_inout is updated.
    With several instances, *t_inout is ignored on entry (every instance continues
@@ -307,10 +307,13 @@ E2D_API int e2d_adjoint_backward(E2DHandle h, double* grad_dev);
    array of E2D_NOALLOC_MAX_CELLS/256 + 1 eight-byte words (512 KiB) that every GPU
    loading the library keeps until the process exits; ncell above
    E2D_NOALLOC_MAX_CELLS returns E2D_ERR_INVALID.  The first call on a device looks
-   up that array's device address, so make it before any stream capture.  All calls
-   share the array and each overwrites the part it uses: calls that overlap on the
-   GPU (different streams or threads) race.  Runs on `stream` (NULL = legacy default
-   stream) and blocks until the result is on the host.                            */
+   up that array's device address (a one-time set-up); make that first call before
+   any stream capture begins.  All calls share the array and each overwrites the part
+   it uses: calls that overlap on the GPU (different streams or threads) race.  Runs
+   on `stream` (NULL = legacy default stream); every call is a blocking host call: it
+   copies the result into host memory and synchronizes `stream` before it returns.
+   A CUDA error already pending on the calling thread is reported (E2D_ERR_CUDA, its
+   text in e2d_last_error) and left in place; nothing is launched then.            */
 #define E2D_NOALLOC_MAX_CELLS 16777216
 E2D_API int e2d_compute_dt_noalloc(const double* dev_state, int64_t ncell, const double* dev_cfl_dx,
                                    const double* dev_cfl_dy, double gamma, double gm1, double cfl,

@@ -306,10 +306,14 @@ static void hlll_flux(const double* WL, const double* WR, double g, double gm1, 
   for (int v = 0; v < 4; ++v) F[v] = (Lplus * FL[v] - Lminus * FR[v] + sc * dU[v]) / den;
 }
 
-/* HLLE with Harten-bounded speeds.  The reference's FluxHLLE cannot be constructed
-   (pyhype/flux/HLLE.py:25 passes the config as the fluid), so this restates the
-   standard HLLE flux on the same bounds HLLL uses; there is no reference output to
-   pin it against. */
+/* FluxHLLE.compute_flux (pyhype/flux/HLLE.py:22-47): the HLL flux (Harten, Lax and van
+   Leer 1983) on Einfeldt's bounds (SIAM J. Numer. Anal. 25(2), 1988; Toro, Riemann
+   Solvers and Numerical Methods for Fluid Dynamics, 3rd ed., 10.3 and 10.6)
+   L+ = max(u_R + a_R, u~ + a~), L- = min(u_L - a_L, u~ - a~) with the Roe speeds
+   Harten-corrected (HLLE.py:27-33).  The reference applies np.where(L- >= 0, F_L, .)
+   and then np.where(L+ <= 0, F_R, .) (HLLE.py:41-43), so F_R wins where both hold.
+   The reference's class cannot be constructed (HLLE.py:25 passes the config as the
+   fluid), so there is no reference output to pin this against. */
 static void hlle_flux(const double* WL, const double* WR, double g, double gm1, double* F) {
   double Q[4];
   roe_average(WL, WR, Q);
@@ -325,8 +329,8 @@ static void hlle_flux(const double* WL, const double* WR, double g, double gm1, 
   prim_to_cons(WR, gm1, UR);
   FL[0] = UL[1]; FL[1] = UL[1] * WL[1] + WL[3]; FL[2] = UL[1] * WL[2]; FL[3] = WL[1] * (UL[3] + WL[3]);
   FR[0] = UR[1]; FR[1] = UR[1] * WR[1] + WR[3]; FR[2] = UR[1] * WR[2]; FR[3] = WR[1] * (UR[3] + WR[3]);
-  if (Lminus >= 0) { for (int v = 0; v < 4; ++v) F[v] = FL[v]; return; }
   if (Lplus <= 0) { for (int v = 0; v < 4; ++v) F[v] = FR[v]; return; }
+  if (Lminus >= 0) { for (int v = 0; v < 4; ++v) F[v] = FL[v]; return; }
   double den = Lplus - Lminus;
   double LL = Lminus * Lplus;
   for (int v = 0; v < 4; ++v) F[v] = (Lplus * FL[v] - Lminus * FR[v] + LL * (UR[v] - UL[v])) / den;
@@ -719,6 +723,22 @@ OR_API int oracle_max_threads(void) {
 #else
   return 1;
 #endif
+}
+
+/* The face flux function alone, for property tests: n face-frame primitive pairs
+   (WL[4 k .. 4 k + 3], WR[...]) -> F[4 k ..], flux code as in E2DConfig.flux. */
+OR_API int oracle_flux(int flux, int64_t n, const double* WL, const double* WR, double gamma, double gm1,
+                       double* F) {
+  E2DConfig cfg;
+  memset(&cfg, 0, sizeof cfg);
+  cfg.flux = flux;
+  cfg.gamma = gamma;
+  cfg.gm1 = gm1;
+  Ctx C;
+  memset(&C, 0, sizeof C);
+  C.cfg = &cfg;
+  for (int64_t k = 0; k < n; ++k) face_flux(&C, WL + 4 * k, WR + 4 * k, F + 4 * k);
+  return 0;
 }
 
 OR_API int oracle_residual(const E2DConfig* cfg, const E2DBlock* blk, const E2DGeometry* geo,

@@ -35,6 +35,7 @@ def lib():
         L.oracle_dt.argtypes = [vp, vp, vp, vp, vp]
         L.oracle_realizable.argtypes = [vp, vp, vp, vp, vp]
         L.oracle_ghost_layer.argtypes = [vp, vp, vp, vp, ctypes.c_double, vp]
+        L.oracle_flux.argtypes = [ctypes.c_int, ctypes.c_int64, vp, vp, ctypes.c_double, ctypes.c_double, vp]
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         L.oracle_max_threads.restype = ctypes.c_int
         _lib = L
@@ -43,6 +44,17 @@ def lib():
 
 def _p(x):
     return ctypes.cast(ctypes.byref(x), ctypes.c_void_p) if not isinstance(x, np.ndarray) else x.ctypes.data
+
+
+def face_flux(flux: int, WL: np.ndarray, WR: np.ndarray, gamma: float = 1.4, gm1: float = 1.4 - 1) -> np.ndarray:
+    """The oracle's Riemann flux (code as in E2DConfig.flux) of face-frame primitive
+    states WL, WR, each (n, 4) (rho, u, v, p); returns (n, 4)."""
+    WL = np.ascontiguousarray(WL, dtype=np.float64).reshape(-1, 4)
+    WR = np.ascontiguousarray(WR, dtype=np.float64).reshape(-1, 4)
+    out = np.zeros_like(WL)
+    lib().oracle_flux(int(flux), WL.shape[0], WL.ctypes.data, WR.ctypes.data, float(gamma), float(gm1),
+                      out.ctypes.data)
+    return out
 
 
 class Oracle:
@@ -89,8 +101,14 @@ class Oracle:
         self.L.oracle_ghost_layer(*self._args(), U.ctypes.data, float(t), out.ctypes.data)
         return out
 
-    def step(self, U: np.ndarray, tableau: np.ndarray, dt: float, t: float = 0.0) -> np.ndarray:
-        U = np.array(U, dtype=np.float64, copy=True).reshape(4, self.P.ncell)
+    def step(self, U: np.ndarray, tableau: np.ndarray, dt: float, t: float = 0.0, inplace: bool = False) -> np.ndarray:
+        """One RK step; returns a new array, or advances U itself with ``inplace`` (U
+        must then be a C-contiguous float64 array of 4 x ncell values)."""
+        if inplace:
+            if U.dtype != np.float64 or not U.flags.c_contiguous or U.size != 4 * self.P.ncell:
+                raise ValueError("inplace step needs a C-contiguous float64 state of 4 x ncell values")
+        else:
+            U = np.array(U, dtype=np.float64, copy=True).reshape(4, self.P.ncell)
         a = np.ascontiguousarray(tableau, dtype=np.float64)
         self.L.oracle_step(*self._args(), U.ctypes.data, a.shape[0], a.ctypes.data, float(dt), float(t))
         return U

@@ -18,15 +18,20 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libeuler2d.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", os.path.join(HERE, "..", "include")]
-# translation unit -> extra flags
+# object name -> (source, extra flags).  The reconstruction launchers of each
+# (arithmetic type, limiter) pair are one object each (e2d_recon_unit.cu), so the
+# largest kernels compile in parallel.
 UNITS = {
-    "e2d_fp64.cu": ["-fmad=false"],
-    "e2d_fp32.cu": [],  # FP32 form: IEEE division (approximate division doubled the L1 density error)
-    "e2d_api.cu": ["-fmad=false"],
-    "e2d_bench.cu": [],
-    "e2d_noalloc.cu": ["-fmad=false"],
-    "e2d_adjoint.cu": ["-fmad=false"],
+    "e2d_fp64": ("e2d_fp64.cu", ["-fmad=false"]),
+    "e2d_fp32": ("e2d_fp32.cu", []),  # FP32 form: contraction allowed, its own division (e2d_device.cuh)
+    "e2d_api": ("e2d_api.cu", ["-fmad=false"]),
+    "e2d_bench": ("e2d_bench.cu", []),
+    "e2d_noalloc": ("e2d_noalloc.cu", ["-fmad=false"]),
+    "e2d_adjoint": ("e2d_adjoint.cu", ["-fmad=false"]),
 }
+for _lim in range(4):
+    UNITS[f"e2d_recon_f64_l{_lim}"] = ("e2d_recon_unit.cu", ["-fmad=false", "-DE2D_T=double", f"-DE2D_LIM={_lim}"])
+    UNITS[f"e2d_recon_f32_l{_lim}"] = ("e2d_recon_unit.cu", ["-DE2D_T=float", f"-DE2D_LIM={_lim}"])
 
 
 def nvcc() -> str:
@@ -52,7 +57,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_unit(name):
         obj = os.path.join(OBJ, name + ".o")
-        cmd = [cc, *ARCH, *COMMON, *UNITS[name], "-c", os.path.join(CSRC, name), "-o", obj]
+        src, flags = UNITS[name]
+        cmd = [cc, *ARCH, *COMMON, *flags, "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -60,7 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             raise RuntimeError(f"nvcc failed for {name}:\n{r.stdout}\n{r.stderr}")
         return obj
 
-    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+    with ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 1)) as ex:
         objs = list(ex.map(compile_unit, UNITS))
     tmp = LIB + ".tmp"
     cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]

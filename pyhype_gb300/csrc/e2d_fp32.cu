@@ -5,6 +5,7 @@
 
 namespace e2d {
 
+E2D_EXTERN_RECON_LIM(float)
 E2D_INSTANTIATE_STAGE_LAUNCHERS(float)
 
 }  // namespace e2d

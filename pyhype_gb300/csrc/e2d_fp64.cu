@@ -5,6 +5,7 @@
 
 namespace e2d {
 
+E2D_EXTERN_RECON_LIM(double)
 E2D_INSTANTIATE_STAGE_LAUNCHERS(double)
 
 // Step bookkeeping, one thread per instance.  begin: decide whether the instance

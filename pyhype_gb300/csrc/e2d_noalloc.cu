@@ -6,6 +6,7 @@
 // handle allocated.  Every GPU that loads the library holds the array until exit.
 #include <cuda_runtime.h>
 
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 
@@ -77,6 +78,12 @@ __global__ void k_dt_final(unsigned long long* __restrict__ scratch, int nparts)
   }
 }
 
+int fail_cuda(const char* what, cudaError_t ce) {
+  char buf[256];
+  snprintf(buf, sizeof buf, "e2d_compute_dt_noalloc: %s: %s", what, cudaGetErrorString(ce));
+  return e2d::set_error(E2D_ERR_CUDA, buf);
+}
+
 }  // namespace
 
 extern "C" int e2d_compute_dt_noalloc(const double* dev_state, int64_t ncell, const double* dev_cfl_dx,
@@ -102,16 +109,21 @@ extern "C" int e2d_compute_dt_noalloc(const double* dev_state, int64_t ncell, co
     }
     scratch = g_scratch_ptr[dev];
   }
+  // An error left by earlier, unrelated work on this thread is reported as such and
+  // left in place for its owner: this call launches nothing on top of it.
+  cudaError_t ce = cudaPeekAtLastError();
+  if (ce != cudaSuccess) return fail_cuda("a CUDA error from earlier work is pending on this thread", ce);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int nparts = (int)((ncell + kTile - 1) / kTile);
   k_dt_partial<<<nparts, kTile, 0, st>>>(dev_state, ncell, dev_cfl_dx, dev_cfl_dy, gamma, gm1, scratch);
+  if ((ce = cudaGetLastError()) != cudaSuccess) return fail_cuda("launch of the per-tile minima", ce);
   k_dt_final<<<1, 1024, 0, st>>>(scratch, nparts);
-  if (cudaGetLastError() != cudaSuccess) return e2d::set_error(E2D_ERR_CUDA, "e2d_compute_dt_noalloc: launch failed");
+  if ((ce = cudaGetLastError()) != cudaSuccess) return fail_cuda("launch of the final minimum", ce);
   unsigned long long bits = 0;
-  if (cudaMemcpyAsync(&bits, scratch + E2D_NOALLOC_MAX_CELLS / kTile, sizeof bits, cudaMemcpyDeviceToHost, st) !=
-          cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess)
-    return e2d::set_error(E2D_ERR_CUDA, "e2d_compute_dt_noalloc: result copy failed");
+  if ((ce = cudaMemcpyAsync(&bits, scratch + E2D_NOALLOC_MAX_CELLS / kTile, sizeof bits, cudaMemcpyDeviceToHost,
+                            st)) != cudaSuccess)
+    return fail_cuda("result copy", ce);
+  if ((ce = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda("stream synchronize", ce);
   double m;
   std::memcpy(&m, &bits, sizeof m);
   *dt_host = cfl * m;

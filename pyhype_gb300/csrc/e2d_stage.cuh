@@ -154,12 +154,20 @@ __device__ __forceinline__ void outside_state(const ParamsT<T>& P, const E2DBloc
 
 // One tile of cells: the body of k_reconstruct.  Returns early (uniformly per CTA)
 // for an inactive instance; the caller synchronises before sW is refilled.
+//
+// A TMA wait that runs out is counted in tma.timeouts (the host then reports the
+// step as failed, and the state it produced is not to be used).  The CTA waits once
+// more, as long again, for the copy in flight: if it lands, sW is the CTA's again and
+// later tiles take plain loads (tma_live = false); if it does not, the CTA sets
+// `abandon` and the caller stops, so nothing writes sW while the copy may still be
+// writing it.
 template <typename T, int LIM, int RECON, bool DBG, int RTY>
 __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4 tl, const T* __restrict__ U,
                                                  const InstanceState* __restrict__ inst, const FaceArraysT<T>& F,
                                                  const DebugOutT<T>& dbg,
                                                  T (&sW)[4][RTY + 2][TileCols<T>::TXW], const TmaTiles& tma,
-                                                 unsigned long long* bar, unsigned& phase, bool& tma_live) {
+                                                 unsigned long long* bar, unsigned& phase, bool& tma_live,
+                                                 bool& abandon) {
   constexpr int C0 = TileCols<T>::C0;
   const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
   const E2DBlock* B = P.blocks + tl.x;
@@ -178,13 +186,15 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
     if (threadIdx.x == 0)
       tma_load_box(&sW[0][0][0], &tma.maps[tl.x], j0 - TileCols<T>::XO, i0 - 1, 0, bar, (unsigned)sizeof(sW));
     const bool arrived = __syncthreads_and(mbar_wait(bar, phase));
-    phase ^= 1u;
     if (!arrived) {  // a wait ran out: report it, wait once more for the copy in flight, drop the tile
       if (threadIdx.x == 0) atomicAdd(tma.timeouts, 1ULL);
-      mbar_wait(bar, phase ^ 1u);
+      const bool landed = __syncthreads_and(mbar_wait(bar, phase));
+      phase ^= 1u;
       tma_live = false;
+      abandon = !landed;  // uniform over the CTA
       return;
     }
+    phase ^= 1u;
     if (RECON == E2D_RECON_PRIMITIVE) {  // conversion in place, one thread per staged cell
       for (int p = threadIdx.x; p < (RTY + 2) * (TX + 2); p += TX * RTY) {
         const int ly = p / (TX + 2), lx = p - ly * (TX + 2);
@@ -393,15 +403,19 @@ __global__ void __launch_bounds__(TX * RTY, MINB) k_reconstruct(ParamsT<T> P, co
   __shared__ __align__(8) unsigned long long bar;
   unsigned phase = 0;
   bool tma_live = tma.maps != nullptr;
+  bool abandon = false;
   if (tma_live) {
     if (threadIdx.x == 0) mbar_init(&bar);
     __syncthreads();
   }
   if constexpr (!PERSIST) {
-    reconstruct_tile<T, LIM, RECON, DBG, RTY>(P, tiles[blockIdx.x], U, inst, F, dbg, sW, tma, &bar, phase, tma_live);
+    reconstruct_tile<T, LIM, RECON, DBG, RTY>(P, tiles[blockIdx.x], U, inst, F, dbg, sW, tma, &bar, phase, tma_live,
+                                              abandon);
   } else {
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-      reconstruct_tile<T, LIM, RECON, DBG, RTY>(P, tiles[tile], U, inst, F, dbg, sW, tma, &bar, phase, tma_live);
+      reconstruct_tile<T, LIM, RECON, DBG, RTY>(P, tiles[tile], U, inst, F, dbg, sW, tma, &bar, phase, tma_live,
+                                                abandon);
+      if (abandon) break;  // a copy may still be writing sW: no further tile touches it
       __syncthreads();  // the next tile refills sW
     }
   }
@@ -873,8 +887,11 @@ static cudaError_t recon_variant(const ParamsT<T>& P, const int4* const* tiles_b
   }
 }
 
+// One limiter's reconstruction launchers (every variant, and the multi-point form).
+// Each (type, limiter) pair is instantiated in a translation unit of its own
+// (e2d_recon_unit.cu), so the kernels compile in parallel.
 template <typename T, int LIM>
-static cudaError_t recon_lim(const ParamsT<T>& P, const int4* const* tiles, const int* n, int variant, bool persistent,
+cudaError_t recon_lim(const ParamsT<T>& P, const int4* const* tiles, const int* n, int variant, bool persistent,
                              const T* U, const InstanceState* inst, FaceArraysT<T> F, const DebugOutT<T>* dbg,
                              cudaStream_t st, const TmaSet* tma) {
   if (P.recon == E2D_RECON_PRIMITIVE)
@@ -893,7 +910,7 @@ static cudaError_t recon_qp(const ParamsT<T>& P, const TileSet& ts, const T* U, 
 }
 
 template <typename T, int LIM>
-static cudaError_t recon_qp_lim(const ParamsT<T>& P, const TileSet& ts, const T* U, const InstanceState* inst,
+cudaError_t recon_qp_lim(const ParamsT<T>& P, const TileSet& ts, const T* U, const InstanceState* inst,
                                 FaceArraysT<T> F, cudaStream_t st) {
   if (P.recon == E2D_RECON_PRIMITIVE) return recon_qp<T, LIM, E2D_RECON_PRIMITIVE>(P, ts, U, inst, F, st);
   return recon_qp<T, LIM, E2D_RECON_CONSERVATIVE>(P, ts, U, inst, F, st);
@@ -1088,6 +1105,20 @@ cudaError_t launch_ghost_layer(const ParamsT<T>& P, const T* U, double t, const 
     k_ghost_layer<T, E2D_RECON_CONSERVATIVE><<<grid, 256, 0, st>>>(P, U, t, base, out, nghost);
   return cudaGetLastError();
 }
+
+// PRE is empty to instantiate, `extern` to declare an instantiation made elsewhere
+#define E2D_RECON_LIM_DECL(PRE, T, LIM)                                                                           \
+  PRE template cudaError_t recon_lim<T, LIM>(const ParamsT<T>&, const int4* const*, const int*, int, bool,        \
+                                             const T*, const InstanceState*, FaceArraysT<T>, const DebugOutT<T>*, \
+                                             cudaStream_t, const TmaSet*);                                        \
+  PRE template cudaError_t recon_qp_lim<T, LIM>(const ParamsT<T>&, const TileSet&, const T*, const InstanceState*, \
+                                                FaceArraysT<T>, cudaStream_t);
+// the per-limiter launchers are instantiated elsewhere (e2d_recon_unit.cu)
+#define E2D_EXTERN_RECON_LIM(T)         \
+  E2D_RECON_LIM_DECL(extern, T, 0)      \
+  E2D_RECON_LIM_DECL(extern, T, 1)      \
+  E2D_RECON_LIM_DECL(extern, T, 2)      \
+  E2D_RECON_LIM_DECL(extern, T, 3)
 
 #define E2D_INSTANTIATE_STAGE_LAUNCHERS(T)                                                                       \
   template cudaError_t launch_reconstruct<T>(const ParamsT<T>&, const TileSet&, KernelChoice, const T*,          \

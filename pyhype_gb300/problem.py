@@ -256,7 +256,7 @@ def build_problem(
 
     ``sizes`` optionally gives per-block ``(nx, ny)`` (independent batched instances);
     otherwise every block uses ``nx, ny`` as the reference does
-    (``pyhype/solvers/base.py:472-482``).  ``geometries`` optionally supplies
+    (``pyhype/solvers/base.py:90-101``).  ``geometries`` optionally supplies
     precomputed block geometry (e.g. arrays recorded from another platform, whose
     libm may round arctan/cos differently in the last bit).
     """

@@ -1,6 +1,6 @@
 """``Euler2D``: the reference's solver API, running its time loop on the GPU.
 
-Same constructor and ``solve()`` as ``pyhype/solvers/Euler2D.py:212-382``:
+Same constructor and ``solve()`` as ``pyhype/solvers/Euler2D.py:46-216``:
 
 * construction resolves the mesh dictionary / generator, builds every block's
   geometry on the host and creates the device solver (``e2d_create``);
@@ -13,7 +13,7 @@ Same constructor and ``solve()`` as ``pyhype/solvers/Euler2D.py:212-382``:
   ``{base}/{name}/mesh/mesh_{x,y}_blk_{n}.npy`` (``pyhype/solvers/base.py:139-172``),
   including its numbering (directory ``k`` holds the state after ``k + 1`` steps);
 * an unrealizable state (rho <= 0 or E <= 0) raises ``RealizabilityException`` where
-  the reference logs and calls ``MPI.Abort`` (``Euler2D.py:310-318``).
+  the reference logs and calls ``MPI.Abort`` (``Euler2D.py:144-152``).
 
 All blocks share one GPU; there is no MPI layer (``distribute_blocks_to_processes``
 has nothing to distribute on one device).

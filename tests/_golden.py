@@ -87,7 +87,9 @@ def geometry(z, b: int):
     )
 
 
-def problem(z, precision: int = 0, reference_geometry: bool = True):
+def problem(z, precision: int = 0, reference_geometry: bool = True, flux=None, recon=None):
+    """The fixture's problem; ``flux`` / ``recon`` replace the recorded scheme choice
+    (cases the reference cannot run, compared with the oracle only)."""
     from pyhype_gb300.fluids import Air
     from pyhype_gb300.problem import build_problem
 
@@ -96,7 +98,7 @@ def problem(z, precision: int = 0, reference_geometry: bool = True):
     geos = {int(b): geometry(z, int(b)) for b in z["blk_ids"]} if reference_geometry else None
     return build_problem(
         mesh_dict(z), int(z["nx"]), int(z["ny"]),
-        flux=str(z["flux"]), limiter=str(z["limiter"]), recon=str(z["recon"]),
+        flux=flux or str(z["flux"]), limiter=str(z["limiter"]), recon=recon or str(z["recon"]),
         gamma=air.gamma(), gm1=air.gamma() - 1, cfl=float(z["cfl"]), fluid=air, precision=precision,
         geometries=geos, nqp=int(z["nqp"]) if "nqp" in z.files else 1,
     )

@@ -5,7 +5,7 @@ its source tree through the import shim in ``_refshim.py`` (identity ``njit``, a
 one-rank MPI world, stub plotting).  Each case builds an ``Euler2D`` solver with the
 reference's own ``SolverConfig``/mesh dictionaries/initial conditions, runs the
 reference's own step loop (``Solver.get_dt`` -> ``ExplicitRungeKutta.integrate`` ->
-``t += dt``; ``pyhype/solvers/Euler2D.py:361-376``) and records:
+``t += dt``; ``pyhype/solvers/Euler2D.py:175-216``) and records:
 
 * the initial conservative state of every block (after ``_pre_process_solve``),
 * the dt of every step and a fingerprint of the state after every step,

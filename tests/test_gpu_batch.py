@@ -30,6 +30,26 @@ def test_batched_fp64_equals_sequential_solves():
         assert np.array_equal(S.states()[0], batched[k]), f"instance {k}"
 
 
+def test_batched_fp64_equals_oracle_per_instance():
+    """Every instance of the batched FP64 run against the CPU oracle run of that
+    instance alone (its own CFL dt each step): time and state value for value."""
+    from oracle.oracle import Oracle
+    from pyhype_gb300.batch import EnsembleSolver, ensemble_problem, ensemble_state
+    from pyhype_gb300.time_marching import tableau
+
+    inst = _small_ensemble()
+    B = EnsembleSolver(inst, precision=0)
+    B.run(12)
+    tb, sb = B.device.instance_times()
+    batched = B.states()
+    a = tableau("SSPRK2")
+    for k, one in enumerate(inst):
+        P1 = ensemble_problem([one])
+        U, t, dts = Oracle(P1).run(ensemble_state(P1, [one]), a, 0.0, float("inf"), 12)
+        assert len(dts) == 12 and t == tb[k], f"instance {k}: t {tb[k]!r} vs oracle {t!r}"
+        assert np.array_equal(P1.from_soa(U)[0], batched[k]), f"instance {k}"
+
+
 def test_batched_fp32_close_to_fp64():
     from pyhype_gb300.batch import EnsembleSolver
 
