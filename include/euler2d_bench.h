@@ -21,8 +21,9 @@ E2D_API int e2d_bench_fp64_peak(int32_t op, double* tflops);
 /* Kernel times of `steps` device-loop steps (as e2d_run issues them), each launch
    bracketed by CUDA events on the handle's stream.  ms[k] receives the average
    duration of one launch of kernel class k and launches[k] the launch count:
-   0 = CFL dt, 1 = reconstruct, 2 = flux, 3 = update, 4 = step bookkeeping.     */
-#define E2D_BENCH_NK 5
+   0 = CFL dt, 1 = reconstruct, 2 = flux, 3 = update, 4 = step bookkeeping,
+   5 = fused stage (stages run by the fused stage kernel).                      */
+#define E2D_BENCH_NK 6
 E2D_API int e2d_bench_kernels(E2DHandle h, int32_t steps, double* ms, int64_t* launches);
 
 /* Cost of the halo: the reconstruction kernel (8-row tiles, default variant) forms
@@ -48,13 +49,17 @@ E2D_API int e2d_bench_set_tma(E2DHandle h, int32_t enable);
    kernel: 0 = reconstruct (variants 0..5: tile height x min CTAs per SM of (8,2),
    (8,1), (4,2), (4,4), (16,1), and (4,8) in the FP32 form, where the FP64 path
    runs variant 0), 1 = flux (variants 0..2: min CTAs per SM 4, 1, 6),
-   2 = update (variant 0).                                                       */
+   2 = update (variant 0), 3 = stage form (variant 0: the three kernels above per
+   stage; 1: one fused stage kernel per stage, tiles of 16 x 32 cells with their face
+   states and fluxes in shared memory; stages whose updates overwrite their own
+   input, and problems with several face quadrature points, stay split).          */
 E2D_API int e2d_set_kernel_choice(E2DHandle h, int32_t kernel, int32_t variant, int32_t persistent);
 /* Autotuner: times every variant and grid shape of the reconstruct and flux kernels
    and the grid shape of the update kernel on the current state (`reps` launches each,
-   CUDA events on the handle's stream), keeps the fastest and returns the choices in
-   chosen[0..5] = {reconstruct variant, persistent, flux variant, persistent, update
-   variant, persistent}.  Graphs captured before are dropped.                    */
+   CUDA events on the handle's stream), keeps the fastest, then compares one stage of
+   those three against one fused stage and keeps the faster form.  Returns the choices
+   in chosen[0..7] = {reconstruct variant, persistent, flux variant, persistent,
+   update variant, persistent, stage form, 0}.  Graphs captured before are dropped. */
 E2D_API int e2d_autotune(E2DHandle h, int32_t reps, int32_t* chosen);
 
 /* The bounded barrier wait of the reconstruction kernel's TMA tile staging, on its

@@ -172,10 +172,10 @@ class DeviceSolver:
 
     def autotune(self, reps: int = 3) -> dict:
         """Pick the fastest kernel variants on the current state (same results)."""
-        ch = np.zeros(6, dtype=np.int32)
+        ch = np.zeros(8, dtype=np.int32)
         _check(self.L.e2d_autotune(self.h, reps, ch.ctypes.data))
         return {"reconstruct": (int(ch[0]), bool(ch[1])), "flux": (int(ch[2]), bool(ch[3])),
-                "update": (int(ch[4]), bool(ch[5]))}
+                "update": (int(ch[4]), bool(ch[5])), "stage": (int(ch[6]), False)}
 
     def instance_times(self):
         n = max(1, self.problem.cfg.ninstances)

@@ -100,6 +100,15 @@ static int build_program(E2DSolver* h, int S, const double* a) {
       }
     }
   }
+  // A stage may run fused when none of its updates writes the buffer it reads as input
+  // (a fused tile would overwrite cells its neighbours still read as halo).  The FP32
+  // Kahan update writes buffer 0 (and the compensation).
+  h->fusable.assign(S, 1);
+  for (int s = 0; s < S; ++s)
+    for (int u = 0; u < h->prog[s].nupd; ++u) {
+      const StageUpdate& up = h->prog[s].upd[u];
+      if (up.dst == h->stage_input[s] || (up.kahan && h->stage_input[s] == 0)) h->fusable[s] = 0;
+    }
   h->nstages = S;
   return 0;
 }
@@ -130,22 +139,24 @@ static int build_tma_t(E2DSolver* h, const T* base) {
   const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return 0;
   const int nb = (int)h->hblocks.size();
-  const int heights[3] = {4, 8, 16};
+  // box rows: tile height + the 1-cell halo for the reconstruction kernel's tiles, and
+  // the fused stage kernel's 16 rows + its 2-cell halo
+  const int box_rows[4] = {4 + 2, 8 + 2, 16 + 2, FUSED_TY + 4};
   E2DSolver::TmaEntry entry{base, {}};
   std::vector<CUtensorMap> maps(nb);
   std::vector<int> ok(nb);
-  for (int r = 0; r < 3; ++r) {
+  for (int r = 0; r < 4; ++r) {
     for (int b = 0; b < nb; ++b) {
       const E2DBlock& B = h->hblocks[b];
       const uint64_t row = (uint64_t)B.nx * sizeof(T), plane = (uint64_t)h->ncell * sizeof(T);
       const T* addr = base + B.cell_offset;
       bool good = row % 16 == 0 && plane % 16 == 0 && (reinterpret_cast<uintptr_t>(addr) % 16) == 0 &&
-                  B.nx > TX && B.ny > heights[r];
+                  B.nx > TX && B.ny >= box_rows[r];
       std::memset(&maps[b], 0, sizeof(CUtensorMap));
       if (good) {
         const cuuint64_t dims[3] = {(cuuint64_t)B.nx, (cuuint64_t)B.ny, 4};
         const cuuint64_t strides[2] = {row, plane};
-        const cuuint32_t box[3] = {(cuuint32_t)TileCols<T>::TXW, (cuuint32_t)(heights[r] + 2), 4};
+        const cuuint32_t box[3] = {(cuuint32_t)TileCols<T>::TXW, (cuuint32_t)box_rows[r], 4};
         const cuuint32_t estr[3] = {1, 1, 1};
         const CUresult cr = enc(&maps[b], sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
                                 3, const_cast<T*>(addr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -313,6 +324,12 @@ static int bench_kernels_t(E2DHandle h, int32_t steps, double* ms, int64_t* laun
     CK(fin());
     for (int s = 0; s < h->nstages; ++s) {
       const T* in = p.S.buf[h->stage_input[s]];
+      if (h->use_fused(s)) {
+        CK(rec(5));
+        CK(launch_stage_fused<T>(p.P, h->ts, in, h->inst, p.S, h->prog[s], h->real, h->stream, h->tma_for(in), false));
+        CK(fin());
+        continue;
+      }
       CK(rec(1));
       CK(launch_reconstruct<T>(p.P, h->ts, h->kr, in, h->inst, p.F, nullptr, h->stream, h->tma_for(in)));
       CK(fin());
@@ -329,8 +346,8 @@ static int bench_kernels_t(E2DHandle h, int32_t steps, double* ms, int64_t* laun
     CK(fin());
   }
   CK(cudaStreamSynchronize(h->stream));
-  double tot[E2D_BENCH_NK] = {0, 0, 0, 0, 0};
-  int64_t cnt[E2D_BENCH_NK] = {0, 0, 0, 0, 0};
+  double tot[E2D_BENCH_NK] = {};
+  int64_t cnt[E2D_BENCH_NK] = {};
   for (size_t q = 0; q < cls.size(); ++q) {
     float t = 0.f;
     CK(cudaEventElapsedTime(&t, ev[2 * q], ev[2 * q + 1]));
@@ -435,7 +452,9 @@ static int time_kernel(E2DHandle h, int which, int reps, float* ms) {
     if (which == 0)
       CK(launch_reconstruct<T>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, nullptr, h->stream, h->tma_for(p.S.buf[0])));
     else if (which == 1) CK(launch_flux<T>(p.P, h->ts, h->kf, h->inst, p.F, nullptr, h->stream));
-    else CK(launch_update<T>(p.P, h->ts, h->ku, p.F, p.S, none, h->inst, h->real, nullptr, h->stream));
+    else if (which == 2) CK(launch_update<T>(p.P, h->ts, h->ku, p.F, p.S, none, h->inst, h->real, nullptr, h->stream));
+    else CK(launch_stage_fused<T>(p.P, h->ts, p.S.buf[0], h->inst, p.S, none, h->real, h->stream,
+                                  h->tma_for(p.S.buf[0]), false));
   }
   CK(cudaEventRecord(e1, h->stream));
   CK(cudaEventSynchronize(e1));
@@ -456,6 +475,7 @@ static int autotune_t(E2DHandle h, int reps, int32_t* chosen) {
   CK(launch_set_time(h->inst, ninst, 0.0, 0.0, h->stream));
   KernelChoice* ch[3] = {&h->kr, &h->kf, &h->ku};
   const int nvar[3] = {N_RECON_VARIANTS, N_FLUX_VARIANTS, 1};
+  float split_ms = 0.f;
   for (int which = 0; which < 3; ++which) {
     KernelChoice best = *ch[which];
     float best_ms = 1e30f;
@@ -474,6 +494,18 @@ static int autotune_t(E2DHandle h, int reps, int32_t* chosen) {
       chosen[2 * which] = best.variant;
       chosen[2 * which + 1] = best.persistent ? 1 : 0;
     }
+    split_ms += best_ms;
+  }
+  // the three tuned kernels of one stage against one fused stage (no updates either way)
+  h->ks = KernelChoice{0, false};
+  if (h->cfg.nqp <= 1) {
+    float fused_ms = 0.f;
+    if (int e = time_kernel<T>(h, 3, reps, &fused_ms)) return e;
+    if (fused_ms < split_ms) h->ks = KernelChoice{1, false};
+  }
+  if (chosen) {
+    chosen[6] = h->ks.variant;
+    chosen[7] = 0;
   }
   CK(cudaMemcpyAsync(h->inst, saved.data(), sizeof(InstanceState) * ninst, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -629,6 +661,12 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
     return bail(fail(E2D_ERR_CUDA, "counter init: %s", cudaGetErrorString(ce)));
 
   if (int e = E2D_DISPATCH(h, init_path)) return bail(e);
+  if ((ce = (h->prec == E2D_FP32 ? launch_stage_fused<float>(h->pf.P, h->ts, nullptr, h->inst, h->pf.S, StageProgram{},
+                                                             h->real, h->stream, nullptr, true)
+                                 : launch_stage_fused<double>(h->pd.P, h->ts, nullptr, h->inst, h->pd.S,
+                                                              StageProgram{}, h->real, h->stream, nullptr, true))) !=
+      cudaSuccess)
+    return bail(fail(E2D_ERR_CUDA, "fused stage kernel set-up: %s", cudaGetErrorString(ce)));
 
   // default integrator: the classical RK4 rows (explicit_runge_kutta.py:212-224)
   const double rk4[16] = {0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1, 0, 1.0 / 6, 1.0 / 3, 1.0 / 3, 1.0 / 6};
@@ -727,6 +765,10 @@ static int enqueue_stages(E2DHandle h, T* dudt_out, const DebugOutT<T>* dbg) {
   PathT<T>& p = path<T>(h);
   for (int s = 0; s < h->nstages; ++s) {
     const T* in = p.S.buf[h->stage_input[s]];
+    if (!dudt_out && !dbg && h->use_fused(s)) {
+      CK(launch_stage_fused<T>(p.P, h->ts, in, h->inst, p.S, h->prog[s], h->real, h->stream, h->tma_for(in), false));
+      continue;
+    }
     CK(launch_reconstruct<T>(p.P, h->ts, h->kr, in, h->inst, p.F, dbg, h->stream, h->tma_for(in)));
     CK(launch_flux<T>(p.P, h->ts, h->kf, h->inst, p.F, dbg, h->stream));
     CK(launch_update<T>(p.P, h->ts, h->ku, p.F, p.S, h->prog[s], h->inst, h->real, dudt_out,
@@ -1033,10 +1075,12 @@ int e2d_bench_halo(E2DHandle h, int32_t reps, double* ms, int64_t* ntiles) {
 
 int e2d_set_kernel_choice(E2DHandle h, int32_t kernel, int32_t variant, int32_t persistent) {
   if (!h) return fail(E2D_ERR_INVALID, "null handle");
-  const int nvar[3] = {N_RECON_VARIANTS, N_FLUX_VARIANTS, 1};
-  if (kernel < 0 || kernel > 2 || variant < 0 || variant >= nvar[kernel])
+  const int nvar[4] = {N_RECON_VARIANTS, N_FLUX_VARIANTS, 1, N_STAGE_FORMS};
+  if (kernel < 0 || kernel > 3 || variant < 0 || variant >= nvar[kernel])
     return fail(E2D_ERR_INVALID, "kernel %d has no variant %d", kernel, variant);
-  KernelChoice* ch[3] = {&h->kr, &h->kf, &h->ku};
+  if (kernel == 3 && variant == 1 && h->cfg.nqp > 1)
+    return fail(E2D_ERR_UNSUPPORTED, "the fused stage kernel has the one-point face rule only");
+  KernelChoice* ch[4] = {&h->kr, &h->kf, &h->ku, &h->ks};
   *ch[kernel] = KernelChoice{variant, persistent != 0};
   h->drop_graphs();
   return 0;

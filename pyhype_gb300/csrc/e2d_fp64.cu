@@ -1,11 +1,13 @@
 // e2d_fp64.cu - FP64 instantiation of the stage kernels (the bit-exact path; this
 // unit builds with -fmad=false so no multiply-add is contracted) and the
 // precision-independent step bookkeeping kernels.
-#include "e2d_stage.cuh"
+#include "e2d_fused.cuh"
 
 namespace e2d {
 
 E2D_EXTERN_RECON_LIM(double)
+E2D_EXTERN_FUSED_LIM(double)
+E2D_INSTANTIATE_FUSED_LAUNCHER(double)
 E2D_INSTANTIATE_STAGE_LAUNCHERS(double)
 
 // Step bookkeeping, one thread per instance.  begin: decide whether the instance

@@ -1,0 +1,341 @@
+// e2d_fused.cuh - the fused stage kernel: one launch per Runge-Kutta stage does what
+// k_reconstruct, k_flux and k_update do in three, with the face states and fluxes kept
+// in shared memory instead of face arrays in HBM (pyhype/fvm/base.py:108-190 for one
+// stage of every block, plus the stage's Butcher updates of
+// time_marching/explicit_runge_kutta.py:63-80).
+//
+// One CTA of 256 threads takes a tile of 16 rows x 32 columns of one block:
+//   staging   the tile and a 2-cell halo (20 x 36 cells, 4 planes) into shared memory:
+//             one TMA box load for tiles whose halo lies inside the block, plain loads
+//             with ghost cells formed on the fly (ghost_cons) for the others;
+//   faces     gradient and limiter of every tile cell and of the 96 cells of the ring
+//             around it (whose face states the tile's edge faces need); each tile cell
+//             writes its four limited face states, each ring cell the one facing the
+//             tile, rotated into the face frame and converted to primitive variables;
+//             block-boundary faces take their outside state from the boundary condition
+//             (outside_state), as in k_reconstruct;
+//   fluxes    one Riemann flux per face of the tile (528 vertical, 544 horizontal),
+//             rotated back and integrated, written over the face's left state;
+//   update    dUdt of every tile cell and the stage program (partial Butcher sums,
+//             Kahan-compensated last row on the FP32 path), positivity on the last stage.
+// Every value is computed by the same functions the split kernels use
+// (limit_cell_var, vface_prim/hface_prim, vface_flux/hface_flux, cell_dudt,
+// stage_program), so the two forms give the same results.
+//
+// The cost of fusion is the ring: gradient and limiter of 96 cells are computed by both
+// tiles that share them (19 % more reconstruction work at 32 x 16), and the 48 edge
+// faces of a tile by both tiles (4.5 % more fluxes).  What it saves is the face arrays'
+// round trip through HBM (four states and two fluxes per face) and two launches.
+//
+// A stage whose Butcher updates write its own input buffer (explicit Euler, a one-stage
+// tableau) cannot be fused: a tile would overwrite cells that its neighbours still read
+// as halo.  The host runs such stages split (E2DSolver::fusable).
+#pragma once
+#include "e2d_stage.cuh"
+
+namespace e2d {
+
+constexpr int FTY = FUSED_TY;   // tile rows (the tile table of height 16)
+constexpr int FTHREADS = 256;   // 8 warps
+static_assert(FTY == 16 && FTHREADS == 256, "the ring task mapping assumes 16 rows and 8 warps");
+
+template <typename T>
+struct FusedSmem {
+  // tile + 2-cell halo in reconstruction variables; block row i0 - 2 + r at row r,
+  // block column j0 - XO + c at column c (XO = 16 / sizeof(T), the TMA box's start)
+  T sW[4][FTY + 4][TileCols<T>::TXW];
+  // vertical face (row i0 + r, face column j0 + c): left / right primitive state in the
+  // face frame; after the flux phase vL holds the integrated flux
+  T vL[4][FTY][TX + 1];
+  T vR[4][FTY][TX + 1];
+  // horizontal face (face row i0 + r, column j0 + c)
+  T hL[4][FTY + 1][TX];
+  T hR[4][FTY + 1][TX];
+};
+
+template <typename T>
+__device__ __forceinline__ void put4(T (&a)[4][FTY][TX + 1], int r, int c, const T* w) {
+  a[0][r][c] = w[0]; a[1][r][c] = w[1]; a[2][r][c] = w[2]; a[3][r][c] = w[3];
+}
+template <typename T>
+__device__ __forceinline__ void put4(T (&a)[4][FTY + 1][TX], int r, int c, const T* w) {
+  a[0][r][c] = w[0]; a[1][r][c] = w[1]; a[2][r][c] = w[2]; a[3][r][c] = w[3];
+}
+
+enum { FACE_E = 1, FACE_W = 2, FACE_N = 4, FACE_S = 8 };
+
+// Gradient, limiter and the face states `which` of the cell at tile-local (lr, lc),
+// lr in [-1, FTY], lc in [-1, TX]; a tile cell (own = true) also writes the outside
+// states of its block-boundary faces.
+template <typename T, int LIM, int RECON>
+__device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G, const E2DBlock* B, FusedSmem<T>& sm,
+                                           int i0, int j0, int lr, int lc, int which, bool own, double t) {
+  constexpr int XO = TileCols<T>::XO;
+  const int i = i0 + lr, j = j0 + lc;
+  const int sr = lr + 2, sc = XO + lc;  // the cell's position in sW
+  CellGeo<T> g;
+  load_cell_geo(P, B, i, j, g);
+  T face[4][4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    T fv[4], gx, gy, ph;
+    limit_cell_var<T, LIM>(sm.sW[v][sr][sc], sm.sW[v][sr][sc - 1], sm.sW[v][sr][sc + 1], sm.sW[v][sr - 1][sc],
+                           sm.sW[v][sr + 1][sc], g, fv, gx, gy, ph);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) face[s][v] = fv[s];
+  }
+  const bool cart = B->is_cartesian != 0;
+  const int64_t fW = vf_at(B, i, j), fE = fW + 1;
+  const int64_t fS = hf_at(B, i, j), fN = fS + B->nx;
+  T w[4];
+  if (which & FACE_E) { vface_prim<T, RECON>(P, G, cart, fE, face[E2D_E], w); put4(sm.vL, lr, lc + 1, w); }
+  if (which & FACE_W) { vface_prim<T, RECON>(P, G, cart, fW, face[E2D_W], w); put4(sm.vR, lr, lc, w); }
+  if (which & FACE_N) { hface_prim<T, RECON>(P, G, cart, fN, face[E2D_N], w); put4(sm.hL, lr + 1, lc, w); }
+  if (which & FACE_S) { hface_prim<T, RECON>(P, G, cart, fS, face[E2D_S], w); put4(sm.hR, lr, lc, w); }
+  if (!own) return;
+  // outside states of block-boundary faces (the ghost cell is staged next to the cell)
+  if (j == 0) {
+    const T gr[4] = {sm.sW[0][sr][sc - 1], sm.sW[1][sr][sc - 1], sm.sW[2][sr][sc - 1], sm.sW[3][sr][sc - 1]};
+    T o[4];
+    outside_state(P, B, E2D_W, i, t, gr, face[E2D_W], o);
+    vface_prim<T, RECON>(P, G, cart, fW, o, w);
+    put4(sm.vL, lr, lc, w);
+  }
+  if (j == B->nx - 1) {
+    const T gr[4] = {sm.sW[0][sr][sc + 1], sm.sW[1][sr][sc + 1], sm.sW[2][sr][sc + 1], sm.sW[3][sr][sc + 1]};
+    T o[4];
+    outside_state(P, B, E2D_E, i, t, gr, face[E2D_E], o);
+    vface_prim<T, RECON>(P, G, cart, fE, o, w);
+    put4(sm.vR, lr, lc + 1, w);
+  }
+  if (i == 0) {
+    const T gr[4] = {sm.sW[0][sr - 1][sc], sm.sW[1][sr - 1][sc], sm.sW[2][sr - 1][sc], sm.sW[3][sr - 1][sc]};
+    T o[4];
+    outside_state(P, B, E2D_S, j, t, gr, face[E2D_S], o);
+    hface_prim<T, RECON>(P, G, cart, fS, o, w);
+    put4(sm.hL, lr, lc, w);
+  }
+  if (i == B->ny - 1) {
+    const T gr[4] = {sm.sW[0][sr + 1][sc], sm.sW[1][sr + 1][sc], sm.sW[2][sr + 1][sc], sm.sW[3][sr + 1][sc]};
+    T o[4];
+    outside_state(P, B, E2D_N, j, t, gr, face[E2D_N], o);
+    hface_prim<T, RECON>(P, G, cart, fN, o, w);
+    put4(sm.hR, lr + 1, lc, w);
+  }
+}
+
+template <typename T, int LIM, int RECON, int FLUX, int MINB>
+__global__ void __launch_bounds__(FTHREADS, MINB)
+    k_stage_fused(ParamsT<T> P, const int4* __restrict__ tiles, const T* __restrict__ U,
+                  InstanceState* __restrict__ inst, StateBuffersT<T> S, StageProgram prog,
+                  RealizState* __restrict__ real, TmaTiles tma) {
+  extern __shared__ __align__(128) unsigned char e2d_fused_smem[];
+  FusedSmem<T>& sm = *reinterpret_cast<FusedSmem<T>*>(e2d_fused_smem);
+  __shared__ __align__(8) unsigned long long bar;
+  constexpr int XO = TileCols<T>::XO;
+  const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
+  const int4 tl = tiles[blockIdx.x];
+  const E2DBlock* B = P.blocks + tl.x;
+  const InstanceState* I = inst + B->instance;
+  if (!I->active) return;  // uniform over the CTA
+  const double t = I->t;
+  const int nx = B->nx, ny = B->ny;
+  const int i0 = tl.y, j0 = tl.z;
+  // the halo lies inside the block: no ghost cell is staged and every ring cell is real
+  const bool interior = i0 >= 2 && j0 >= 2 && i0 + FTY + 2 <= ny && j0 + TX + 2 <= nx;
+
+  // ---- staging ---------------------------------------------------------------------
+  if (interior && tma.maps != nullptr && tma.ok[tl.x]) {
+    if (threadIdx.x == 0) {
+      mbar_init(&bar);
+      tma_load_box(&sm.sW[0][0][0], &tma.maps[tl.x], j0 - XO, i0 - 2, 0, &bar, (unsigned)sizeof(sm.sW));
+    }
+    __syncthreads();  // the barrier is initialised before anyone waits on it
+    if (!__syncthreads_and(mbar_wait(&bar, 0))) {
+      // the wait ran out: report it and drop the tile (the host fails the step); wait once
+      // more, as long again, so that the CTA does not exit while the copy is landing
+      if (threadIdx.x == 0) atomicAdd(tma.timeouts, 1ULL);
+      __syncthreads_and(mbar_wait(&bar, 0));
+      return;
+    }
+    if (RECON == E2D_RECON_PRIMITIVE) {  // conversion in place, one thread per staged cell
+      for (int p = threadIdx.x; p < (FTY + 4) * (TX + 4); p += FTHREADS) {
+        const int ly = p / (TX + 4), lx = p - ly * (TX + 4);
+        const int c = XO - 2 + lx;
+        T q[4] = {sm.sW[0][ly][c], sm.sW[1][ly][c], sm.sW[2][ly][c], sm.sW[3][ly][c]}, r[4];
+        to_recon<RECON>(q, G, r);
+        sm.sW[0][ly][c] = r[0]; sm.sW[1][ly][c] = r[1]; sm.sW[2][ly][c] = r[2]; sm.sW[3][ly][c] = r[3];
+      }
+    }
+  } else {
+    for (int p = threadIdx.x; p < (FTY + 4) * (TX + 4); p += FTHREADS) {
+      const int ly = p / (TX + 4), lx = p - ly * (TX + 4);
+      const int gi = i0 + ly - 2, gj = j0 + lx - 2;
+      T q[4], r[4] = {T(0), T(0), T(0), T(0)};
+      if (interior) {
+        load_cell(U, P.ncell, cell_at(B, gi, gj), q);
+        to_recon<RECON>(q, G, r);
+      } else {
+        const bool in_i = gi >= 0 && gi < ny, in_j = gj >= 0 && gj < nx;
+        bool ok = true;
+        if (in_i && in_j) load_cell(U, P.ncell, cell_at(B, gi, gj), q);
+        else if (in_i && gj == -1) ghost_cons(P, B, E2D_W, gi, U, t, q);
+        else if (in_i && gj == nx) ghost_cons(P, B, E2D_E, gi, U, t, q);
+        else if (in_j && gi == -1) ghost_cons(P, B, E2D_S, gj, U, t, q);
+        else if (in_j && gi == ny) ghost_cons(P, B, E2D_N, gj, U, t, q);
+        else ok = false;
+        if (ok) to_recon<RECON>(q, G, r);
+      }
+      const int c = XO - 2 + lx;
+      sm.sW[0][ly][c] = r[0]; sm.sW[1][ly][c] = r[1]; sm.sW[2][ly][c] = r[2]; sm.sW[3][ly][c] = r[3];
+    }
+  }
+  __syncthreads();
+
+  // ---- face states: tile rows, then the ring (S row, N row, W and E columns) ---------
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int task = warp; task < FTY + 3; task += FTHREADS / 32) {
+    if (task < FTY) {
+      if (i0 + task < ny && j0 + lane < nx)
+        fused_cell<T, LIM, RECON>(P, G, B, sm, i0, j0, task, lane, FACE_E | FACE_W | FACE_N | FACE_S, true, t);
+    } else if (task == FTY) {
+      if (i0 >= 1 && j0 + lane < nx) fused_cell<T, LIM, RECON>(P, G, B, sm, i0, j0, -1, lane, FACE_N, false, t);
+    } else if (task == FTY + 1) {
+      if (i0 + FTY < ny && j0 + lane < nx)
+        fused_cell<T, LIM, RECON>(P, G, B, sm, i0, j0, FTY, lane, FACE_S, false, t);
+    } else {
+      const int r = lane & 15;
+      if (lane < 16) {
+        if (j0 >= 1 && i0 + r < ny) fused_cell<T, LIM, RECON>(P, G, B, sm, i0, j0, r, -1, FACE_E, false, t);
+      } else {
+        if (j0 + TX < nx && i0 + r < ny) fused_cell<T, LIM, RECON>(P, G, B, sm, i0, j0, r, TX, FACE_W, false, t);
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- one flux per face of the tile ------------------------------------------------
+  {
+    const bool cart = B->is_cartesian != 0;
+    const DebugOutT<T> none{};
+    constexpr int NV = FTY * (TX + 1), NH = (FTY + 1) * TX;
+    for (int item = threadIdx.x; item < NV + NH; item += FTHREADS) {
+      if (item < NV) {
+        const int r = item / (TX + 1), c = item - r * (TX + 1);
+        if (i0 + r < ny && j0 + c <= nx) {
+          const int64_t f = vf_at(B, i0 + r, j0 + c);
+          const T L[4] = {sm.vL[0][r][c], sm.vL[1][r][c], sm.vL[2][r][c], sm.vL[3][r][c]};
+          const T R[4] = {sm.vR[0][r][c], sm.vR[1][r][c], sm.vR[2][r][c], sm.vR[3][r][c]};
+          T Iv[4];
+          vface_flux<T, FLUX, false>(P, G, cart, f, L, R, Iv, none);
+          put4(sm.vL, r, c, Iv);
+        }
+      } else {
+        const int h = item - NV;
+        const int r = h / TX, c = h - r * TX;
+        if (i0 + r <= ny && j0 + c < nx) {
+          const int64_t f = hf_at(B, i0 + r, j0 + c);
+          const T L[4] = {sm.hL[0][r][c], sm.hL[1][r][c], sm.hL[2][r][c], sm.hL[3][r][c]};
+          const T R[4] = {sm.hR[0][r][c], sm.hR[1][r][c], sm.hR[2][r][c], sm.hR[3][r][c]};
+          T Iv[4];
+          hface_flux<T, FLUX, false>(P, G, cart, f, L, R, Iv, none);
+          put4(sm.hL, r, c, Iv);
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- dUdt and the stage program of every tile cell --------------------------------
+  int nbad = 0;
+#pragma unroll
+  for (int round = 0; round < FTY / (FTHREADS / 32); ++round) {
+    const int r = warp + round * (FTHREADS / 32);
+    const int i = i0 + r, j = j0 + lane;
+    bool bad = false;
+    if (i < ny && j < nx) {
+      const int64_t c = cell_at(B, i, j);
+      const T A = P.geo.cell[E2D_G_A][c];
+      T k[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) k[v] = cell_dudt(sm.vL[v][r][lane], sm.vL[v][r][lane + 1], sm.hL[v][r][lane],
+                                                   sm.hL[v][r + 1][lane], A);
+      stage_program(P, S, prog, I->dt, c, k);
+      if (prog.final_stage) {
+        const T rho = S.buf[0][c], E = S.buf[0][3 * P.ncell + c];
+        bad = !(rho > T(0)) || !(E > T(0));
+        if (bad) atomicMin(&real->first, ((unsigned long long)tl.x << 40) | (unsigned long long)(c - B->cell_offset));
+      }
+    }
+    if (prog.final_stage) nbad += __syncthreads_count(bad);
+  }
+  if (prog.final_stage && threadIdx.x == 0 && nbad) {
+    atomicAdd(&real->nbad, (unsigned long long)nbad);
+    atomicAdd(&inst[B->instance].nbad, nbad);  // halts this instance only
+  }
+}
+
+// ---- launchers --------------------------------------------------------------------------
+template <typename T, int LIM, int RECON, int FLUX>
+static cudaError_t fused_launch(const ParamsT<T>& P, const TileSet& ts, const T* U, InstanceState* inst,
+                                StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
+                                const TmaSet* tset, bool prepare_only) {
+  constexpr int MINB = sizeof(T) == 4 ? 4 : 2;  // 64 / 128 registers per thread
+  auto kern = k_stage_fused<T, LIM, RECON, FLUX, MINB>;
+  constexpr int bytes = (int)sizeof(FusedSmem<T>);
+  if (prepare_only) return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  const TmaTiles tma = tset ? tset->by_rty[3] : TmaTiles{nullptr, nullptr, nullptr};
+  kern<<<ts.ncell[2], FTHREADS, bytes, st>>>(P, ts.cell[2], U, inst, S, prog, real, tma);
+  return cudaGetLastError();
+}
+
+template <typename T, int LIM>
+cudaError_t fused_lim(const ParamsT<T>& P, const TileSet& ts, const T* U, InstanceState* inst, StateBuffersT<T> S,
+                      const StageProgram& prog, RealizState* real, cudaStream_t st, const TmaSet* tma,
+                      bool prepare_only) {
+#define E2D_FUSED_FLUX(RC)                                                                                          \
+  switch (P.flux) {                                                                                                 \
+    case E2D_FLUX_HLLL: return fused_launch<T, LIM, RC, E2D_FLUX_HLLL>(P, ts, U, inst, S, prog, real, st, tma, prepare_only); \
+    case E2D_FLUX_HLLE: return fused_launch<T, LIM, RC, E2D_FLUX_HLLE>(P, ts, U, inst, S, prog, real, st, tma, prepare_only); \
+    default: return fused_launch<T, LIM, RC, E2D_FLUX_ROE>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);   \
+  }
+  if (P.recon == E2D_RECON_PRIMITIVE) {
+    E2D_FUSED_FLUX(E2D_RECON_PRIMITIVE)
+  }
+  E2D_FUSED_FLUX(E2D_RECON_CONSERVATIVE)
+#undef E2D_FUSED_FLUX
+}
+
+#define E2D_FUSED_LIM_DECL(PRE, T, LIM)                                                                           \
+  PRE template cudaError_t fused_lim<T, LIM>(const ParamsT<T>&, const TileSet&, const T*, InstanceState*,         \
+                                             StateBuffersT<T>, const StageProgram&, RealizState*, cudaStream_t,   \
+                                             const TmaSet*, bool);
+#define E2D_EXTERN_FUSED_LIM(T)    \
+  E2D_FUSED_LIM_DECL(extern, T, 0) \
+  E2D_FUSED_LIM_DECL(extern, T, 1) \
+  E2D_FUSED_LIM_DECL(extern, T, 2) \
+  E2D_FUSED_LIM_DECL(extern, T, 3)
+
+// One stage (one-point face rule) in one launch; prepare_only sets the kernel's shared
+// memory limit and launches nothing (done once when a handle is created, outside any
+// stream capture).
+template <typename T>
+cudaError_t launch_stage_fused(const ParamsT<T>& P, const TileSet& ts, const T* U, InstanceState* inst,
+                               StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
+                               const TmaSet* tma, bool prepare_only) {
+  if (ts.ncell[2] <= 0) return cudaSuccess;
+  switch (P.limiter) {
+    case E2D_LIM_BARTH_JESPERSEN:
+      return fused_lim<T, E2D_LIM_BARTH_JESPERSEN>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);
+    case E2D_LIM_VAN_ALBADA: return fused_lim<T, E2D_LIM_VAN_ALBADA>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);
+    case E2D_LIM_VAN_LEER: return fused_lim<T, E2D_LIM_VAN_LEER>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);
+    default: return fused_lim<T, E2D_LIM_VENKATAKRISHNAN>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);
+  }
+}
+
+#define E2D_INSTANTIATE_FUSED_LAUNCHER(T)                                                                        \
+  template cudaError_t launch_stage_fused<T>(const ParamsT<T>&, const TileSet&, const T*, InstanceState*,         \
+                                             StateBuffersT<T>, const StageProgram&, RealizState*, cudaStream_t,  \
+                                             const TmaSet*, bool);
+
+}  // namespace e2d

@@ -12,6 +12,7 @@ namespace e2d {
 constexpr int TX = 32;        // cell tile width  (one warp along x)
 constexpr int TY = 8;         // cell tile height
 constexpr int MAX_STAGES = 8;
+constexpr int FUSED_TY = 16;  // tile rows of the fused stage kernel (e2d_fused.cuh)
 
 // Device view of the geometry planes (in the arithmetic type of the path).
 template <typename T>
@@ -146,9 +147,10 @@ struct TileCols {
   static constexpr int TXW = TX + 2 * XO;
   static constexpr int C0 = XO - 1;
 };
-// the three tile heights (4, 8, 16) of one state buffer
+// the three tile heights (4, 8, 16) of one state buffer, and the fused stage kernel's
+// box (16 rows and a 2-cell halo: 20 rows) at index 3
 struct TmaSet {
-  TmaTiles by_rty[3];
+  TmaTiles by_rty[4];
 };
 
 // Kernel variant chosen by the autotuner (0 = default) and persistent-grid flag.
@@ -158,6 +160,7 @@ struct KernelChoice {
 };
 constexpr int N_RECON_VARIANTS = 6;  // (tile height, min CTAs/SM): (8,2) (8,1) (4,2) (4,4) (16,1), (4,8) FP32 only
 constexpr int N_FLUX_VARIANTS = 3;   // min CTAs/SM: 4, 1, 6
+constexpr int N_STAGE_FORMS = 2;     // 0: three kernels per stage, 1: the fused stage kernel
 
 // launchers, instantiated for double (e2d_fp64.cu) and float (e2d_fp32.cu)
 template <typename T>
@@ -183,6 +186,12 @@ cudaError_t launch_totals(const ParamsT<T>& P, const int4* tiles, int n, const T
 template <typename T>
 cudaError_t launch_ghost_layer(const ParamsT<T>& P, const T* U, double t, const int64_t* base, double* out,
                                int64_t nghost, int maxlen, cudaStream_t st);
+// one RK stage in one launch (e2d_fused.cuh); prepare_only sets the kernel's shared
+// memory limit on the current device and launches nothing
+template <typename T>
+cudaError_t launch_stage_fused(const ParamsT<T>& P, const TileSet& ts, const T* U, InstanceState* inst,
+                               StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
+                               const TmaSet* tma, bool prepare_only);
 cudaError_t launch_begin_step(InstanceState* inst, int ninst, double cfl, int use_min, cudaStream_t st);
 cudaError_t launch_end_step(InstanceState* inst, int ninst, const RealizState* real, cudaStream_t st);
 cudaError_t launch_set_time(InstanceState* inst, int ninst, double t, double dt, cudaStream_t st);

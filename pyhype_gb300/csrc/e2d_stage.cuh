@@ -149,6 +149,188 @@ __device__ __forceinline__ void outside_state(const ParamsT<T>& P, const E2DBloc
 }
 
 // --------------------------------------------------------------------------------------
+// Per-cell and per-face pieces shared by the split stage kernels (k_reconstruct, k_flux,
+// k_update) and the fused stage kernel (e2d_fused.cuh), so both forms evaluate the same
+// expressions.
+// --------------------------------------------------------------------------------------
+
+// Geometry one cell's reconstruction reads: L cos and L sin of its four faces, 1/A and
+// the face points' offsets from the centroid (E, W, N, S).
+template <typename T>
+struct CellGeo {
+  T LcE, LsE, LcW, LsW, LcN, LsN, LcS, LsS, ia;
+  T hx[4], hy[4];
+};
+
+template <typename T>
+__device__ __forceinline__ void load_cell_geo(const ParamsT<T>& P, const E2DBlock* B, int i, int j, CellGeo<T>& g) {
+  const int64_t c = cell_at(B, i, j);
+  const int64_t fW = vf_at(B, i, j), fE = fW + 1;
+  const int64_t fS = hf_at(B, i, j), fN = fS + B->nx;
+  g.LcE = P.geo.vface[E2D_F_LC][fE]; g.LsE = P.geo.vface[E2D_F_LS][fE];
+  g.LcW = P.geo.vface[E2D_F_LC][fW]; g.LsW = P.geo.vface[E2D_F_LS][fW];
+  g.LcN = P.geo.hface[E2D_F_LC][fN]; g.LsN = P.geo.hface[E2D_F_LS][fN];
+  g.LcS = P.geo.hface[E2D_F_LC][fS]; g.LsS = P.geo.hface[E2D_F_LS][fS];
+  g.ia = P.geo.cell[E2D_G_INV_A][c];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    g.hx[s] = P.geo.cell[E2D_G_HX_E + s][c];
+    g.hy[s] = P.geo.cell[E2D_G_HY_E + s][c];
+  }
+}
+
+// Green-Gauss gradient, limiter value and the limited face states fv (E, W, N, S) of
+// one variable at one cell from its five-point stencil (reconstruction variables).
+template <typename T, int LIM>
+__device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, const CellGeo<T>& g, T (&fv)[4],
+                                               T& gx_out, T& gy_out, T& ph_out) {
+  // interface averages (quad_block.py:181-218) and Green-Gauss (greengauss.py:137-155)
+  const T ie = half(w0 + ea), iw = half(we + w0);
+  const T in = half(w0 + no), is = half(so + w0);
+  const T gx = (ie * g.LcE + iw * (-g.LcW) + in * g.LcN + is * (-g.LcS)) * g.ia;
+  const T gy = (ie * g.LsE + iw * (-g.LsW) + in * g.LsN + is * (-g.LsS)) * g.ia;
+  // limiter (limiters/base.py:47-221)
+  const T dmax = vmax(vmax(vmax(vmax(w0, we), ea), so), no) - w0;
+  const T dmin = vmin(vmin(vmin(vmin(w0, we), ea), so), no) - w0;
+  T hot[4];
+  T ph = T(0);
+  if constexpr (sizeof(T) == 8) {
+    // FP64: psi only at the faces that decide the minimum (e2d_slope_pick.cuh); all
+    // four when the pick cannot rule a face out.  Same expressions, same phi.
+    double davg[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      hot[s] = gx * g.hx[s] + gy * g.hy[s];
+      davg[s] = (w0 + hot[s]) - w0;
+    }
+    const SlopePick k = pick_slopes<LIM>(dmax, dmin, davg);
+    if (k.ok) {
+      ph = psi_s<LIM>(k.ga ? qdiv(k.na, k.da) : T(1));
+      if (k.second) ph = vmin(ph, psi_s<LIM>(k.gb ? qdiv(k.nb, k.db) : T(1)));
+    } else {
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        const bool pos = is_pos(davg[s]), neg = is_neg(davg[s]);
+        const T p = psi_s<LIM>((pos || neg) ? qdiv(pos ? dmax : dmin, davg[s]) : T(1));
+        ph = (s == 0) ? p : vmin(ph, p);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      hot[s] = gx * g.hx[s] + gy * g.hy[s];
+      // FP64's round trip (w0 + hot) - w0 is hot itself unless |hot| is below half
+      // an FP64 ulp of w0, where it is zero and the slope takes its davg == 0
+      // branch (psi(1)).  In FP32 the same round trip would zero every |hot| below
+      // 2^-25 |w0| and switch branches where the FP64 path does not, so the FP32 form
+      // applies the FP64 threshold, 2^-53 times the power of two of w0.
+      const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
+      const T davg = (fabs(hot[s]) < half_ulp64) ? T(0) : hot[s];
+      // slope dmax/davg (davg > 0), dmin/davg (davg < 0), 1 (davg == 0), with a single
+      // division so lanes of different signs share one division sequence; a zero davg
+      // divides nothing
+      const bool pos = is_pos(davg), neg = is_neg(davg);
+      const T sl = (pos || neg) ? qdiv(pos ? dmax : dmin, davg) : T(1);
+      const T p = psi_s<LIM>(sl);
+      ph = (s == 0) ? p : vmin(ph, p);
+    }
+  }
+  ph = is_neg(ph) ? T(0) : ph;
+#pragma unroll
+  for (int s = 0; s < 4; ++s) fv[s] = w0 + ph * hot[s];
+  gx_out = gx;
+  gy_out = gy;
+  ph_out = ph;
+}
+
+// A face state (reconstruction variables) rotated into the frame of vertical face f
+// and converted to primitive variables (fvm/base.py:327-390).
+template <typename T, int RECON>
+__device__ __forceinline__ void vface_prim(const ParamsT<T>& P, const Gas<T>& G, bool cart, int64_t f, const T* in,
+                                           T* w) {
+  T q[4] = {in[0], in[1], in[2], in[3]};
+  if (!cart) rotate(q, P.geo.vface[E2D_F_COS][f], P.geo.vface[E2D_F_SIN][f]);
+  recon_to_prim<RECON>(q, G, w);
+}
+// the same for horizontal face f (the y sweep in the x frame, fvm/base.py:392-486)
+template <typename T, int RECON>
+__device__ __forceinline__ void hface_prim(const ParamsT<T>& P, const Gas<T>& G, bool cart, int64_t f, const T* in,
+                                           T* w) {
+  T q[4] = {in[0], in[1], in[2], in[3]};
+  if (cart) rotate90(q);
+  else rotate(q, P.geo.hface[E2D_F_COS][f], P.geo.hface[E2D_F_SIN][f]);
+  recon_to_prim<RECON>(q, G, w);
+}
+
+// Riemann flux of vertical face f in its frame, rotated back and integrated with the
+// one-point rule (I = L * 2 F); DBG records the raw and rotated-back fluxes.
+template <typename T, int FLUX, bool DBG>
+__device__ __forceinline__ void vface_flux(const ParamsT<T>& P, const Gas<T>& G, bool cart, int64_t f, const T* L,
+                                           const T* R, T* I, const DebugOutT<T>& dbg) {
+  T Fx[4];
+  riemann<FLUX>(L, R, G, Fx);
+  if (DBG && dbg.vflux_raw) store4(dbg.vflux_raw, P.nvface, f, Fx);
+  if (!cart) unrotate(Fx, P.geo.vface[E2D_F_COS][f], P.geo.vface[E2D_F_SIN][f]);
+  if (DBG && dbg.vflux) store4(dbg.vflux, P.nvface, f, Fx);
+  const T len = P.geo.vface[E2D_F_L][f];
+  I[0] = len * twice(Fx[0]); I[1] = len * twice(Fx[1]); I[2] = len * twice(Fx[2]); I[3] = len * twice(Fx[3]);
+}
+template <typename T, int FLUX, bool DBG>
+__device__ __forceinline__ void hface_flux(const ParamsT<T>& P, const Gas<T>& G, bool cart, int64_t f, const T* L,
+                                           const T* R, T* I, const DebugOutT<T>& dbg) {
+  T Fy[4];
+  riemann<FLUX>(L, R, G, Fy);
+  if (DBG && dbg.hflux_raw) store4(dbg.hflux_raw, P.nhface, f, Fy);
+  if (cart) unrotate90(Fy);
+  else unrotate(Fy, P.geo.hface[E2D_F_COS][f], P.geo.hface[E2D_F_SIN][f]);
+  if (DBG && dbg.hflux) store4(dbg.hflux, P.nhface, f, Fy);
+  const T len = P.geo.hface[E2D_F_L][f];
+  I[0] = len * twice(Fy[0]); I[1] = len * twice(Fy[1]); I[2] = len * twice(Fy[2]); I[3] = len * twice(Fy[3]);
+}
+
+// dUdt of one variable of a cell from its integrated face fluxes and area
+// (fvm/base.py:171-190): 0.5 * (((I_W - I_E) + I_S) - I_N) / A.
+template <typename T>
+__device__ __forceinline__ T cell_dudt(T IW, T IE, T IS, T IN, T A) {
+  return qdiv(half(IW - IE + IS - IN), A);
+}
+
+// The RK stage program at cell c: every partial Butcher sum this stage contributes
+// to, dst = src + (dt a) k, or on the FP32 path the last row's increment added to U^n
+// with Kahan compensation carried across steps.
+template <typename T>
+__device__ __forceinline__ void stage_program(const ParamsT<T>& P, const StateBuffersT<T>& S, const StageProgram& prog,
+                                              double dt, int64_t c, const T* k) {
+#pragma unroll
+  for (int u = 0; u < MAX_STAGES; ++u) {  // unrolled: the program is read from kernel parameters
+    if (u >= prog.nupd) break;
+    const StageUpdate& up = prog.upd[u];
+    const T* src = S.at(up.src);
+    const T dta = T(dt * up.a);
+    if (!up.kahan) {
+      T* dst = S.at(up.dst);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const T base = up.src_zero ? T(0) : src[v * P.ncell + c];
+        dst[v * P.ncell + c] = base + dta * k[v];
+      }
+    } else {
+      // U^{n+1} = U^n + increment with Kahan compensation carried across steps
+      T* U0 = S.buf[0];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const T inc = (up.src_zero ? T(0) : src[v * P.ncell + c]) + dta * k[v];
+        const T y = inc - S.comp[v * P.ncell + c];
+        const T u0 = U0[v * P.ncell + c];
+        const T tt = u0 + y;
+        S.comp[v * P.ncell + c] = (tt - u0) - y;
+        U0[v * P.ncell + c] = tt;
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------------------------------
 // K1: reconstruction
 // --------------------------------------------------------------------------------------
 
@@ -239,80 +421,17 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
   const int64_t c = cell_at(B, i, j);
   const int64_t fE = vf_at(B, i, j + 1), fW = vf_at(B, i, j);
   const int64_t fN = hf_at(B, i + 1, j), fS = hf_at(B, i, j);
-  const T LcE = P.geo.vface[E2D_F_LC][fE], LsE = P.geo.vface[E2D_F_LS][fE];
-  const T LcW = P.geo.vface[E2D_F_LC][fW], LsW = P.geo.vface[E2D_F_LS][fW];
-  const T LcN = P.geo.hface[E2D_F_LC][fN], LsN = P.geo.hface[E2D_F_LS][fN];
-  const T LcS = P.geo.hface[E2D_F_LC][fS], LsS = P.geo.hface[E2D_F_LS][fS];
-  const T ia = P.geo.cell[E2D_G_INV_A][c];
-  T hx[4], hy[4];
-#pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    hx[s] = P.geo.cell[E2D_G_HX_E + s][c];
-    hy[s] = P.geo.cell[E2D_G_HY_E + s][c];
-  }
+  CellGeo<T> g;
+  load_cell_geo(P, B, i, j, g);
 
   T face[4][4];  // [side][var] limited face states, reconstruction variables
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
-    const T w0 = sW[v][ty + 1][C0 + tx + 1];
-    const T we = sW[v][ty + 1][C0 + tx];
-    const T ea = sW[v][ty + 1][C0 + tx + 2];
-    const T so = sW[v][ty][C0 + tx + 1];
-    const T no = sW[v][ty + 2][C0 + tx + 1];
-    // interface averages (quad_block.py:181-218) and Green-Gauss (greengauss.py:137-155)
-    const T ie = half(w0 + ea), iw = half(we + w0);
-    const T in = half(w0 + no), is = half(so + w0);
-    const T gx = (ie * LcE + iw * (-LcW) + in * LcN + is * (-LcS)) * ia;
-    const T gy = (ie * LsE + iw * (-LsW) + in * LsN + is * (-LsS)) * ia;
-    // limiter (limiters/base.py:47-221)
-    const T dmax = vmax(vmax(vmax(vmax(w0, we), ea), so), no) - w0;
-    const T dmin = vmin(vmin(vmin(vmin(w0, we), ea), so), no) - w0;
-    T hot[4];
-    T ph = T(0);
-    if constexpr (sizeof(T) == 8) {
-      // FP64: psi only at the faces that decide the minimum (e2d_slope_pick.cuh); all
-      // four when the pick cannot rule a face out.  Same expressions, same phi.
-      double davg[4];
+    T fv[4], gx, gy, ph;
+    limit_cell_var<T, LIM>(sW[v][ty + 1][C0 + tx + 1], sW[v][ty + 1][C0 + tx], sW[v][ty + 1][C0 + tx + 2],
+                           sW[v][ty][C0 + tx + 1], sW[v][ty + 2][C0 + tx + 1], g, fv, gx, gy, ph);
 #pragma unroll
-      for (int s = 0; s < 4; ++s) {
-        hot[s] = gx * hx[s] + gy * hy[s];
-        davg[s] = (w0 + hot[s]) - w0;
-      }
-      const SlopePick k = pick_slopes<LIM>(dmax, dmin, davg);
-      if (k.ok) {
-        ph = psi_s<LIM>(k.ga ? qdiv(k.na, k.da) : T(1));
-        if (k.second) ph = vmin(ph, psi_s<LIM>(k.gb ? qdiv(k.nb, k.db) : T(1)));
-      } else {
-#pragma unroll
-        for (int s = 0; s < 4; ++s) {
-          const bool pos = is_pos(davg[s]), neg = is_neg(davg[s]);
-          const T p = psi_s<LIM>((pos || neg) ? qdiv(pos ? dmax : dmin, davg[s]) : T(1));
-          ph = (s == 0) ? p : vmin(ph, p);
-        }
-      }
-    } else {
-#pragma unroll
-      for (int s = 0; s < 4; ++s) {
-        hot[s] = gx * hx[s] + gy * hy[s];
-        // FP64's round trip (w0 + hot) - w0 is hot itself unless |hot| is below half
-        // an FP64 ulp of w0, where it is zero and the slope takes its davg == 0
-        // branch (psi(1)).  In FP32 the same round trip would zero every |hot| below
-        // 2^-25 |w0| and switch branches where the FP64 path does not, so the FP32 form
-        // applies the FP64 threshold, 2^-53 times the power of two of w0.
-        const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
-        const T davg = (fabs(hot[s]) < half_ulp64) ? T(0) : hot[s];
-        // slope dmax/davg (davg > 0), dmin/davg (davg < 0), 1 (davg == 0), with a single
-        // division so lanes of different signs share one division sequence; a zero davg
-        // divides nothing
-        const bool pos = is_pos(davg), neg = is_neg(davg);
-        const T sl = (pos || neg) ? qdiv(pos ? dmax : dmin, davg) : T(1);
-        const T p = psi_s<LIM>(sl);
-        ph = (s == 0) ? p : vmin(ph, p);
-      }
-    }
-    ph = is_neg(ph) ? T(0) : ph;
-#pragma unroll
-    for (int s = 0; s < 4; ++s) face[s][v] = w0 + ph * hot[s];
+    for (int s = 0; s < 4; ++s) face[s][v] = fv[s];
     if (DBG) {
       if (dbg.gx) dbg.gx[v * P.ncell + c] = gx;
       if (dbg.gy) dbg.gy[v * P.ncell + c] = gy;
@@ -321,72 +440,45 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
   }
 
   const bool cart = B->is_cartesian != 0;
-  // east face of this cell = left state of vertical face j+1
-  {
-    T q[4] = {face[E2D_E][0], face[E2D_E][1], face[E2D_E][2], face[E2D_E][3]}, w[4];
-    if (!cart) rotate(q, P.geo.vface[E2D_F_COS][fE], P.geo.vface[E2D_F_SIN][fE]);
-    recon_to_prim<RECON>(q, G, w);
-    store4(F.vL, P.nvface, fE, w);
-  }
-  // west face = right state of vertical face j
-  {
-    T q[4] = {face[E2D_W][0], face[E2D_W][1], face[E2D_W][2], face[E2D_W][3]}, w[4];
-    if (!cart) rotate(q, P.geo.vface[E2D_F_COS][fW], P.geo.vface[E2D_F_SIN][fW]);
-    recon_to_prim<RECON>(q, G, w);
-    store4(F.vR, P.nvface, fW, w);
-  }
-  // north face = left state of horizontal face i+1 (y sweep in the x frame)
-  {
-    T q[4] = {face[E2D_N][0], face[E2D_N][1], face[E2D_N][2], face[E2D_N][3]}, w[4];
-    if (cart) rotate90(q);
-    else rotate(q, P.geo.hface[E2D_F_COS][fN], P.geo.hface[E2D_F_SIN][fN]);
-    recon_to_prim<RECON>(q, G, w);
-    store4(F.hL, P.nhface, fN, w);
-  }
-  // south face = right state of horizontal face i
-  {
-    T q[4] = {face[E2D_S][0], face[E2D_S][1], face[E2D_S][2], face[E2D_S][3]}, w[4];
-    if (cart) rotate90(q);
-    else rotate(q, P.geo.hface[E2D_F_COS][fS], P.geo.hface[E2D_F_SIN][fS]);
-    recon_to_prim<RECON>(q, G, w);
-    store4(F.hR, P.nhface, fS, w);
-  }
+  T w[4];
+  vface_prim<T, RECON>(P, G, cart, fE, face[E2D_E], w);  // east face = left state of vertical face j+1
+  store4(F.vL, P.nvface, fE, w);
+  vface_prim<T, RECON>(P, G, cart, fW, face[E2D_W], w);  // west face = right state of vertical face j
+  store4(F.vR, P.nvface, fW, w);
+  hface_prim<T, RECON>(P, G, cart, fN, face[E2D_N], w);  // north face = left state of horizontal face i+1
+  store4(F.hL, P.nhface, fN, w);
+  hface_prim<T, RECON>(P, G, cart, fS, face[E2D_S], w);  // south face = right state of horizontal face i
+  store4(F.hR, P.nhface, fS, w);
   // outside states of block-boundary faces
   if (!edge) return;
   if (j == 0) {
     const T gr[4] = {sW[0][ty + 1][C0 + tx], sW[1][ty + 1][C0 + tx], sW[2][ty + 1][C0 + tx], sW[3][ty + 1][C0 + tx]};
-    T o[4], w[4];
+    T o[4];
     outside_state(P, B, E2D_W, i, t, gr, face[E2D_W], o);
-    if (!cart) rotate(o, P.geo.vface[E2D_F_COS][fW], P.geo.vface[E2D_F_SIN][fW]);
-    recon_to_prim<RECON>(o, G, w);
+    vface_prim<T, RECON>(P, G, cart, fW, o, w);
     store4(F.vL, P.nvface, fW, w);
   }
   if (j == nx - 1) {
     const T gr[4] = {sW[0][ty + 1][C0 + tx + 2], sW[1][ty + 1][C0 + tx + 2], sW[2][ty + 1][C0 + tx + 2],
-                      sW[3][ty + 1][C0 + tx + 2]};
-    T o[4], w[4];
+                     sW[3][ty + 1][C0 + tx + 2]};
+    T o[4];
     outside_state(P, B, E2D_E, i, t, gr, face[E2D_E], o);
-    if (!cart) rotate(o, P.geo.vface[E2D_F_COS][fE], P.geo.vface[E2D_F_SIN][fE]);
-    recon_to_prim<RECON>(o, G, w);
+    vface_prim<T, RECON>(P, G, cart, fE, o, w);
     store4(F.vR, P.nvface, fE, w);
   }
   if (i == 0) {
     const T gr[4] = {sW[0][ty][C0 + tx + 1], sW[1][ty][C0 + tx + 1], sW[2][ty][C0 + tx + 1], sW[3][ty][C0 + tx + 1]};
-    T o[4], w[4];
+    T o[4];
     outside_state(P, B, E2D_S, j, t, gr, face[E2D_S], o);
-    if (cart) rotate90(o);
-    else rotate(o, P.geo.hface[E2D_F_COS][fS], P.geo.hface[E2D_F_SIN][fS]);
-    recon_to_prim<RECON>(o, G, w);
+    hface_prim<T, RECON>(P, G, cart, fS, o, w);
     store4(F.hL, P.nhface, fS, w);
   }
   if (i == ny - 1) {
     const T gr[4] = {sW[0][ty + 2][C0 + tx + 1], sW[1][ty + 2][C0 + tx + 1], sW[2][ty + 2][C0 + tx + 1],
-                      sW[3][ty + 2][C0 + tx + 1]};
-    T o[4], w[4];
+                     sW[3][ty + 2][C0 + tx + 1]};
+    T o[4];
     outside_state(P, B, E2D_N, j, t, gr, face[E2D_N], o);
-    if (cart) rotate90(o);
-    else rotate(o, P.geo.hface[E2D_F_COS][fN], P.geo.hface[E2D_F_SIN][fN]);
-    recon_to_prim<RECON>(o, G, w);
+    hface_prim<T, RECON>(P, G, cart, fN, o, w);
     store4(F.hR, P.nhface, fN, w);
   }
 }
@@ -651,27 +743,16 @@ __device__ __forceinline__ void flux_tile(const ParamsT<T>& P, const int4 tl, co
     const int64_t f = vf_at(B, i, j);
     T L[4] = {F.vL[f], F.vL[P.nvface + f], F.vL[2 * P.nvface + f], F.vL[3 * P.nvface + f]};
     T R[4] = {F.vR[f], F.vR[P.nvface + f], F.vR[2 * P.nvface + f], F.vR[3 * P.nvface + f]};
-    T Fx[4];
-    riemann<FLUX>(L, R, G, Fx);
-    if (DBG && dbg.vflux_raw) store4(dbg.vflux_raw, P.nvface, f, Fx);
-    if (!cart) unrotate(Fx, P.geo.vface[E2D_F_COS][f], P.geo.vface[E2D_F_SIN][f]);
-    if (DBG && dbg.vflux) store4(dbg.vflux, P.nvface, f, Fx);
-    const T len = P.geo.vface[E2D_F_L][f];
-    T I[4] = {len * twice(Fx[0]), len * twice(Fx[1]), len * twice(Fx[2]), len * twice(Fx[3])};
+    T I[4];
+    vface_flux<T, FLUX, DBG>(P, G, cart, f, L, R, I, dbg);
     store4(F.vI, P.nvface, f, I);
   }
   if (j < nx) {
     const int64_t f = hf_at(B, i, j);
     T L[4] = {F.hL[f], F.hL[P.nhface + f], F.hL[2 * P.nhface + f], F.hL[3 * P.nhface + f]};
     T R[4] = {F.hR[f], F.hR[P.nhface + f], F.hR[2 * P.nhface + f], F.hR[3 * P.nhface + f]};
-    T Fy[4];
-    riemann<FLUX>(L, R, G, Fy);
-    if (DBG && dbg.hflux_raw) store4(dbg.hflux_raw, P.nhface, f, Fy);
-    if (cart) unrotate90(Fy);
-    else unrotate(Fy, P.geo.hface[E2D_F_COS][f], P.geo.hface[E2D_F_SIN][f]);
-    if (DBG && dbg.hflux) store4(dbg.hflux, P.nhface, f, Fy);
-    const T len = P.geo.hface[E2D_F_L][f];
-    T I[4] = {len * twice(Fy[0]), len * twice(Fy[1]), len * twice(Fy[2]), len * twice(Fy[3])};
+    T I[4];
+    hface_flux<T, FLUX, DBG>(P, G, cart, f, L, R, I, dbg);
     store4(F.hI, P.nhface, f, I);
   }
 }
@@ -710,43 +791,14 @@ __device__ __forceinline__ void update_tile(const ParamsT<T>& P, const int4 tl, 
     const T A = P.geo.cell[E2D_G_A][c];
     T k[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const T IW = F.vI[v * P.nvface + fW], IE = F.vI[v * P.nvface + fE];
-      const T IS = F.hI[v * P.nhface + fS], IN = F.hI[v * P.nhface + fN];
-      k[v] = qdiv(half(IW - IE + IS - IN), A);
-    }
+    for (int v = 0; v < 4; ++v)
+      k[v] = cell_dudt(F.vI[v * P.nvface + fW], F.vI[v * P.nvface + fE], F.hI[v * P.nhface + fS],
+                       F.hI[v * P.nhface + fN], A);
     if (dudt_out) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) dudt_out[v * P.ncell + c] = k[v];
     }
-    const double dt = I->dt;
-#pragma unroll
-    for (int u = 0; u < MAX_STAGES; ++u) {  // unrolled: the program is read from kernel parameters
-      if (u >= prog.nupd) break;
-      const StageUpdate& up = prog.upd[u];
-      const T* src = S.at(up.src);
-      const T dta = T(dt * up.a);
-      if (!up.kahan) {
-        T* dst = S.at(up.dst);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const T base = up.src_zero ? T(0) : src[v * P.ncell + c];
-          dst[v * P.ncell + c] = base + dta * k[v];
-        }
-      } else {
-        // U^{n+1} = U^n + increment with Kahan compensation carried across steps
-        T* U0 = S.buf[0];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const T inc = (up.src_zero ? T(0) : src[v * P.ncell + c]) + dta * k[v];
-          const T y = inc - S.comp[v * P.ncell + c];
-          const T u0 = U0[v * P.ncell + c];
-          const T tt = u0 + y;
-          S.comp[v * P.ncell + c] = (tt - u0) - y;
-          U0[v * P.ncell + c] = tt;
-        }
-      }
-    }
+    stage_program(P, S, prog, I->dt, c, k);
     if (prog.final_stage) {
       const T rho = S.buf[0][c], E = S.buf[0][3 * P.ncell + c];
       bad = !(rho > T(0)) || !(E > T(0));

@@ -109,7 +109,7 @@ def test_run_stops_at_t_final():
     assert np.array_equal(S.get_state(), Ut)
 
 
-@pytest.mark.parametrize("kernel,variants", [(0, range(6)), (1, range(3)), (2, range(1))])
+@pytest.mark.parametrize("kernel,variants", [(0, range(6)), (1, range(3)), (2, range(1)), (3, range(2))])
 @pytest.mark.parametrize("persistent", [False, True])
 def test_kernel_variants_bitwise(kernel, variants, persistent):
     """Every autotuner variant (tile height, occupancy target, persistent grid)
@@ -128,6 +128,6 @@ def test_autotuned_run_bitwise():
     P, S = _solver(z)
     S.set_state(P.to_soa(list(z["ic"])))
     choice = S.autotune(reps=2)
-    assert set(choice) == {"reconstruct", "flux", "update"}
+    assert set(choice) == {"reconstruct", "flux", "update", "stage"}
     t, steps = S.run(0.0, G.t_final(z), max_steps=10)
     assert G.fingerprint(P.from_soa(S.get_state())) == str(z["fingerprints"][9])
