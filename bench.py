@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--skip-ensemble", action="store_true", help="omit the batched-ensemble section")
     ap.add_argument("--skip-adjoint", action="store_true", help="omit the adjoint section")
     ap.add_argument("--skip-dmr", action="store_true", help="omit the double-Mach-reflection section")
+    ap.add_argument("--stage-form", default="default", choices=["default", "split", "fused"],
+                    help="stage form of the --precision fp32 profiling run")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
                     help="arithmetic of the timed multiblock run (fp32: the FP32 form; for profiling)")
     ap.add_argument("--workload", default="multiblock",
@@ -631,8 +633,8 @@ def main():
     import torch
 
     from pyhype_gb300 import _native
-    from pyhype_gb300.roofline import (BYTES_PER_CELL_STAGE_FP64, FP64_INST_PER_CELL, FP64_INST_PER_SM_CLOCK,
-                                       kernel_flops)
+    from pyhype_gb300.roofline import (BYTES_PER_CELL_STAGE_FP32, BYTES_PER_CELL_STAGE_FP64, FP64_INST_PER_CELL,
+                                       FP64_INST_PER_SM_CLOCK, kernel_flops)
 
     torch.cuda.set_device(local)
     solver, cfg = make_solver(args.n)
@@ -640,6 +642,8 @@ def main():
     P = solver.problem
     if args.precision == "fp32":  # the FP32 form alone (profiling runs; the default line is FP64)
         S32 = _native.DeviceSolver(P.with_precision(1), tableau=solver._time_integrator.tableau())
+        if args.stage_form != "default":
+            S32.set_kernel_choice(3, 1 if args.stage_form == "fused" else 0)
         S32.set_state(P.to_soa([b.state.data for b in solver.blocks]))
         t32, _ = S32.run(0.0, 1e30, max_steps=args.warmup)
         g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -697,12 +701,12 @@ def main():
     nbytes = 4 * P.ncell * 8
 
     # per-kernel event timing + measured FP64 rate -> roofline of the dominant kernel
-    kms = np.zeros(5)
-    kcnt = np.zeros(5, dtype=np.int64)
+    kms = np.zeros(6)
+    kcnt = np.zeros(6, dtype=np.int64)
     code = L.e2d_bench_kernels(dev.h, 2, kms.ctypes.data, kcnt.ctypes.data)
     if code != 0:
         raise RuntimeError(L.e2d_last_error().decode())
-    names = ["dt", "reconstruct", "flux", "update", "bookkeeping"]
+    names = ["dt", "reconstruct", "flux", "update", "bookkeeping", "fused_stage"]
     share = kms * kcnt
     dom = int(np.argmax(share))
     # inter-block halo: reconstruction over the real tiles against the same number of
@@ -747,20 +751,50 @@ def main():
     step_ms = ms / args.steps
     hbm_achieved = P.ncell * stages * BYTES_PER_CELL_STAGE_FP64 / (step_ms * 1e-3) / 1e9
 
-    # FP32 form on the same workload and seeded state (same warm-up + timed steps)
+    # FP64 fused stage form on the same workload (for comparison; the line's value is
+    # the default form)
+    fp64_fused = None
+    try:
+        SF = _native.DeviceSolver(P, tableau=solver._time_integrator.tableau())
+        SF.set_stream(stream.cuda_stream)
+        SF.set_kernel_choice(3, 1)
+        SF.set_state(P.to_soa([b.state.data for b in solver.blocks]))
+        tf_, _ = SF.run(0.0, t_final, max_steps=args.warmup)
+        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        h0.record(stream)
+        SF.run(tf_, t_final, max_steps=args.steps)
+        h1.record(stream)
+        torch.cuda.synchronize()
+        fms = h0.elapsed_time(h1) / args.steps
+        fp64_fused = {"ms_per_step": fms, "value": P.ncell * stages / (fms * 1e-3),
+                      "speedup_vs_split": step_ms / fms}
+        SF.close()
+    except Exception as exc:
+        fp64_fused = {"error": str(exc)}
+
+    # FP32 form on the same workload and seeded state (same warm-up + timed steps), both
+    # stage forms; the faster one is the form's number
     fp32 = None
     try:
-        S32 = _native.DeviceSolver(P.with_precision(1), tableau=solver._time_integrator.tableau())
-        S32.set_stream(stream.cuda_stream)
-        S32.set_state(P.to_soa([b.state.data for b in solver.blocks]))
-        t32, _ = S32.run(0.0, t_final, max_steps=args.warmup)
-        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        g0.record(stream)
-        t32, _ = S32.run(t32, t_final, max_steps=args.steps)
-        g1.record(stream)
-        torch.cuda.synchronize()
-        ms32 = max_over_ranks(g0.elapsed_time(g1), ws)
-        U32 = S32.get_state()
+        forms = {}
+        for form, name in ((0, "split"), (1, "fused")):
+            S32 = _native.DeviceSolver(P.with_precision(1), tableau=solver._time_integrator.tableau())
+            S32.set_stream(stream.cuda_stream)
+            S32.set_kernel_choice(3, form)
+            S32.set_state(P.to_soa([b.state.data for b in solver.blocks]))
+            t32, _ = S32.run(0.0, t_final, max_steps=args.warmup)
+            g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            g0.record(stream)
+            t32, _ = S32.run(t32, t_final, max_steps=args.steps)
+            g1.record(stream)
+            torch.cuda.synchronize()
+            forms[name] = (max_over_ranks(g0.elapsed_time(g1), ws), S32.get_state(), S32)
+        best = min(forms, key=lambda k: forms[k][0])
+        ms32, U32, S32 = forms[best]
+        forms_equal = bool(np.array_equal(forms["split"][1], forms["fused"][1]))
+        for k, v in forms.items():
+            if k != best:
+                v[2].close()
         # the FP64 solver has taken e2e steps more; rerun FP64 to the same step count
         S64b = _native.DeviceSolver(P, tableau=solver._time_integrator.tableau())
         S64b.set_stream(stream.cuda_stream)
@@ -780,14 +814,23 @@ def main():
             "note": "FP64 sums of A*U; the 2x4 layout is not conservative across blocks (the reference's "
                     "inter-block faces), so the drift includes the scheme's own"}
         # per-kernel timing advances the FP32 state further: after the comparison
-        k32 = np.zeros(5)
-        c32 = np.zeros(5, dtype=np.int64)
+        k32 = np.zeros(6)
+        c32 = np.zeros(6, dtype=np.int64)
         L.e2d_bench_kernels(S32.h, 2, k32.ctypes.data, c32.ctypes.data)
+        b32 = BYTES_PER_CELL_STAGE_FP32
+        ach32 = P.ncell * stages * b32 / (ms32 / args.steps * 1e-3) / 1e9
         fp32 = {"value": ws * P.ncell * stages * args.steps / (ms32 * 1e-3), "unit": "cell-stage updates/s",
-                "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": ms / ms32,
+                "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": ms / ms32, "stage_form": best,
+                "forms_ms_per_step": {k: v[0] / args.steps for k, v in forms.items()},
+                "forms_bitwise_equal": forms_equal,
                 "l1_density_rel_vs_fp64": l1, "l1_after_steps": args.warmup + args.steps,
                 "conservation": conservation,
-                "kernel_ms": {n: float(x) for n, x in zip(names, k32)}}
+                "kernel_ms": {n: float(x) for n, x in zip(names, k32)},
+                "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": ach32 / hbm_peak, "bytes_per_cell_stage": b32,
+                             "note": "whole-step algorithmic bytes (stage program state values, geometry, "
+                                     "CFL dt; pyhype_gb300/roofline.py) / ms per step; peak "
+                                     + ("MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback")}}
         S32.close()
         S64b.close()
     except Exception as exc:
@@ -869,6 +912,7 @@ def main():
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"},
         },
         "fp32": fp32,
+        "fp64_fused_stage": fp64_fused,
         "ensemble": ensemble,
         "adjoint": adjoint,
         "dmr": dmr,

@@ -44,12 +44,62 @@ FP64_INST_PER_CELL = {"reconstruct": 432, "flux": 407, "update": 63}
 # peak that ncu's FP64 pipe utilisation is relative to).
 FP64_INST_PER_SM_CLOCK = 2
 
-# Algorithmic HBM bytes per cell-stage of the whole stage (state reads/writes and
-# geometry of the cell and its two owned faces), FP64, RK4 low-storage average:
-# U_s 32 + U^n 32 + accumulator read+write 64 + U_{s+1} 32 + geometry 64 (A, 1/A and
-# 8 quadrature offsets ... counted once per cell).  Face-array traffic between the
-# three kernels and halo re-reads are implementation overhead, not counted.
-BYTES_PER_CELL_STAGE_FP64 = 224
+# Geometry planes a stage reads once per cell: A, 1/A, the 8 face-point offsets, and
+# of the two faces the cell owns (its west and south faces) L, L cos, L sin, cos, sin.
+GEOMETRY_PLANES_PER_CELL = 2 + 8 + 2 * 5
+
+
+def stage_state_values(tableau, kahan: bool) -> list:
+    """State values (of 4 variables) one RK stage must read and write per cell, per
+    stage, as the stage program of the C ABI forms them (e2d_api.cu build_program):
+    the stage input, then per Butcher update its source (U^n, or the row's partial
+    sum once started; the input is counted once when the source is the input) and
+    destination; with Kahan compensation (the FP32 form) the last row's update reads
+    and writes U^n and its compensation.  Values of every buffer are 4 per cell."""
+    import numpy as np
+
+    a = np.asarray(tableau, dtype=float)
+    S = a.shape[0]
+    row_buf = lambda r: S if r == S - 1 else r + 1  # noqa: E731
+    started = [False] * S
+    out = []
+    inp = 0
+    for s in range(S):
+        if s > 0:
+            inp = row_buf(s - 1) if any(a[s - 1, j] != 0.0 for j in range(s)) else 0
+        n = 1  # the stage input
+        for r in range(s, S):
+            c = a[r, s]
+            if c == 0.0:
+                continue
+            src = row_buf(r) if started[r] else 0
+            zero = kahan and r == S - 1 and not started[r]
+            if not zero and src != inp:
+                n += 1  # read the source
+            if kahan and r == S - 1 and s == S - 1:
+                n += 4  # U^n and compensation, read and written
+            else:
+                n += 1  # write the destination
+            started[r] = True
+        out.append(4 * n)
+    return out
+
+
+def bytes_per_cell_stage(tableau, elem: int, kahan: bool) -> float:
+    """Algorithmic HBM bytes per cell-stage of a whole step: the stage program's state
+    values, the geometry planes once per cell and stage, and the CFL dt's state and
+    two geometry planes once per step, averaged over the stages.  Face states, fluxes
+    and halo re-reads are implementation traffic, not counted."""
+    vals = stage_state_values(tableau, kahan)
+    S = len(vals)
+    per_stage = sum(vals) / S + GEOMETRY_PLANES_PER_CELL
+    return elem * (per_stage + 6.0 / S)
+
+
+# the benchmark's RK4: FP64 128 + 160 + 12 = 300 B, FP32 form (Kahan) 76 + 80 + 6 = 162 B
+_RK4 = [[0.5, 0, 0, 0], [0, 0.5, 0, 0], [0, 0, 1, 0], [1 / 6, 1 / 3, 1 / 3, 1 / 6]]
+BYTES_PER_CELL_STAGE_FP64 = bytes_per_cell_stage(_RK4, 8, False)
+BYTES_PER_CELL_STAGE_FP32 = bytes_per_cell_stage(_RK4, 4, True)
 
 
 def kernel_flops(kind: str, ncell: int, nvface: int, nhface: int) -> float:
