@@ -465,6 +465,55 @@ def adjoint_section(stream, nsteps: int = 400, ckpt: int = 20, n: int = 256, fd:
     return out
 
 
+def adjoint_dmr_section(stream, nsteps: int = 200, ckpt: int = 20):
+    """Adjoint at the double-Mach size: 5 blocks x 400 x 500 cells, HLLL, primitive
+    reconstruction, SSP-RK2 at CFL 0.4 from the double-Mach initial state; J = sum dt *
+    pressure integral along the south side of the middle block (the reflecting wall).
+    Times the recorded forward pass, the reverse pass and a plain forward run of the
+    same steps."""
+    import torch
+
+    from pyhype_gb300.adjoint import AdjointSolver
+    from pyhype_gb300.configs import double_mach
+    from pyhype_gb300.solvers import Euler2D
+
+    cfg, gen = double_mach()
+    sim = Euler2D(cfg, gen, precision="fp64")
+    sim._pre_process_solve()
+    U0 = torch.from_numpy(sim.device.get_state()).cuda()
+    P = sim.problem
+    sim.device.close()
+    A = AdjointSolver(P, "SSPRK2", block=2, side="S", nsteps=nsteps, ckpt_every=ckpt)
+    A.device.set_stream(stream.cuda_stream)
+    A.forward(U0)  # first-touch allocations of the checkpoint and segment storage
+    A.backward()
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    e0, e1, e2, f0, f1 = ev(), ev(), ev(), ev(), ev()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    J = A.forward(U0)
+    e1.record(stream)
+    g = A.backward()
+    e2.record(stream)
+    A.device.set_state_device(U0.data_ptr())
+    f0.record(stream)
+    A.device.run(0.0, float("inf"), max_steps=nsteps)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    t_plain = f0.elapsed_time(f1)
+    out = {"workload": f"double-Mach reflection 5 x 400x500 cells, HLLL/Venkatakrishnan, primitive reconstruction, "
+                       f"SSP-RK2, CFL 0.4, {nsteps} steps, checkpoints every {ckpt}; J = sum dt * south-wall "
+                       "pressure integral of the middle block",
+           "J": J, "forward_recorded_ms": e0.elapsed_time(e1), "backward_ms": e1.elapsed_time(e2),
+           "plain_forward_ms": t_plain, "adjoint_cost_over_forward": e1.elapsed_time(e2) / t_plain,
+           "grad_finite": bool(torch.isfinite(g).all().item())}
+    A.device.close()
+    return out
+
+
 def adjoint_study(limiters=("Venkatakrishnan", "BarthJespersen"), steps=(100, 200, 400), n: int = 256):
     """Central differences of J against the reverse pass, for several step counts and
     difference steps h, on the adjoint configuration off its symmetry point
@@ -504,9 +553,11 @@ def dmr_section(stream, sensitivity: bool = False):
     """Mach-10 double-Mach reflection: [0,4] x [0,1] as 5 blocks of 400 x 500 cells
     (dx = dy = 0.002), HLLL/Venkatakrishnan/Green-Gauss, primitive reconstruction,
     SSP-RK2 at CFL 0.4 to t = 0.2, FP64 and FP32 through Euler2D; FP32 L1 density
-    difference at t_final.  With ``sensitivity`` also an FP64 run whose initial
-    densities and energies are one ulp larger (the FP64 scheme's own round-off
-    sensitivity beside the FP32 difference)."""
+    difference at t_final.  With ``sensitivity`` also FP64 runs (i) whose initial
+    densities and energies are one ulp larger, (ii) from the initial state rounded to
+    FP32 once, (iii) on the geometry planes rounded to FP32 once: the FP64 scheme's own
+    response to the perturbations that any FP32 representation makes, beside the FP32
+    form's difference."""
     import numpy as np
     import torch
 
@@ -518,9 +569,24 @@ def dmr_section(stream, sensitivity: bool = False):
     states = {}
     totals = {}
     start = None
-    for prec in ("fp64", "fp32") + (("fp64_ulp",) if sensitivity else ()):
+    runs = ("fp64", "fp32") + (("fp64_ulp", "fp64_state32", "fp64_geometry32") if sensitivity else ())
+    for prec in runs:
         cfg, gen = double_mach()
         sim = Euler2D(cfg, gen, precision=prec[:4])
+        if prec == "fp64_geometry32":
+            # the FP64 path on the geometry planes rounded to FP32 once (the FP32 form's
+            # geometry, nothing else rounded): round the host planes, upload again
+            from pyhype_gb300._native import DeviceSolver
+
+            Pr = sim.problem
+            g = Pr.geometry
+            planes = [(g.cell[q], Pr.ncell) for q in range(12)]
+            planes += [(g.vface[q], Pr.nvface) for q in range(5)] + [(g.hface[q], Pr.nhface) for q in range(5)]
+            for ptr, n in planes:
+                arr = np.ctypeslib.as_array(ptr, shape=(n,))
+                arr[:] = arr.astype(np.float32).astype(np.float64)
+            sim.device.close()
+            sim.device = DeviceSolver(Pr, tableau=sim._time_integrator.tableau())
         sim.device.set_stream(stream.cuda_stream)
         sim._pre_process_solve()
         if prec == "fp64":
@@ -530,6 +596,8 @@ def dmr_section(stream, sensitivity: bool = False):
             U[0] = np.nextafter(U[0], np.inf)
             U[3] = np.nextafter(U[3], np.inf)
             sim.device.set_state(U)
+        if prec == "fp64_state32":  # the initial state rounded to FP32 once, FP64 after
+            sim.device.set_state(sim.device.get_state().astype(np.float32).astype(np.float64))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
@@ -547,8 +615,12 @@ def dmr_section(stream, sensitivity: bool = False):
     a, b = states["fp64"], states["fp32"]
     out["fp32_l1_density_rel_vs_fp64"] = float(np.sum(np.abs(b - a)) / np.sum(np.abs(a)))
     if sensitivity:
-        out["fp64_one_ulp_initial_change_l1_density"] = float(np.sum(np.abs(states["fp64_ulp"] - a)) / np.sum(np.abs(a)))
-        out.pop("fp64_ulp", None)
+        l1 = lambda k: float(np.sum(np.abs(states[k] - a)) / np.sum(np.abs(a)))  # noqa: E731
+        out["fp64_one_ulp_initial_change_l1_density"] = l1("fp64_ulp")
+        out["fp64_initial_state_rounded_to_fp32_l1_density"] = l1("fp64_state32")
+        out["fp64_geometry_rounded_to_fp32_l1_density"] = l1("fp64_geometry32")
+        for k in ("fp64_ulp", "fp64_state32", "fp64_geometry32"):
+            out.pop(k, None)
     # inflow and outflow sides: the totals are not conserved; FP32 against FP64 at t_final
     out["fp32_totals_rel_vs_fp64"] = {
         "mass": float(abs(totals["fp32"][0] - totals["fp64"][0]) / abs(totals["fp64"][0])),
@@ -851,6 +923,7 @@ def main():
             a32 = adjoint_section(stream, fd=False, precision="fp32")
             adjoint["fp32"] = {k: a32[k] for k in ("J", "backward_ms", "plain_forward_ms",
                                                    "adjoint_cost_over_forward")}
+            adjoint["double_mach_hlll"] = adjoint_dmr_section(stream)
         except Exception as exc:
             adjoint = {"error": str(exc)}
 

@@ -265,10 +265,13 @@ E2D_API int e2d_ghost_layer(E2DHandle h, double t, double* ghosts_dev);
 
 /* ---- adjoint (reverse mode) -------------------------------------------------------
    No counterpart in the reference (it has no differentiation); the forward steps are
-   the functions above.  Roe flux, one instance, one face quadrature point; FP64 or
-   FP32 path, any limiter, reconstruction type, side kind and explicit tableau.  Subgradients: min/max take the
-   operand the forward selects, Harten's fix the branch taken, the slope's davg == 0
-   branch is constant, a clipped negative limiter value passes nothing back.        */
+   the functions above.  Roe, HLLL or HLLE flux, one instance, one face quadrature
+   point; FP64 or FP32 path, any limiter, reconstruction type, side kind and explicit
+   tableau.  Subgradients: min/max take the operand the forward selects (the wave-speed
+   bounds of HLLL/HLLE included), Harten's fix and the HLL branches the branch taken,
+   HLLL's alpha = max(0, 1 - |r|/k) nothing where it is 0, a norm nothing at a zero
+   vector, the slope's davg == 0 branch is constant, a clipped negative limiter value
+   passes nothing back.                                                             */
 
 /* Objective J = sum over steps n of dt_n * P(U^{n+1}), where P(U) sums, over the cells
    along side `side` (e2d_side) of block `block`, the cell pressure times the length

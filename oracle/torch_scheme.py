@@ -6,7 +6,7 @@ autograd through this transcription gives the reference gradient that
 
 It restates the residual and RK stepping of the reference's FP64 path for a single
 block whose sides are Reflection, OutletDirichlet or copy sides (no inter-block
-halos), Roe flux, any of the four limiters, conservative or primitive
+halos), Roe, HLLL or HLLE flux, any of the four limiters, conservative or primitive
 reconstruction, in the reference's operation order so that every value (and hence
 every min/max/branch selection) equals the CUDA path's:
 
@@ -18,6 +18,8 @@ every min/max/branch selection) equals the CUDA path's:
     face / boundary states        pyhype/fvm/SecondOrderMUSCL.py:106-126, fvm/base.py:255-325
     Roe flux + Harten fix         pyhype/flux/Roe.py:175-304, flux/base.py:119-146,
                                   flux/eigen_system.py:150-252, states/primitive.py:223-320
+    HLLL / HLLE                   pyhype/flux/HLLL.py:25-103, flux/HLLE.py:22-47 (the norm
+                                  as an exactly rounded FMA chain, as numpy/OpenBLAS)
     dUdt                          pyhype/fvm/base.py:108-190
     RK stages                     pyhype/time_marching/explicit_runge_kutta.py:47-89
 
@@ -174,13 +176,139 @@ def roe_flux(L, R, g, gm, k):
                         0.5 * (FL[2] + FR[2]) - 0.5 * r2, 0.5 * (FL[3] + FR[3]) - 0.5 * r3])
 
 
+# ---- HLLL and HLLE fluxes -------------------------------------------------------------
+def _two_prod(a, b):
+    """a * b = p + e exactly (Dekker's product with Veltkamp's split, float64 arrays)."""
+    p = a * b
+    c = 134217729.0  # 2^27 + 1
+    t = c * a
+    ah = t - (t - a)
+    al = a - ah
+    t = c * b
+    bh = t - (t - b)
+    bl = b - bh
+    e = ((ah * bh - p) + ah * bl + al * bh) + al * bl
+    return p, e
+
+
+def _fma(a, b, c):
+    """Correctly rounded a * b + c, elementwise: the exact product's two parts and c
+    summed once with correct rounding (math.fsum)."""
+    import math
+
+    p, e = _two_prod(a, b)
+    out = np.empty_like(p)
+    pf, ef, cf, of = p.ravel(), e.ravel(), np.broadcast_to(c, p.shape).ravel(), out.ravel()
+    for i in range(pf.size):
+        of[i] = math.fsum((pf[i], ef[i], cf[i]))
+    return out
+
+
+class _Norm4(torch.autograd.Function):
+    """numpy.linalg.norm of a 4-vector as the reference environment evaluates it (the
+    square root of a sequential fused multiply-add dot product, OpenBLAS), over the
+    leading dimension; derivative x / |x|, 0 at a zero vector."""
+
+    @staticmethod
+    def forward(ctx, x):
+        xn = x.detach().cpu().numpy()
+        r = _fma(xn[0], xn[0], np.zeros_like(xn[0]))
+        for k in (1, 2, 3):
+            r = _fma(xn[k], xn[k], r)
+        n = torch.from_numpy(np.sqrt(r)).to(x.device)
+        ctx.save_for_backward(x, n)
+        return n
+
+    @staticmethod
+    def backward(ctx, g):
+        x, n = ctx.saved_tensors
+        safe = torch.where(n > 0, n, torch.ones_like(n))
+        return torch.where(n > 0, g / safe, torch.zeros_like(n)) * x
+
+
+norm4 = _Norm4.apply
+
+
+def _vmax(a, b):
+    """max keeping the first operand on ties (the CUDA path's selection)."""
+    return torch.where(vlt(a, b), b, a)
+
+
+def _vmin(a, b):
+    return torch.where(vlt(b, a), b, a)
+
+
+def _hll_bounds(L, R, g):
+    """Roe u and a~ and the Harten-corrected bounds L+ = max(u_R + a_R, u~ + a~),
+    L- = min(u_L - a_L, u~ - a~) (pyhype/flux/HLLL.py:28-37, HLLE.py:25-33)."""
+    sqL, sqR = sqrt(L[0]), sqrt(R[0])
+    inv = 1.0 / (sqL + sqR)
+    Q0 = sqrt(L[0] * R[0])
+    Q1 = (L[1] * sqL + R[1] * sqR) * inv
+    Q3 = (L[3] * sqL + R[3] * sqR) * inv
+    aL = sqrt(g * L[3] / L[0])
+    aR = sqrt(g * R[3] / R[0])
+    aQ = sqrt(g * Q3 / Q0)
+    slowL, fastL = L[1] - aL, L[1] + aL
+    slowR, fastR = R[1] - aR, R[1] + aR
+    rs, rf = Q1 - aQ, Q1 + aQ
+    tp = 2 * (slowR - slowL)
+    tm = 2 * (fastR - fastL)
+    tp = torch.where(tp > 0, tp, torch.full_like(tp, 1e-8))
+    tm = torch.where(tm > 0, tm, torch.full_like(tm, 1e-8))
+    rs = torch.where(torch.abs(rs) < tp, 0.5 * ((rs * rs) / tp + tp), rs)
+    rf = torch.where(torch.abs(rf) < tm, 0.5 * ((rf * rf) / tm + tm), rf)
+    return Q1, aQ, _vmax(fastR, rf), _vmin(slowL, rs)
+
+
+def _cons_flux(Wv, gm1):
+    """ConservativeState of a primitive state and PrimitiveState.F(U=...)
+    (pyhype/states/primitive.py:203-209)."""
+    ek = 0.5 * Wv[0] * (Wv[1] * Wv[1] + Wv[2] * Wv[2])
+    U = torch.stack([Wv[0], Wv[0] * Wv[1], Wv[0] * Wv[2], Wv[3] / gm1 + ek])
+    F = torch.stack([U[1], U[1] * Wv[1] + Wv[3], U[1] * Wv[2], Wv[1] * (U[3] + Wv[3])])
+    return U, F
+
+
+def hlll_flux(L, R, g, gm1):
+    """FluxHLLL (pyhype/flux/HLLL.py:25-103, its JIT branch order)."""
+    u, aQ, Lp, Lm = _hll_bounds(L, R, g)
+    UL, FL = _cons_flux(L, gm1)
+    UR, FR = _cons_flux(R, gm1)
+    mid = (Lm < 0) & (Lp > 0)
+    # the middle branch with its denominators made safe where it is not taken (the
+    # gradient of an unselected torch.where branch must stay finite)
+    Lms = torch.where(mid, Lm, -torch.ones_like(Lm))
+    Lps = torch.where(mid, Lp, torch.ones_like(Lp))
+    dU = UR - UL
+    r = (FR - FL) - u * dU
+    kk = aQ * norm4(dU)
+    den_k = torch.where(kk < 1e-16, kk + 1e-14, kk)
+    alpha = _vmax(torch.zeros_like(kk), 1 - norm4(r) / den_k)
+    sc = Lms * Lps * (1 - alpha * (1 - _vmax(u / Lms, u / Lps)))
+    F = (Lps * FL - Lms * FR + sc * dU) / (Lps - Lms)
+    return torch.where(Lm >= 0, FL, torch.where(Lp <= 0, FR, F))
+
+
+def hlle_flux(L, R, g, gm1):
+    """FluxHLLE (pyhype/flux/HLLE.py:22-47): F_R where L+ <= 0, else F_L where L- >= 0."""
+    _, _, Lp, Lm = _hll_bounds(L, R, g)
+    UL, FL = _cons_flux(L, gm1)
+    UR, FR = _cons_flux(R, gm1)
+    mid = (Lm < 0) & (Lp > 0)
+    Lms = torch.where(mid, Lm, -torch.ones_like(Lm))
+    Lps = torch.where(mid, Lp, torch.ones_like(Lp))
+    F = (Lps * FL - Lms * FR + Lms * Lps * (UR - UL)) / (Lps - Lms)
+    return torch.where(Lp <= 0, FR, torch.where(Lm >= 0, FL, F))
+
+
 # ---- residual ------------------------------------------------------------------------
 class Scheme:
     """dUdt of one block and its RK steps.  ``sides`` maps E/W/N/S to Reflection,
     OutletDirichlet or copy."""
 
     def __init__(self, geo: Geometry, gamma: float, gm1: float, limiter="Venkatakrishnan",
-                 recon="ConservativeState", sides=None):
+                 recon="ConservativeState", sides=None, flux="Roe"):
         self.geo = geo
         self.g, self.gm1 = gamma, gm1
         self.gm = gamma / (gamma - 1.0)
@@ -188,6 +316,16 @@ class Scheme:
         self.lim = limiter
         self.prim = recon == "PrimitiveState"
         self.sides = sides or {s: REFLECT for s in "EWNS"}
+        if flux not in ("Roe", "HLLL", "HLLE"):
+            raise ValueError(f"flux {flux}")
+        self.flux = flux
+
+    def riemann(self, L, R):
+        if self.flux == "HLLL":
+            return hlll_flux(L, R, self.g, self.gm1)
+        if self.flux == "HLLE":
+            return hlle_flux(L, R, self.g, self.gm1)
+        return roe_flux(L, R, self.g, self.gm, self.k)
 
     def to_recon(self, U):
         return cons_to_prim(U, self.gm1) if self.prim else U
@@ -288,10 +426,10 @@ class Scheme:
         vRs = torch.cat([wR, oE[:, :, None]], dim=2)
         hLs = torch.cat([oS[:, None, :], nL], dim=1)
         hRs = torch.cat([sR, oN[:, None, :]], dim=1)
-        Fv = roe_flux(vLs, vRs, self.g, self.gm, self.k)
+        Fv = self.riemann(vLs, vRs)
         if not G.cart:
             Fv = unrotate(Fv, G.vc, G.vs)
-        Fh = roe_flux(hLs, hRs, self.g, self.gm, self.k)
+        Fh = self.riemann(hLs, hRs)
         Fh = unrotate90(Fh) if G.cart else unrotate(Fh, G.hc, G.hs)
         Iv = G.vL * (2 * Fv)
         Ih = G.hL * (2 * Fh)
@@ -346,7 +484,8 @@ class MultiBlockScheme:
 
     KIND = {0: NEIGHBOR, 1: COPY, 2: REFLECT, 3: OUTLET}
 
-    def __init__(self, problem, gamma: float, gm1: float, limiter="Venkatakrishnan", recon="ConservativeState"):
+    def __init__(self, problem, gamma: float, gm1: float, limiter="Venkatakrishnan", recon="ConservativeState",
+                 flux="Roe"):
         self.P = problem
         self.blocks = []
         for b in range(problem.nblocks):
@@ -357,7 +496,7 @@ class MultiBlockScheme:
                 if k not in self.KIND:
                     raise ValueError("the transcription covers neighbour, copy, reflection and outlet sides")
                 kinds[s] = self.KIND[k]
-            sch = Scheme(Geometry(problem.block_geometry[b]), gamma, gm1, limiter, recon, kinds)
+            sch = Scheme(Geometry(problem.block_geometry[b]), gamma, gm1, limiter, recon, kinds, flux)
             self.blocks.append((B.cell_offset, B.nx, B.ny, [int(B.neighbor[si]) for si in range(4)], sch))
 
     def residual(self, U):

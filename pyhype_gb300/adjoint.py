@@ -46,9 +46,10 @@ def single_block_mesh(length: float = 10.0, bc: str = "Reflection") -> dict:
 
 
 def adjoint_problem(n: int = 256, length: float = 10.0, limiter: str = "Venkatakrishnan",
-                    recon: str = "ConservativeState", cfl: float = 0.5, bc: str = "Reflection") -> Problem:
+                    recon: str = "ConservativeState", cfl: float = 0.5, bc: str = "Reflection",
+                    flux: str = "Roe") -> Problem:
     air = Air(a_inf=343.0, rho_inf=1.0)
-    return build_problem(single_block_mesh(length, bc), n, n, flux="Roe", limiter=limiter, recon=recon,
+    return build_problem(single_block_mesh(length, bc), n, n, flux=flux, limiter=limiter, recon=recon,
                          gamma=air.gamma(), gm1=air.gamma() - 1, cfl=cfl, fluid=air)
 
 

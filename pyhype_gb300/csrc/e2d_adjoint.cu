@@ -84,7 +84,6 @@ FaceArraysT<T> face_slot(E2DSolver* h, T* base) {
 }
 
 int check_supported(E2DSolver* h) {
-  if (h->cfg.flux != E2D_FLUX_ROE) return fail(E2D_ERR_UNSUPPORTED, "the adjoint supports the Roe flux");
   if (h->hinst.size() != 1) return fail(E2D_ERR_UNSUPPORTED, "the adjoint runs on single-instance problems");
   if (h->nstages < 1) return fail(E2D_ERR_INVALID, "no tableau set");
   if (h->cfg.nqp > 1) return fail(E2D_ERR_UNSUPPORTED, "the adjoint is built for one face quadrature point");
@@ -152,7 +151,13 @@ cudaError_t launch_gather(E2DSolver* h, const T* Y, const T* st, T* lamU, const 
 template <typename T>
 int residual_vjp(E2DSolver* h, const T* Y, FaceArraysT<T> F, const T* lk, T* lamU, const AdjProgramT<T>& prog) {
   E2DAdjoint* A = h->adj;
-  k_flux_vjp<T><<<h->nface_tiles, TX * TY, 0, h->stream>>>(path<T>(h).P, h->face_tiles, h->inst, F, lk);
+  const ParamsT<T>& P = path<T>(h).P;
+  if (P.flux == E2D_FLUX_HLLL)
+    k_flux_vjp<T, E2D_FLUX_HLLL><<<h->nface_tiles, TX * TY, 0, h->stream>>>(P, h->face_tiles, h->inst, F, lk);
+  else if (P.flux == E2D_FLUX_HLLE)
+    k_flux_vjp<T, E2D_FLUX_HLLE><<<h->nface_tiles, TX * TY, 0, h->stream>>>(P, h->face_tiles, h->inst, F, lk);
+  else
+    k_flux_vjp<T, E2D_FLUX_ROE><<<h->nface_tiles, TX * TY, 0, h->stream>>>(P, h->face_tiles, h->inst, F, lk);
   CK(cudaGetLastError());
   CK(launch_reconstruct_vjp<T>(h, Y, F, as<T>(A->st)));
   CK(launch_gather<T>(h, Y, as<T>(A->st), lamU, prog));

@@ -7,7 +7,8 @@
 //
 //   k_flux_vjp          per face: the adjoint of the two cells' dUdt that the face
 //                       feeds (K3^T, one face at a time), times 2L, rotated by the
-//                       transpose of the flux un-rotation, through the Roe flux VJP;
+//                       transpose of the flux un-rotation, through the Roe, HLLL or
+//                       HLLE flux VJP;
 //                       the face's left/right adjoints overwrite its stored states.
 //   k_reconstruct_vjp   per cell: recomputes the cell's reconstruction from the stage
 //                       state (the same expressions as the forward kernel, so every
@@ -121,6 +122,33 @@ __device__ __forceinline__ void limiter_forward(T w0, T we, T ea, T so, T no, T 
       }
     }
   }
+  if constexpr (sizeof(T) == 4) {
+    // the FP32 forward's limiter (limit_cell_var): slopes from the reciprocal
+    // approximation, psi at the smallest and (limiters with a maximum) the largest;
+    // the selected face is the first face with the smallest (largest) slope
+    T sls[4];
+    int imn_s = 0, imx_s = 0;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      sls[s] = slope32(dmax, dmin, dv[s]);
+      if (s > 0 && vlt(sls[s], sls[imn_s])) imn_s = s;
+      if (s > 0 && vlt(sls[imx_s], sls[s])) imx_s = s;
+    }
+    T smin = sls[0], smax = sls[0], dmn = dv[0], dmx = dv[0];
+#pragma unroll
+    for (int s = 1; s < 4; ++s) {  // constant indices only (no local-memory array)
+      if (s == imn_s) { smin = sls[s]; dmn = dv[s]; }
+      if (s == imx_s) { smax = sls[s]; dmx = dv[s]; }
+    }
+    ph = psi_s<LIM>(smin);
+    sel = imn_s; ssl = smin; sdavg = dmn;
+    if constexpr (psi_has_peak<LIM>()) {
+      const T pb = psi_s<LIM>(smax);
+      if (vlt(pb, ph)) { ph = pb; sel = imx_s; ssl = smax; sdavg = dmx; }
+    }
+    ssign = is_pos(sdavg) ? 1 : (is_neg(sdavg) ? -1 : 0);
+    done = true;
+  }
   if (!done) {
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
@@ -153,7 +181,7 @@ __device__ __forceinline__ void limiter_forward(T w0, T we, T ea, T so, T no, T 
 // ---------------------------------------------------------------------------------
 // K2^T, K3^T
 // ---------------------------------------------------------------------------------
-template <typename T>
+template <typename T, int FLUX>
 __global__ void __launch_bounds__(TX * TY) k_flux_vjp(ParamsT<T> P, const int4* __restrict__ tiles,
                                                       const InstanceState* __restrict__ inst, FaceArraysT<T> F,
                                                       const T* __restrict__ lk) {
@@ -187,7 +215,7 @@ __global__ void __launch_bounds__(TX * TY) k_flux_vjp(ParamsT<T> P, const int4* 
       L[v] = F.vL[v * P.nvface + f];
       R[v] = F.vR[v * P.nvface + f];
     }
-    roe_flux_vjp(L, R, G, lF, lL, lR);
+    riemann_vjp<FLUX>(L, R, G, lF, lL, lR);
     store4(F.vL, P.nvface, f, lL);
     store4(F.vR, P.nvface, f, lR);
   }
@@ -210,7 +238,7 @@ __global__ void __launch_bounds__(TX * TY) k_flux_vjp(ParamsT<T> P, const int4* 
       L[v] = F.hL[v * P.nhface + f];
       R[v] = F.hR[v * P.nhface + f];
     }
-    roe_flux_vjp(L, R, G, lF, lL, lR);
+    riemann_vjp<FLUX>(L, R, G, lF, lL, lR);
     store4(F.hL, P.nhface, f, lL);
     store4(F.hR, P.nhface, f, lR);
   }

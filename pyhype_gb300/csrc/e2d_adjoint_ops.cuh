@@ -1,5 +1,5 @@
 // e2d_adjoint_ops.cuh - hand-written reverse-mode (vector-Jacobian) products of the
-// pointwise pieces of the scheme: the Roe flux, the conservative->primitive
+// pointwise pieces of the scheme: the Roe, HLLL and HLLE fluxes, the conservative->primitive
 // conversion, the rotations and the reflection, and the limiter functions.
 //
 // Each *_vjp recomputes the forward intermediates it needs from the forward inputs
@@ -185,6 +185,276 @@ __device__ void roe_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* l
     lL[v] += acc[0][v];
     lR[v] += acc[1][v];
   }
+}
+
+// ---- HLL-type fluxes (HLLL, HLLE) --------------------------------------------------
+// The forward pieces both share: Roe average (u and a only), sound speeds, the
+// Harten-corrected Roe speeds and the bounds L+ = max(u_R + a_R, rf), L- = min(u_L -
+// a_L, rs), with the selections the forward makes (vmax keeps its first operand on
+// ties, vmin its first).
+template <typename T>
+struct HllBounds {
+  T sqL, sqR, inv, Q0, n1, n3, Q1, Q3, aL, aR, aQ;
+  T rs0, rf0, tp, tm;
+  bool tp_pos, tm_pos, cs, cf, plus_fastR, minus_slowL;
+  T Lp, Lm;
+};
+
+template <typename T>
+__device__ __forceinline__ void hll_bounds(const T* L, const T* R, const Gas<T>& G, HllBounds<T>& b) {
+  b.sqL = sqrt(L[0]);
+  b.sqR = sqrt(R[0]);
+  b.inv = pdiv(T(1), b.sqL + b.sqR);
+  b.Q0 = sqrt(L[0] * R[0]);
+  b.n1 = L[1] * b.sqL + R[1] * b.sqR;
+  b.n3 = L[3] * b.sqL + R[3] * b.sqR;
+  b.Q1 = b.n1 * b.inv;
+  b.Q3 = b.n3 * b.inv;
+  b.aL = sqrt(pdiv(G.g * L[3], L[0]));
+  b.aR = sqrt(pdiv(G.g * R[3], R[0]));
+  b.aQ = sqrt(pdiv(G.g * b.Q3, b.Q0));
+  b.rs0 = b.Q1 - b.aQ;
+  b.rf0 = b.Q1 + b.aQ;
+  const T slowL = L[1] - b.aL, fastL = L[1] + b.aL, slowR = R[1] - b.aR, fastR = R[1] + b.aR;
+  const T tp0 = twice(slowR - slowL), tm0 = twice(fastR - fastL);
+  b.tp_pos = is_pos(tp0);
+  b.tm_pos = is_pos(tm0);
+  b.tp = b.tp_pos ? tp0 : T(1e-8);
+  b.tm = b.tm_pos ? tm0 : T(1e-8);
+  b.cs = vlt(T(fabs(b.rs0)), b.tp);
+  b.cf = vlt(T(fabs(b.rf0)), b.tm);
+  const T rs = b.cs ? half(qdiv(b.rs0 * b.rs0, b.tp) + b.tp) : b.rs0;
+  const T rf = b.cf ? half(qdiv(b.rf0 * b.rf0, b.tm) + b.tm) : b.rf0;
+  b.plus_fastR = !vlt(fastR, rf);
+  b.minus_slowL = !vlt(rs, slowL);
+  b.Lp = b.plus_fastR ? fastR : rf;
+  b.Lm = b.minus_slowL ? slowL : rs;
+}
+
+// reverse of hll_bounds (+ the Roe average's u and a~): lL, lR += the adjoints of
+// L+, L-, u and a~ pulled back to the states
+template <typename T>
+__device__ __forceinline__ void hll_bounds_vjp(const T* L, const T* R, const Gas<T>& G, const HllBounds<T>& b, T lLp,
+                                               T lLm, T lu, T laQ_in, T* lL, T* lR) {
+  T lslowL = T(0), lfastL = T(0), lslowR = T(0), lfastR = T(0), lrs = T(0), lrf = T(0);
+  if (b.plus_fastR) lfastR += lLp; else lrf += lLp;
+  if (b.minus_slowL) lslowL += lLm; else lrs += lLm;
+  // Harten's correction of the Roe speeds
+  T lrs0 = lrs, lrf0 = lrf, ltp = T(0), ltm = T(0);
+  if (b.cs) {
+    lrs0 = lrs * qdiv(b.rs0, b.tp);
+    ltp = half(lrs) * (T(1) - qdiv(b.rs0 * b.rs0, b.tp * b.tp));
+  }
+  if (b.cf) {
+    lrf0 = lrf * qdiv(b.rf0, b.tm);
+    ltm = half(lrf) * (T(1) - qdiv(b.rf0 * b.rf0, b.tm * b.tm));
+  }
+  if (!b.tp_pos) ltp = T(0);
+  if (!b.tm_pos) ltm = T(0);
+  lslowR += twice(ltp);
+  lslowL -= twice(ltp);
+  lfastR += twice(ltm);
+  lfastL -= twice(ltm);
+  // rs0 = u - aQ, rf0 = u + aQ; slow/fast = W1 -/+ a
+  const T lQ1 = lu + lrs0 + lrf0;
+  const T laQ = laQ_in + lrf0 - lrs0;
+  lR[1] += lslowR + lfastR;
+  lL[1] += lslowL + lfastL;
+  const T laR = lfastR - lslowR, laL = lfastL - lslowL;
+  // sound speeds a = sqrt(g p / rho)
+  lR[0] += qdiv(-laR * G.g * R[3], twice(b.aR) * R[0] * R[0]);
+  lR[3] += qdiv(laR * G.g, twice(b.aR) * R[0]);
+  lL[0] += qdiv(-laL * G.g * L[3], twice(b.aL) * L[0] * L[0]);
+  lL[3] += qdiv(laL * G.g, twice(b.aL) * L[0]);
+  const T lQ3 = qdiv(laQ * G.g, twice(b.aQ) * b.Q0);
+  const T lQ0 = qdiv(-laQ * G.g * b.Q3, twice(b.aQ) * b.Q0 * b.Q0);
+  // Roe average (Q2 does not enter these fluxes)
+  const T linv = lQ1 * b.n1 + lQ3 * b.n3;
+  lL[1] += lQ1 * b.inv * b.sqL;
+  lR[1] += lQ1 * b.inv * b.sqR;
+  lL[3] += lQ3 * b.inv * b.sqL;
+  lR[3] += lQ3 * b.inv * b.sqR;
+  const T lsqL = (lQ1 * L[1] + lQ3 * L[3]) * b.inv - b.inv * b.inv * linv;
+  const T lsqR = (lQ1 * R[1] + lQ3 * R[3]) * b.inv - b.inv * b.inv * linv;
+  lL[0] += qdiv(lQ0 * R[0], twice(b.Q0)) + qdiv(lsqL, twice(b.sqL));
+  lR[0] += qdiv(lQ0 * L[0], twice(b.Q0)) + qdiv(lsqR, twice(b.sqR));
+}
+
+// U = prim_to_cons(W) and F = {U1, U1 W1 + W3, U1 W2, W1 (U3 + W3)} (PrimitiveState.F
+// with U): the forward values, and lW += (dU/dW)^T lU + (dF/dW)^T lF.
+template <typename T>
+__device__ __forceinline__ void cons_and_flux(const T* W, const Gas<T>& G, T* U, T* F) {
+  prim_to_cons(W, G, U);
+  F[0] = U[1];
+  F[1] = U[1] * W[1] + W[3];
+  F[2] = U[1] * W[2];
+  F[3] = W[1] * (U[3] + W[3]);
+}
+template <typename T>
+__device__ __forceinline__ void cons_and_flux_vjp(const T* W, const Gas<T>& G, const T* U, const T* lF, const T* lU_in,
+                                                  T* lW) {
+  T lU[4] = {lU_in[0], lU_in[1], lU_in[2], lU_in[3]};
+  lU[1] += lF[0] + lF[1] * W[1] + lF[2] * W[2];
+  lU[3] += lF[3] * W[1];
+  lW[1] += lF[1] * U[1] + lF[3] * (U[3] + W[3]);
+  lW[2] += lF[2] * U[1];
+  lW[3] += lF[1] + lF[3] * W[1];
+  // U = {W0, W0 W1, W0 W2, W3 / gm1 + 0.5 W0 (W1^2 + W2^2)}
+  lW[0] += lU[0] + lU[1] * W[1] + lU[2] * W[2] + lU[3] * half(W[1] * W[1] + W[2] * W[2]);
+  lW[1] += lU[1] * W[0] + lU[3] * W[0] * W[1];
+  lW[2] += lU[2] * W[0] + lU[3] * W[0] * W[2];
+  lW[3] += pdiv(lU[3], G.gm1);
+}
+
+// F = hlll_flux(WL, WR) (pyhype/flux/HLLL.py:25-103).  Subgradients: the branch the
+// forward takes; alpha = max(0, 1 - |r|/k) passes nothing back where it is 0; the
+// norms pass nothing back at a zero vector; max(u/L-, u/L+) the operand selected.
+template <typename T>
+__device__ void hlll_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* lF, T* lL, T* lR) {
+  HllBounds<T> b;
+  hll_bounds(L, R, G, b);
+  T UL[4], UR[4], FL[4], FR[4];
+  cons_and_flux(L, G, UL, FL);
+  cons_and_flux(R, G, UR, FR);
+  const T zero4[4] = {T(0), T(0), T(0), T(0)};
+  if (b.Lm >= T(0)) {
+    cons_and_flux_vjp(L, G, UL, lF, zero4, lL);
+    return;
+  }
+  if (b.Lp <= T(0)) {
+    cons_and_flux_vjp(R, G, UR, lF, zero4, lR);
+    return;
+  }
+  const T Lp = b.Lp, Lm = b.Lm, u = b.Q1;
+  T dU[4], rr[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    dU[v] = UR[v] - UL[v];
+    rr[v] = (FR[v] - FL[v]) - u * dU[v];
+  }
+  const T nd = norm4(dU[0], dU[1], dU[2], dU[3]);
+  const T kk = b.aQ * nd;
+  const T nr = norm4(rr[0], rr[1], rr[2], rr[3]);
+  const T den_k = (kk < T(1e-16)) ? kk + T(1e-14) : kk;
+  const T x = T(1) - qdiv(nr, den_k);
+  const bool alpha_pos = vlt(T(0), x);
+  const T alpha = alpha_pos ? x : T(0);
+  const T qm = qdiv(u, Lm), qp = qdiv(u, Lp);
+  const bool m_sel = !vlt(qm, qp);
+  const T M = m_sel ? qm : qp;
+  const T Bv = T(1) - alpha * (T(1) - M);
+  const T sc = Lm * Lp * Bv;
+  const T den = Lp - Lm;
+  // reverse
+  T g[4], lFL[4], lFR[4], ldU[4];
+  T lsc = T(0), lden = T(0), lLp = T(0), lLm = T(0);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    g[v] = pdiv(lF[v], den);
+    const T Fv = pdiv(Lp * FL[v] - Lm * FR[v] + sc * dU[v], den);
+    lFL[v] = Lp * g[v];
+    lFR[v] = -Lm * g[v];
+    ldU[v] = sc * g[v];
+    lsc += g[v] * dU[v];
+    lden -= g[v] * Fv;
+    lLp += g[v] * FL[v];
+    lLm -= g[v] * FR[v];
+  }
+  lLp += lden;
+  lLm -= lden;
+  lLm += lsc * Lp * Bv;
+  lLp += lsc * Lm * Bv;
+  const T lB = lsc * Lm * Lp;
+  const T lalpha = -lB * (T(1) - M);
+  const T lM = lB * alpha;
+  T lu = T(0);
+  if (m_sel) {
+    lu += qdiv(lM, Lm);
+    lLm -= lM * qdiv(qm, Lm);
+  } else {
+    lu += qdiv(lM, Lp);
+    lLp -= lM * qdiv(qp, Lp);
+  }
+  T lnr = T(0), lkk = T(0);
+  if (alpha_pos) {
+    lnr = -qdiv(lalpha, den_k);
+    lkk = lalpha * qdiv(qdiv(nr, den_k), den_k);
+  }
+  const T laQ_k = lkk * nd;
+  const T lnd = lkk * b.aQ;
+  if (nd > T(0)) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) ldU[v] += lnd * qdiv(dU[v], nd);
+  }
+  if (nr > T(0)) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const T lr = lnr * qdiv(rr[v], nr);
+      lFR[v] += lr;
+      lFL[v] -= lr;
+      lu -= lr * dU[v];
+      ldU[v] -= u * lr;
+    }
+  }
+  T lUL[4], lUR[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    lUR[v] = ldU[v];
+    lUL[v] = -ldU[v];
+  }
+  cons_and_flux_vjp(L, G, UL, lFL, lUL, lL);
+  cons_and_flux_vjp(R, G, UR, lFR, lUR, lR);
+  hll_bounds_vjp(L, R, G, b, lLp, lLm, lu, laQ_k, lL, lR);  // a~ also enters k = a~ |dU|
+}
+
+// F = hlle_flux(WL, WR) (pyhype/flux/HLLE.py:22-47): F_R where L+ <= 0, else F_L where
+// L- >= 0, else (L+ F_L - L- F_R + L- L+ (U_R - U_L)) / (L+ - L-).
+template <typename T>
+__device__ void hlle_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* lF, T* lL, T* lR) {
+  HllBounds<T> b;
+  hll_bounds(L, R, G, b);
+  T UL[4], UR[4], FL[4], FR[4];
+  cons_and_flux(L, G, UL, FL);
+  cons_and_flux(R, G, UR, FR);
+  const T zero4[4] = {T(0), T(0), T(0), T(0)};
+  if (b.Lp <= T(0)) {
+    cons_and_flux_vjp(R, G, UR, lF, zero4, lR);
+    return;
+  }
+  if (b.Lm >= T(0)) {
+    cons_and_flux_vjp(L, G, UL, lF, zero4, lL);
+    return;
+  }
+  const T Lp = b.Lp, Lm = b.Lm;
+  const T den = Lp - Lm, LL = Lm * Lp;
+  T lFL[4], lFR[4], lUL[4], lUR[4];
+  T lLL = T(0), lden = T(0), lLp = T(0), lLm = T(0);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    const T dU = UR[v] - UL[v];
+    const T gv = pdiv(lF[v], den);
+    const T Fv = pdiv(Lp * FL[v] - Lm * FR[v] + LL * dU, den);
+    lFL[v] = Lp * gv;
+    lFR[v] = -Lm * gv;
+    lUR[v] = LL * gv;
+    lUL[v] = -LL * gv;
+    lLL += gv * dU;
+    lden -= gv * Fv;
+    lLp += gv * FL[v];
+    lLm -= gv * FR[v];
+  }
+  lLp += lden + lLL * Lm;
+  lLm += -lden + lLL * Lp;
+  cons_and_flux_vjp(L, G, UL, lFL, lUL, lL);
+  cons_and_flux_vjp(R, G, UR, lFR, lUR, lR);
+  hll_bounds_vjp(L, R, G, b, lLp, lLm, T(0), T(0), lL, lR);
+}
+
+template <int FLUX, typename T>
+__device__ __forceinline__ void riemann_vjp(const T* L, const T* R, const Gas<T>& G, const T* lF, T* lL, T* lR) {
+  if (FLUX == E2D_FLUX_HLLL) hlll_flux_vjp(L, R, G, lF, lL, lR);
+  else if (FLUX == E2D_FLUX_HLLE) hlle_flux_vjp(L, R, G, lF, lL, lR);
+  else roe_flux_vjp(L, R, G, lF, lL, lR);
 }
 
 }  // namespace e2d

@@ -531,7 +531,7 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
   int64_t ncell = 0, nv = 0, nh = 0;
   for (int b = 0; b < cfg->nblocks; ++b) {
     const E2DBlock& B = blocks[b];
-    if (B.nx < 2 || B.ny < 2) return fail(E2D_ERR_INVALID, "block %d: nx, ny must be >= 2", b);
+    if (B.nx < 1 || B.ny < 1) return fail(E2D_ERR_INVALID, "block %d: nx, ny must be >= 1", b);
     if (B.instance < 0 || B.instance >= ninst) return fail(E2D_ERR_INVALID, "block %d: bad instance id", b);
     if (B.cell_offset < 0 || B.vface_offset < 0 || B.hface_offset < 0)
       return fail(E2D_ERR_INVALID, "block %d: negative offset", b);

@@ -193,54 +193,70 @@ __global__ void __launch_bounds__(FTHREADS, MINB)
   __syncthreads();
 
   // ---- face states: tile rows, then the ring (S row, N row, W and E columns) ---------
+  // One call site for every kind of task (the reconstruction is the kernel's largest
+  // piece of code; four inlined copies of it crowded the instruction cache).
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int task = warp; task < FTY + 3; task += FTHREADS / 32) {
-    if (task < FTY) {
-      if (i0 + task < ny && j0 + lane < nx)
-        fused_cell<T, LIM, RECON>(P, G, B, sm, i0, j0, task, lane, FACE_E | FACE_W | FACE_N | FACE_S, true, t);
-    } else if (task == FTY) {
-      if (i0 >= 1 && j0 + lane < nx) fused_cell<T, LIM, RECON>(P, G, B, sm, i0, j0, -1, lane, FACE_N, false, t);
-    } else if (task == FTY + 1) {
-      if (i0 + FTY < ny && j0 + lane < nx)
-        fused_cell<T, LIM, RECON>(P, G, B, sm, i0, j0, FTY, lane, FACE_S, false, t);
-    } else {
-      const int r = lane & 15;
-      if (lane < 16) {
-        if (j0 >= 1 && i0 + r < ny) fused_cell<T, LIM, RECON>(P, G, B, sm, i0, j0, r, -1, FACE_E, false, t);
-      } else {
-        if (j0 + TX < nx && i0 + r < ny) fused_cell<T, LIM, RECON>(P, G, B, sm, i0, j0, r, TX, FACE_W, false, t);
-      }
+    int lr, lc, which;
+    bool live;
+    if (task < FTY) {  // a tile row: all four faces, and block-boundary outside states
+      lr = task;
+      lc = lane;
+      which = FACE_E | FACE_W | FACE_N | FACE_S;
+      live = i0 + lr < ny && j0 + lc < nx;
+    } else if (task == FTY) {  // the ring row below the tile: its north faces
+      lr = -1;
+      lc = lane;
+      which = FACE_N;
+      live = i0 >= 1 && j0 + lc < nx;
+    } else if (task == FTY + 1) {  // the ring row above: its south faces
+      lr = FTY;
+      lc = lane;
+      which = FACE_S;
+      live = i0 + FTY < ny && j0 + lc < nx;
+    } else {  // the ring columns: west (lanes 0-15, east faces), east (16-31, west faces)
+      lr = lane & 15;
+      const bool east = lane >= 16;
+      lc = east ? TX : -1;
+      which = east ? FACE_W : FACE_E;
+      live = i0 + lr < ny && (east ? j0 + TX < nx : j0 >= 1);
     }
+    if (live) fused_cell<T, LIM, RECON>(P, G, B, sm, i0, j0, lr, lc, which, task < FTY, t);
   }
   __syncthreads();
 
-  // ---- one flux per face of the tile ------------------------------------------------
+  // ---- one flux per face of the tile (one call site for both face families) ---------
   {
     const bool cart = B->is_cartesian != 0;
-    const DebugOutT<T> none{};
     constexpr int NV = FTY * (TX + 1), NH = (FTY + 1) * TX;
     for (int item = threadIdx.x; item < NV + NH; item += FTHREADS) {
-      if (item < NV) {
-        const int r = item / (TX + 1), c = item - r * (TX + 1);
-        if (i0 + r < ny && j0 + c <= nx) {
-          const int64_t f = vf_at(B, i0 + r, j0 + c);
-          const T L[4] = {sm.vL[0][r][c], sm.vL[1][r][c], sm.vL[2][r][c], sm.vL[3][r][c]};
-          const T R[4] = {sm.vR[0][r][c], sm.vR[1][r][c], sm.vR[2][r][c], sm.vR[3][r][c]};
-          T Iv[4];
-          vface_flux<T, FLUX, false>(P, G, cart, f, L, R, Iv, none);
-          put4(sm.vL, r, c, Iv);
-        }
-      } else {
-        const int h = item - NV;
-        const int r = h / TX, c = h - r * TX;
-        if (i0 + r <= ny && j0 + c < nx) {
-          const int64_t f = hf_at(B, i0 + r, j0 + c);
-          const T L[4] = {sm.hL[0][r][c], sm.hL[1][r][c], sm.hL[2][r][c], sm.hL[3][r][c]};
-          const T R[4] = {sm.hR[0][r][c], sm.hR[1][r][c], sm.hR[2][r][c], sm.hR[3][r][c]};
-          T Iv[4];
-          hface_flux<T, FLUX, false>(P, G, cart, f, L, R, Iv, none);
-          put4(sm.hL, r, c, Iv);
-        }
+      const bool vert = item < NV;
+      const int h = vert ? item : item - NV;
+      const int w = vert ? TX + 1 : TX;
+      const int r = h / w, c = h - r * w;
+      const bool live = vert ? (i0 + r < ny && j0 + c <= nx) : (i0 + r <= ny && j0 + c < nx);
+      if (!live) continue;
+      const int64_t f = vert ? vf_at(B, i0 + r, j0 + c) : hf_at(B, i0 + r, j0 + c);
+      T L[4], R[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        L[v] = vert ? sm.vL[v][r][c] : sm.hL[v][r][c];
+        R[v] = vert ? sm.vR[v][r][c] : sm.hR[v][r][c];
+      }
+      T Fq[4];
+      riemann<FLUX>(L, R, G, Fq);
+      // rotated back to the x/y frame and integrated, as vface_flux / hface_flux
+      const T* cosp = vert ? P.geo.vface[E2D_F_COS] : P.geo.hface[E2D_F_COS];
+      const T* sinp = vert ? P.geo.vface[E2D_F_SIN] : P.geo.hface[E2D_F_SIN];
+      const T* lenp = vert ? P.geo.vface[E2D_F_L] : P.geo.hface[E2D_F_L];
+      if (!vert && cart) unrotate90(Fq);
+      else if (!cart) unrotate(Fq, cosp[f], sinp[f]);
+      const T len = lenp[f];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const T Iv = len * twice(Fq[v]);
+        if (vert) sm.vL[v][r][c] = Iv;
+        else sm.hL[v][r][c] = Iv;
       }
     }
   }

@@ -216,24 +216,26 @@ __device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, con
       }
     }
   } else {
+    // FP32: every face's slope from the reciprocal approximation (slope32), psi only at
+    // the smallest and, for the limiters with a maximum, the largest of them (the
+    // functions are unimodal: psi_has_peak)
+    T smin = T(0), smax = T(0);
+    // FP64's round trip (w0 + hot) - w0 is hot itself unless |hot| is below half an
+    // FP64 ulp of w0, where it is zero and the slope takes its davg == 0 branch
+    // (psi(1)).  In FP32 the same round trip would zero every |hot| below 2^-25 |w0|
+    // and switch branches where the FP64 path does not, so the FP32 form applies the
+    // FP64 threshold, 2^-53 times the power of two of w0.
+    const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
       hot[s] = gx * g.hx[s] + gy * g.hy[s];
-      // FP64's round trip (w0 + hot) - w0 is hot itself unless |hot| is below half
-      // an FP64 ulp of w0, where it is zero and the slope takes its davg == 0
-      // branch (psi(1)).  In FP32 the same round trip would zero every |hot| below
-      // 2^-25 |w0| and switch branches where the FP64 path does not, so the FP32 form
-      // applies the FP64 threshold, 2^-53 times the power of two of w0.
-      const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
       const T davg = (fabs(hot[s]) < half_ulp64) ? T(0) : hot[s];
-      // slope dmax/davg (davg > 0), dmin/davg (davg < 0), 1 (davg == 0), with a single
-      // division so lanes of different signs share one division sequence; a zero davg
-      // divides nothing
-      const bool pos = is_pos(davg), neg = is_neg(davg);
-      const T sl = (pos || neg) ? qdiv(pos ? dmax : dmin, davg) : T(1);
-      const T p = psi_s<LIM>(sl);
-      ph = (s == 0) ? p : vmin(ph, p);
+      const T sl = slope32(dmax, dmin, davg);
+      smin = (s == 0) ? sl : vmin(smin, sl);
+      smax = (s == 0) ? sl : vmax(smax, sl);
     }
+    ph = psi_s<LIM>(smin);
+    if constexpr (psi_has_peak<LIM>()) ph = vmin(ph, psi_s<LIM>(smax));
   }
   ph = is_neg(ph) ? T(0) : ph;
 #pragma unroll

@@ -90,9 +90,12 @@ class QuadMeshGenerator(MeshGenerator):
                     "BCTypeW": self.BCW[i] if j == 0 else None,
                     "BCTypeN": self.BCN[j] if i == ny - 1 else None,
                     "BCTypeS": self.BCS[j] if i == 0 else None,
-                    "BCTypeNE": None,
-                    "BCTypeNW": None,
-                    "BCTypeSE": None,
-                    "BCTypeSW": None,
+                    # the reference's corner keys (mesh/base.py:219-222), kept for the
+                    # dictionary format; the corners carry no boundary condition on the
+                    # path (the ghost layers are the four sides)
+                    "BCTypeNE": self.BCE[i] if j == nx - 1 else None,
+                    "BCTypeNW": self.BCW[i] if j == 0 else None,
+                    "BCTypeSE": self.BCN[j] if i == ny - 1 else None,
+                    "BCTypeSW": self.BCS[j] if i == 0 else None,
                 }
         return out

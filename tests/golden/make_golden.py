@@ -363,6 +363,12 @@ CASES["qp3_hlll_prim"] = (dict(nx=16, ny=12, fvm_num_quadrature_points=3, fvm_fl
 CASES["qp2_skew"] = (dict(nx=12, ny=12, fvm_num_quadrature_points=2, fvm_flux_function_type="HLLL",
                           reconstruction_type=PrimitiveState, time_integrator="RK2", CFL=0.4), dmr_example_mesh,
                      lambda: DMRExampleIC(), 4, "all", None, None)
+# one-cell-wide and one-cell-high blocks (a shock tube along the block), and a 2 x 1
+# layout of one-cell-wide blocks with an inter-block side
+CASES["thin_x1"] = (dict(nx=1, ny=16), lambda: single_block(3, 4, 0, 8, bce="OutletDirichlet"),
+                    lambda: ExplosionIC(**MOVING), 5, "all", 2, None)
+CASES["thin_y1"] = (dict(nx=16, ny=1, fvm_flux_function_type="HLLL"), lambda: single_block(0, 8, 3, 4, bcs=None),
+                    lambda: ExplosionIC(**MOVING), 5, "all", 2, None)
 CASES["dmr5"] = (dict(nx=16, ny=20, fvm_flux_function_type="HLLL", reconstruction_type=PrimitiveState, CFL=0.4,
                      t_final=0.2, fluid=AIR_UNIT), lambda: dmr_mesh(5), lambda: DMRIC(), 8, "all", 3, [[1], [0.5, 0.5]])
 for _ti in ("ExplicitEuler1", "RK2", "Ralston2", "RK3", "RK3SSP", "Ralston3", "Ralston4", "DormandPrince5"):

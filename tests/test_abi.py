@@ -96,7 +96,7 @@ def _mutations():
         ("precision", cfg("precision", 7), "unknown precision"),
         ("flux code", cfg("flux", 9), "unknown flux/limiter/reconstruction code"),
         ("quadrature points", cfg("nqp", 4), "nqp must be 1, 2 or 3"),
-        ("block size", blk(0, "nx", 1), "block 0: nx, ny must be >= 2"),
+        ("block size", blk(0, "nx", 0), "block 0: nx, ny must be >= 1"),
         ("instance id", blk(0, "instance", 5), "block 0: bad instance id"),
         ("offset", blk(1, "cell_offset", -1), "block 1: negative offset"),
         ("side kind", blk(0, "side_kind", 99, 0), "block 0 side 0: bad kind"),

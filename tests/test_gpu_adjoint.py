@@ -53,6 +53,90 @@ def test_residual_vjp_matches_autograd(limiter, recon):
     assert _rel(got, want) < 1e-11, _rel(got, want)
 
 
+@pytest.mark.parametrize("flux", ["HLLL", "HLLE"])
+@pytest.mark.parametrize("recon", ["ConservativeState", "PrimitiveState"])
+@pytest.mark.parametrize("mach", [0.0, 2.5, -2.5])
+def test_residual_vjp_hll_matches_autograd(flux, recon, mach):
+    """The HLLL and HLLE reverse kernels against autograd of the transcription, on a
+    smooth state at rest and with supersonic streams either way (every branch of the
+    flux taken somewhere)."""
+    from test_torch_scheme import _flow_state
+
+    from pyhype_gb300._native import DeviceSolver
+    from pyhype_gb300.adjoint import adjoint_problem
+    from pyhype_gb300.time_marching import tableau
+
+    n = 40
+    P = adjoint_problem(n=n, limiter="Venkatakrishnan", recon=recon, flux=flux)
+    U = _flow_state(P, mach)
+    lam = np.random.default_rng(1).standard_normal(U.shape)
+    S = Scheme(Geometry(P.block_geometry[0]), AIR.gamma(), AIR.gamma() - 1, "Venkatakrishnan", recon, None, flux)
+    Ut = torch.tensor(U.reshape(4, n, n), requires_grad=True)
+    R = S.residual(Ut)
+    (R * torch.tensor(lam.reshape(4, n, n))).sum().backward()
+    want = Ut.grad.numpy().reshape(4, -1)
+    D = DeviceSolver(P, tableau=tableau("RK4"))
+    D.set_state(U)
+    assert np.array_equal(D.residual(), R.detach().numpy().reshape(4, -1))  # same forward values
+    got = D.residual_vjp(torch.tensor(lam, device="cuda")).cpu().numpy()
+    assert _rel(got, want) < 1e-11, _rel(got, want)
+
+
+def test_time_loop_gradient_hlll_matches_autograd():
+    """dJ/dU0 over 10 SSP-RK2 steps with HLLL and primitive reconstruction (the
+    double-Mach scheme), checkpoints every 4, against autograd of the transcription."""
+    from test_torch_scheme import _flow_state
+
+    from pyhype_gb300.adjoint import AdjointSolver, adjoint_problem
+    from pyhype_gb300.time_marching import tableau
+
+    n = 32
+    P = adjoint_problem(n=n, recon="PrimitiveState", flux="HLLL")
+    U0 = torch.tensor(_flow_state(P, 0.8, seed=2))
+    A = AdjointSolver(P, "SSPRK2", side="N", nsteps=10, ckpt_every=4)
+    J = A.forward(U0.cuda())
+    g = A.backward().cpu().numpy()
+    S = Scheme(Geometry(P.block_geometry[0]), AIR.gamma(), AIR.gamma() - 1, "Venkatakrishnan", "PrimitiveState",
+               None, "HLLL")
+    Ut = U0.clone().reshape(4, n, n).requires_grad_(True)
+    Jt = S.objective(Ut, A.dts, tableau("SSPRK2"), side="N")
+    Jt.backward()
+    assert abs(J - Jt.item()) <= 1e-13 * abs(J)
+    want = Ut.grad.numpy().reshape(4, -1)
+    assert _rel(g, want) < 1e-10, _rel(g, want)
+
+
+@pytest.mark.parametrize("nx,ny", [(1, 12), (14, 1)])
+def test_residual_vjp_thin_block(nx, ny):
+    """A one-cell-wide (or -high) block: both ghost images of a side pair fall on the
+    same cells."""
+    from pyhype_gb300._native import DeviceSolver
+    from pyhype_gb300.adjoint import single_block_mesh
+    from pyhype_gb300.problem import build_problem
+    from pyhype_gb300.time_marching import tableau
+
+    mesh = single_block_mesh(10.0)
+    mesh[0]["BCTypeE"] = "OutletDirichlet"
+    P = build_problem(mesh, nx, ny, flux="HLLL", limiter="Venkatakrishnan", recon="ConservativeState",
+                      gamma=AIR.gamma(), gm1=AIR.gamma() - 1, cfl=0.5, fluid=AIR)
+    g = P.block_geometry[0]
+    rho = 1.0 + 0.2 * np.sin(0.6 * g.xc + 0.5 * g.yc)
+    u, v = 0.3 * np.cos(0.3 * g.yc), 0.2 * np.sin(0.4 * g.xc)
+    p = 0.7 + 0.1 * np.cos(0.5 * g.xc - 0.3 * g.yc)
+    U = P.to_soa([np.stack([rho, rho * u, rho * v, p / 0.4 + 0.5 * rho * (u * u + v * v)], axis=-1)])
+    lam = np.random.default_rng(4).standard_normal(U.shape)
+    S = Scheme(Geometry(g), AIR.gamma(), AIR.gamma() - 1, "Venkatakrishnan", "ConservativeState",
+               {"E": OUTLET, "W": REFLECT, "N": REFLECT, "S": REFLECT}, "HLLL")
+    Ut = torch.tensor(U.reshape(4, ny, nx), requires_grad=True)
+    R = S.residual(Ut)
+    (R * torch.tensor(lam.reshape(4, ny, nx))).sum().backward()
+    D = DeviceSolver(P, tableau=tableau("RK4"))
+    D.set_state(U)
+    assert np.array_equal(D.residual(), R.detach().numpy().reshape(4, -1))
+    got = D.residual_vjp(torch.tensor(lam, device="cuda")).cpu().numpy()
+    assert _rel(got, Ut.grad.numpy().reshape(4, -1)) < 1e-11
+
+
 def test_residual_vjp_non_cartesian_outlet():
     from pyhype_gb300._native import DeviceSolver
     from pyhype_gb300.adjoint import single_block_mesh

@@ -49,6 +49,60 @@ def test_fp32_density_l1_vs_fp64(name, steps, bound):
     assert S32.check_realizable().ok == 1
 
 
+def _seeded_problem(nx, ny, bx, by, flux="Roe", recon="ConservativeState", limiter="Venkatakrishnan"):
+    """Reflecting multiblock square, smooth waves with seeded cell noise on every
+    variable: no region is uniform, so the reference limiter's round-off switch
+    (psi = 0.75 exactly at davg == 0) plays no part and the FP32 form's own rounding
+    error shows."""
+    from pyhype_gb300.fluids import Air
+    from pyhype_gb300.mesh import RectagularMeshGenerator
+    from pyhype_gb300.problem import build_problem
+    from pyhype_gb300.states import ConservativeState, PrimitiveState
+
+    air = Air(a_inf=343.0, rho_inf=1.0)
+    mesh = RectagularMeshGenerator.generate(["Reflection"], ["Reflection"], ["Reflection"], ["Reflection"],
+                                            10.0, 0.0, 10.0, 0.0, bx, by)
+    P = build_problem(mesh.dict, nx, ny, flux=flux, limiter=limiter, recon=recon, gamma=air.gamma(),
+                      gm1=air.gamma() - 1, cfl=0.8, fluid=air)
+    rng = np.random.default_rng(nx * 31 + ny)
+    blocks = []
+    for g in P.block_geometry:
+        x, y, n = g.xc, g.yc, g.xc.shape
+        W = np.stack([1.2 * (1 + 0.3 * np.sin(0.9 * x) * np.cos(0.7 * y)) * (1 + rng.uniform(-0.02, 0.02, n)),
+                      60.0 * np.sin(0.5 * y + 0.3 * x) + rng.uniform(-3.4, 3.4, n),
+                      40.0 * np.cos(0.6 * x) + rng.uniform(-3.4, 3.4, n),
+                      101100.0 * (1 + 0.2 * np.cos(0.8 * x + 0.4 * y)) * (1 + rng.uniform(-0.02, 0.02, n))], axis=-1)
+        s = PrimitiveState(air, array=W).to_type(ConservativeState)
+        s.make_non_dimensional()
+        blocks.append(s.data)
+    return P, P.to_soa(blocks)
+
+
+@pytest.mark.parametrize("flux,recon", [("Roe", "ConservativeState"), ("HLLL", "PrimitiveState")])
+def test_fp32_seeded_state_l1_vs_fp64(flux, recon):
+    """On a state without uniform regions the FP32 form stays within 2e-6 (L1 density,
+    relative) of the FP64 path over 20 RK4 steps of a 2 x 2 x 96^2 problem, and its
+    conserved totals within 1e-6."""
+    from pyhype_gb300._native import DeviceSolver
+    from pyhype_gb300.time_marching import tableau
+
+    P, U0 = _seeded_problem(96, 96, 2, 2, flux, recon)
+    out, tot = [], []
+    for prec in (0, 1):
+        S = DeviceSolver(P.with_precision(prec), tableau=tableau("RK4"))
+        S.set_state(U0)
+        t, n = S.run(0.0, 1e30, max_steps=20)
+        assert n == 20
+        out.append(S.get_state())
+        tot.append(S.totals()[0])
+        S.close()
+    err = _l1_rel(out[1][0], out[0][0])
+    print(f"{flux}/{recon}: FP32 L1 density {err:.2e}, totals {np.abs(tot[1] - tot[0]) / np.abs(tot[0])}")
+    assert err < 2e-6, err
+    assert abs(tot[1][0] - tot[0][0]) <= 1e-6 * abs(tot[0][0])
+    assert abs(tot[1][3] - tot[0][3]) <= 1e-6 * abs(tot[0][3])
+
+
 def test_fp32_residual_close_to_fp64():
     z = G.load("ops_explosion_cons")
     P, S64, S32 = _pair(z)
