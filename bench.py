@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--skip-ensemble", action="store_true", help="omit the batched-ensemble section")
     ap.add_argument("--skip-adjoint", action="store_true", help="omit the adjoint section")
     ap.add_argument("--skip-dmr", action="store_true", help="omit the double-Mach-reflection section")
-    ap.add_argument("--stage-form", default="default", choices=["default", "split", "fused"],
+    ap.add_argument("--stage-form", default="default", choices=["default", "split", "fused28", "fused13"],
                     help="stage form of the --precision fp32 profiling run")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
                     help="arithmetic of the timed multiblock run (fp32: the FP32 form; for profiling)")
@@ -715,7 +715,7 @@ def main():
     if args.precision == "fp32":  # the FP32 form alone (profiling runs; the default line is FP64)
         S32 = _native.DeviceSolver(P.with_precision(1), tableau=solver._time_integrator.tableau())
         if args.stage_form != "default":
-            S32.set_kernel_choice(3, 1 if args.stage_form == "fused" else 0)
+            S32.set_kernel_choice(3, {"split": 0, "fused28": 1, "fused13": 2}[args.stage_form])
         S32.set_state(P.to_soa([b.state.data for b in solver.blocks]))
         t32, _ = S32.run(0.0, 1e30, max_steps=args.warmup)
         g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -823,24 +823,25 @@ def main():
     step_ms = ms / args.steps
     hbm_achieved = P.ncell * stages * BYTES_PER_CELL_STAGE_FP64 / (step_ms * 1e-3) / 1e9
 
-    # FP64 fused stage form on the same workload (for comparison; the line's value is
+    # FP64 fused stage forms on the same workload (for comparison; the line's value is
     # the default form)
-    fp64_fused = None
+    fp64_fused = {}
     try:
-        SF = _native.DeviceSolver(P, tableau=solver._time_integrator.tableau())
-        SF.set_stream(stream.cuda_stream)
-        SF.set_kernel_choice(3, 1)
-        SF.set_state(P.to_soa([b.state.data for b in solver.blocks]))
-        tf_, _ = SF.run(0.0, t_final, max_steps=args.warmup)
-        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        h0.record(stream)
-        SF.run(tf_, t_final, max_steps=args.steps)
-        h1.record(stream)
-        torch.cuda.synchronize()
-        fms = h0.elapsed_time(h1) / args.steps
-        fp64_fused = {"ms_per_step": fms, "value": P.ncell * stages / (fms * 1e-3),
-                      "speedup_vs_split": step_ms / fms}
-        SF.close()
+        for form, name in ((1, "fused28"), (2, "fused13")):
+            SF = _native.DeviceSolver(P, tableau=solver._time_integrator.tableau())
+            SF.set_stream(stream.cuda_stream)
+            SF.set_kernel_choice(3, form)
+            SF.set_state(P.to_soa([b.state.data for b in solver.blocks]))
+            tf_, _ = SF.run(0.0, t_final, max_steps=args.warmup)
+            h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            h0.record(stream)
+            SF.run(tf_, t_final, max_steps=args.steps)
+            h1.record(stream)
+            torch.cuda.synchronize()
+            fms = h0.elapsed_time(h1) / args.steps
+            fp64_fused[name] = {"ms_per_step": fms, "value": P.ncell * stages / (fms * 1e-3),
+                                "speedup_vs_split": step_ms / fms}
+            SF.close()
     except Exception as exc:
         fp64_fused = {"error": str(exc)}
 
@@ -849,7 +850,7 @@ def main():
     fp32 = None
     try:
         forms = {}
-        for form, name in ((0, "split"), (1, "fused")):
+        for form, name in ((0, "split"), (1, "fused28"), (2, "fused13")):
             S32 = _native.DeviceSolver(P.with_precision(1), tableau=solver._time_integrator.tableau())
             S32.set_stream(stream.cuda_stream)
             S32.set_kernel_choice(3, form)
@@ -863,7 +864,7 @@ def main():
             forms[name] = (max_over_ranks(g0.elapsed_time(g1), ws), S32.get_state(), S32)
         best = min(forms, key=lambda k: forms[k][0])
         ms32, U32, S32 = forms[best]
-        forms_equal = bool(np.array_equal(forms["split"][1], forms["fused"][1]))
+        forms_equal = all(bool(np.array_equal(forms["split"][1], v[1])) for v in forms.values())
         for k, v in forms.items():
             if k != best:
                 v[2].close()

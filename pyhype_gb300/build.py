@@ -23,7 +23,9 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hi
 # largest kernels compile in parallel.
 UNITS = {
     "e2d_fp64": ("e2d_fp64.cu", ["-fmad=false"]),
-    "e2d_fp32": ("e2d_fp32.cu", []),  # FP32 form: contraction allowed, its own division (e2d_device.cuh)
+    # the FP32 form's multiply-adds are explicit (fmaT in e2d_device.cuh): contraction off
+    # everywhere, so every kernel form evaluates the same operations
+    "e2d_fp32": ("e2d_fp32.cu", ["-fmad=false"]),
     "e2d_api": ("e2d_api.cu", ["-fmad=false"]),
     "e2d_bench": ("e2d_bench.cu", []),
     "e2d_noalloc": ("e2d_noalloc.cu", ["-fmad=false"]),
@@ -31,7 +33,7 @@ UNITS = {
 }
 for _lim in range(4):
     UNITS[f"e2d_recon_f64_l{_lim}"] = ("e2d_recon_unit.cu", ["-fmad=false", "-DE2D_T=double", f"-DE2D_LIM={_lim}"])
-    UNITS[f"e2d_recon_f32_l{_lim}"] = ("e2d_recon_unit.cu", ["-DE2D_T=float", f"-DE2D_LIM={_lim}"])
+    UNITS[f"e2d_recon_f32_l{_lim}"] = ("e2d_recon_unit.cu", ["-fmad=false", "-DE2D_T=float", f"-DE2D_LIM={_lim}"])
 
 
 def nvcc() -> str:

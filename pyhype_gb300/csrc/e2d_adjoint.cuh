@@ -442,7 +442,9 @@ __global__ void __launch_bounds__(TX * VTY, 4) k_reconstruct_vjp(ParamsT<T> P, c
     if (!tr.clipped) {
       const T lsl = lph * psi_deriv<LIM>(tr.sl);
       T ld = T(0), lden = T(0);
-      if (tr.sign != 0) {
+      // a slope in the capped region has psi constant (lsl = 0); its value may be +inf
+      // (an FP32 davg below the reciprocal's range), so it passes nothing back
+      if (tr.sign != 0 && lsl != T(0)) {
         ld = qdiv(lsl, tr.davg);
         lden = qdiv(-lsl * tr.sl, tr.davg);
       }

@@ -140,12 +140,12 @@ static int build_tma_t(E2DSolver* h, const T* base) {
   if (!enc) return 0;
   const int nb = (int)h->hblocks.size();
   // box rows: tile height + the 1-cell halo for the reconstruction kernel's tiles, and
-  // the fused stage kernel's 16 rows + its 2-cell halo
-  const int box_rows[4] = {4 + 2, 8 + 2, 16 + 2, FUSED_TY + 4};
+  // the fused stage kernel's tile rows + its 2-cell halo
+  const int box_rows[5] = {4 + 2, 8 + 2, 16 + 2, FUSED_TY[0] + 4, FUSED_TY[1] + 4};
   E2DSolver::TmaEntry entry{base, {}};
   std::vector<CUtensorMap> maps(nb);
   std::vector<int> ok(nb);
-  for (int r = 0; r < 4; ++r) {
+  for (int r = 0; r < 5; ++r) {
     for (int b = 0; b < nb; ++b) {
       const E2DBlock& B = h->hblocks[b];
       const uint64_t row = (uint64_t)B.nx * sizeof(T), plane = (uint64_t)h->ncell * sizeof(T);
@@ -173,7 +173,7 @@ static int build_tma_t(E2DSolver* h, const T* base) {
     if (int e = h->alloc(&dok, nb)) return e;
     CK(cudaMemcpy(dmaps, maps.data(), sizeof(CUtensorMap) * nb, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(dok, ok.data(), sizeof(int) * nb, cudaMemcpyHostToDevice));
-    entry.set.by_rty[r] = TmaTiles{dmaps, dok, h->tma_timeouts};
+    (r < 3 ? entry.set.by_rty[r] : entry.set.fused[r - 3]) = TmaTiles{dmaps, dok, h->tma_timeouts};
   }
   h->tma_reg.push_back(entry);
   return 0;
@@ -326,7 +326,8 @@ static int bench_kernels_t(E2DHandle h, int32_t steps, double* ms, int64_t* laun
       const T* in = p.S.buf[h->stage_input[s]];
       if (h->use_fused(s)) {
         CK(rec(5));
-        CK(launch_stage_fused<T>(p.P, h->ts, in, h->inst, p.S, h->prog[s], h->real, h->stream, h->tma_for(in), false));
+        CK(launch_stage_fused<T>(p.P, h->ts, h->ks.variant, in, h->inst, p.S, h->prog[s], h->real, h->stream,
+                                 h->tma_for(in), false));
         CK(fin());
         continue;
       }
@@ -453,7 +454,7 @@ static int time_kernel(E2DHandle h, int which, int reps, float* ms) {
       CK(launch_reconstruct<T>(p.P, h->ts, h->kr, p.S.buf[0], h->inst, p.F, nullptr, h->stream, h->tma_for(p.S.buf[0])));
     else if (which == 1) CK(launch_flux<T>(p.P, h->ts, h->kf, h->inst, p.F, nullptr, h->stream));
     else if (which == 2) CK(launch_update<T>(p.P, h->ts, h->ku, p.F, p.S, none, h->inst, h->real, nullptr, h->stream));
-    else CK(launch_stage_fused<T>(p.P, h->ts, p.S.buf[0], h->inst, p.S, none, h->real, h->stream,
+    else CK(launch_stage_fused<T>(p.P, h->ts, h->ks.variant, p.S.buf[0], h->inst, p.S, none, h->real, h->stream,
                                   h->tma_for(p.S.buf[0]), false));
   }
   CK(cudaEventRecord(e1, h->stream));
@@ -496,12 +497,22 @@ static int autotune_t(E2DHandle h, int reps, int32_t* chosen) {
     }
     split_ms += best_ms;
   }
-  // the three tuned kernels of one stage against one fused stage (no updates either way)
+  // the three tuned kernels of one stage against one fused stage of each tile height
+  // (no updates either way)
   h->ks = KernelChoice{0, false};
   if (h->cfg.nqp <= 1) {
-    float fused_ms = 0.f;
-    if (int e = time_kernel<T>(h, 3, reps, &fused_ms)) return e;
-    if (fused_ms < split_ms) h->ks = KernelChoice{1, false};
+    float best_ms = split_ms;
+    for (int form = 1; form < N_STAGE_FORMS; ++form) {
+      const KernelChoice keep = h->ks;
+      h->ks = KernelChoice{form, false};
+      float fused_ms = 0.f;
+      if (int e = time_kernel<T>(h, 3, reps, &fused_ms)) return e;
+      h->ks = keep;
+      if (fused_ms < best_ms) {
+        best_ms = fused_ms;
+        h->ks = KernelChoice{form, false};
+      }
+    }
   }
   if (chosen) {
     chosen[6] = h->ks.variant;
@@ -628,6 +639,20 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
       h->ts.cell[v] = d;
       h->ts.ncell[v] = (int)ct.size();
     }
+    for (int v = 0; v < 2; ++v) {  // the fused stage kernel's tiles
+      std::vector<int4> ct;
+      for (int b = 0; b < cfg->nblocks; ++b) {
+        const E2DBlock& B = h->hblocks[b];
+        for (int i0 = 0; i0 < B.ny; i0 += FUSED_TY[v])
+          for (int j0 = 0; j0 < B.nx; j0 += TX) ct.push_back(make_int4(b, i0, j0, 0));
+      }
+      int4* d = nullptr;
+      if (int e = h->alloc(&d, ct.size())) return bail(e);
+      if ((ce = cudaMemcpy(d, ct.data(), sizeof(int4) * ct.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail(fail(E2D_ERR_CUDA, "tile copy: %s", cudaGetErrorString(ce)));
+      h->ts.fused[v] = d;
+      h->ts.nfused[v] = (int)ct.size();
+    }
     std::vector<int4> ft;
     for (int b = 0; b < cfg->nblocks; ++b) {
       const E2DBlock& B = h->hblocks[b];
@@ -661,12 +686,13 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
     return bail(fail(E2D_ERR_CUDA, "counter init: %s", cudaGetErrorString(ce)));
 
   if (int e = E2D_DISPATCH(h, init_path)) return bail(e);
-  if ((ce = (h->prec == E2D_FP32 ? launch_stage_fused<float>(h->pf.P, h->ts, nullptr, h->inst, h->pf.S, StageProgram{},
-                                                             h->real, h->stream, nullptr, true)
-                                 : launch_stage_fused<double>(h->pd.P, h->ts, nullptr, h->inst, h->pd.S,
-                                                              StageProgram{}, h->real, h->stream, nullptr, true))) !=
-      cudaSuccess)
-    return bail(fail(E2D_ERR_CUDA, "fused stage kernel set-up: %s", cudaGetErrorString(ce)));
+  for (int form = 1; form < N_STAGE_FORMS; ++form)
+    if ((ce = (h->prec == E2D_FP32
+                   ? launch_stage_fused<float>(h->pf.P, h->ts, form, nullptr, h->inst, h->pf.S, StageProgram{}, h->real,
+                                               h->stream, nullptr, true)
+                   : launch_stage_fused<double>(h->pd.P, h->ts, form, nullptr, h->inst, h->pd.S, StageProgram{},
+                                                h->real, h->stream, nullptr, true))) != cudaSuccess)
+      return bail(fail(E2D_ERR_CUDA, "fused stage kernel set-up: %s", cudaGetErrorString(ce)));
 
   // default integrator: the classical RK4 rows (explicit_runge_kutta.py:212-224)
   const double rk4[16] = {0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1, 0, 1.0 / 6, 1.0 / 3, 1.0 / 3, 1.0 / 6};
@@ -766,7 +792,8 @@ static int enqueue_stages(E2DHandle h, T* dudt_out, const DebugOutT<T>* dbg) {
   for (int s = 0; s < h->nstages; ++s) {
     const T* in = p.S.buf[h->stage_input[s]];
     if (!dudt_out && !dbg && h->use_fused(s)) {
-      CK(launch_stage_fused<T>(p.P, h->ts, in, h->inst, p.S, h->prog[s], h->real, h->stream, h->tma_for(in), false));
+      CK(launch_stage_fused<T>(p.P, h->ts, h->ks.variant, in, h->inst, p.S, h->prog[s], h->real, h->stream,
+                               h->tma_for(in), false));
       continue;
     }
     CK(launch_reconstruct<T>(p.P, h->ts, h->kr, in, h->inst, p.F, dbg, h->stream, h->tma_for(in)));
@@ -1078,7 +1105,7 @@ int e2d_set_kernel_choice(E2DHandle h, int32_t kernel, int32_t variant, int32_t 
   const int nvar[4] = {N_RECON_VARIANTS, N_FLUX_VARIANTS, 1, N_STAGE_FORMS};
   if (kernel < 0 || kernel > 3 || variant < 0 || variant >= nvar[kernel])
     return fail(E2D_ERR_INVALID, "kernel %d has no variant %d", kernel, variant);
-  if (kernel == 3 && variant == 1 && h->cfg.nqp > 1)
+  if (kernel == 3 && variant >= 1 && h->cfg.nqp > 1)
     return fail(E2D_ERR_UNSUPPORTED, "the fused stage kernel has the one-point face rule only");
   KernelChoice* ch[4] = {&h->kr, &h->kf, &h->ku, &h->ks};
   *ch[kernel] = KernelChoice{variant, persistent != 0};

@@ -4,28 +4,30 @@
 // stage of every block, plus the stage's Butcher updates of
 // time_marching/explicit_runge_kutta.py:63-80).
 //
-// One CTA of 256 threads takes a tile of 16 rows x 32 columns of one block:
-//   staging   the tile and a 2-cell halo (20 x 36 cells, 4 planes) into shared memory:
+// One CTA of NW warps takes a tile of FTY rows x 32 columns of one block (two shapes:
+// 28 rows with 16 warps, 13 rows with 8 warps; in both the tile rows and the ring tasks
+// fill whole rounds of warps, so no warp idles through a reconstruction round):
+//   staging   the tile and a 2-cell halo (FTY + 4 rows x 36 columns, 4 planes) into shared memory:
 //             one TMA box load for tiles whose halo lies inside the block, plain loads
 //             with ghost cells formed on the fly (ghost_cons) for the others;
-//   faces     gradient and limiter of every tile cell and of the 96 cells of the ring
-//             around it (whose face states the tile's edge faces need); each tile cell
+//   faces     gradient and limiter of every tile cell and of the ring of cells around
+//             it (whose face states the tile's edge faces need); each tile cell
 //             writes its four limited face states, each ring cell the one facing the
 //             tile, rotated into the face frame and converted to primitive variables;
 //             block-boundary faces take their outside state from the boundary condition
 //             (outside_state), as in k_reconstruct;
-//   fluxes    one Riemann flux per face of the tile (528 vertical, 544 horizontal),
-//             rotated back and integrated, written over the face's left state;
+//   fluxes    one Riemann flux per face of the tile, rotated back and integrated,
+//             written over the face's left state;
 //   update    dUdt of every tile cell and the stage program (partial Butcher sums,
 //             Kahan-compensated last row on the FP32 path), positivity on the last stage.
 // Every value is computed by the same functions the split kernels use
 // (limit_cell_var, vface_prim/hface_prim, vface_flux/hface_flux, cell_dudt,
 // stage_program), so the two forms give the same results.
 //
-// The cost of fusion is the ring: gradient and limiter of 96 cells are computed by both
-// tiles that share them (19 % more reconstruction work at 32 x 16), and the 48 edge
-// faces of a tile by both tiles (4.5 % more fluxes).  What it saves is the face arrays'
-// round trip through HBM (four states and two fluxes per face) and two launches.
+// The cost of fusion is the ring: gradient and limiter of the 2 (32 + FTY) ring cells
+// are computed by both tiles that share them (13 % more reconstruction work at 28 rows,
+// 22 % at 13), and the tile's edge faces by both tiles.  What it saves is the face
+// arrays' round trip through HBM (four states and two fluxes per face) and two launches.
 //
 // A stage whose Butcher updates write its own input buffer (explicit Euler, a one-stage
 // tableau) cannot be fused: a tile would overwrite cells that its neighbours still read
@@ -35,11 +37,7 @@
 
 namespace e2d {
 
-constexpr int FTY = FUSED_TY;   // tile rows (the tile table of height 16)
-constexpr int FTHREADS = 256;   // 8 warps
-static_assert(FTY == 16 && FTHREADS == 256, "the ring task mapping assumes 16 rows and 8 warps");
-
-template <typename T>
+template <typename T, int FTY>
 struct FusedSmem {
   // tile + 2-cell halo in reconstruction variables; block row i0 - 2 + r at row r,
   // block column j0 - XO + c at column c (XO = 16 / sizeof(T), the TMA box's start)
@@ -53,12 +51,8 @@ struct FusedSmem {
   T hR[4][FTY + 1][TX];
 };
 
-template <typename T>
-__device__ __forceinline__ void put4(T (&a)[4][FTY][TX + 1], int r, int c, const T* w) {
-  a[0][r][c] = w[0]; a[1][r][c] = w[1]; a[2][r][c] = w[2]; a[3][r][c] = w[3];
-}
-template <typename T>
-__device__ __forceinline__ void put4(T (&a)[4][FTY + 1][TX], int r, int c, const T* w) {
+template <typename T, int R, int C>
+__device__ __forceinline__ void put4(T (&a)[4][R][C], int r, int c, const T* w) {
   a[0][r][c] = w[0]; a[1][r][c] = w[1]; a[2][r][c] = w[2]; a[3][r][c] = w[3];
 }
 
@@ -67,8 +61,8 @@ enum { FACE_E = 1, FACE_W = 2, FACE_N = 4, FACE_S = 8 };
 // Gradient, limiter and the face states `which` of the cell at tile-local (lr, lc),
 // lr in [-1, FTY], lc in [-1, TX]; a tile cell (own = true) also writes the outside
 // states of its block-boundary faces.
-template <typename T, int LIM, int RECON>
-__device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G, const E2DBlock* B, FusedSmem<T>& sm,
+template <typename T, int LIM, int RECON, int FTY>
+__device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G, const E2DBlock* B, FusedSmem<T, FTY>& sm,
                                            int i0, int j0, int lr, int lc, int which, bool own, double t) {
   constexpr int XO = TileCols<T>::XO;
   const int i = i0 + lr, j = j0 + lc;
@@ -124,13 +118,16 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
   }
 }
 
-template <typename T, int LIM, int RECON, int FLUX, int MINB>
-__global__ void __launch_bounds__(FTHREADS, MINB)
+template <typename T, int LIM, int RECON, int FLUX, int FTY, int NW, int MINB>
+__global__ void __launch_bounds__(NW * 32, MINB)
     k_stage_fused(ParamsT<T> P, const int4* __restrict__ tiles, const T* __restrict__ U,
                   InstanceState* __restrict__ inst, StateBuffersT<T> S, StageProgram prog,
                   RealizState* __restrict__ real, TmaTiles tma) {
+  constexpr int FTHREADS = NW * 32;
+  constexpr int RING_COL_TASKS = (2 * FTY + 31) / 32;  // the W and E ring columns, 32 cells a task
+  static_assert(FTY + 2 + RING_COL_TASKS <= 2 * NW, "tile rows and ring tasks must fill two rounds of warps");
   extern __shared__ __align__(128) unsigned char e2d_fused_smem[];
-  FusedSmem<T>& sm = *reinterpret_cast<FusedSmem<T>*>(e2d_fused_smem);
+  FusedSmem<T, FTY>& sm = *reinterpret_cast<FusedSmem<T, FTY>*>(e2d_fused_smem);
   __shared__ __align__(8) unsigned long long bar;
   constexpr int XO = TileCols<T>::XO;
   const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
@@ -196,7 +193,7 @@ __global__ void __launch_bounds__(FTHREADS, MINB)
   // One call site for every kind of task (the reconstruction is the kernel's largest
   // piece of code; four inlined copies of it crowded the instruction cache).
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int task = warp; task < FTY + 3; task += FTHREADS / 32) {
+  for (int task = warp; task < FTY + 2 + RING_COL_TASKS; task += NW) {
     int lr, lc, which;
     bool live;
     if (task < FTY) {  // a tile row: all four faces, and block-boundary outside states
@@ -214,14 +211,15 @@ __global__ void __launch_bounds__(FTHREADS, MINB)
       lc = lane;
       which = FACE_S;
       live = i0 + FTY < ny && j0 + lc < nx;
-    } else {  // the ring columns: west (lanes 0-15, east faces), east (16-31, west faces)
-      lr = lane & 15;
-      const bool east = lane >= 16;
+    } else {  // the ring columns: west (ring cells 0..FTY-1: east faces), then east (west faces)
+      const int q = (task - FTY - 2) * 32 + lane;
+      const bool east = q >= FTY;
+      lr = east ? q - FTY : q;
       lc = east ? TX : -1;
       which = east ? FACE_W : FACE_E;
-      live = i0 + lr < ny && (east ? j0 + TX < nx : j0 >= 1);
+      live = q < 2 * FTY && i0 + lr < ny && (east ? j0 + TX < nx : j0 >= 1);
     }
-    if (live) fused_cell<T, LIM, RECON>(P, G, B, sm, i0, j0, lr, lc, which, task < FTY, t);
+    if (live) fused_cell<T, LIM, RECON, FTY>(P, G, B, sm, i0, j0, lr, lc, which, task < FTY, t);
   }
   __syncthreads();
 
@@ -265,11 +263,11 @@ __global__ void __launch_bounds__(FTHREADS, MINB)
   // ---- dUdt and the stage program of every tile cell --------------------------------
   int nbad = 0;
 #pragma unroll
-  for (int round = 0; round < FTY / (FTHREADS / 32); ++round) {
-    const int r = warp + round * (FTHREADS / 32);
+  for (int round = 0; round < (FTY + NW - 1) / NW; ++round) {  // every thread runs every round
+    const int r = warp + round * NW;
     const int i = i0 + r, j = j0 + lane;
     bool bad = false;
-    if (i < ny && j < nx) {
+    if (r < FTY && i < ny && j < nx) {
       const int64_t c = cell_at(B, i, j);
       const T A = P.geo.cell[E2D_G_A][c];
       T k[4];
@@ -292,28 +290,39 @@ __global__ void __launch_bounds__(FTHREADS, MINB)
 }
 
 // ---- launchers --------------------------------------------------------------------------
-template <typename T, int LIM, int RECON, int FLUX>
+template <typename T, int LIM, int RECON, int FLUX, int FORM>
 static cudaError_t fused_launch(const ParamsT<T>& P, const TileSet& ts, const T* U, InstanceState* inst,
                                 StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
                                 const TmaSet* tset, bool prepare_only) {
-  constexpr int MINB = sizeof(T) == 4 ? 4 : 2;  // 64 / 128 registers per thread
-  auto kern = k_stage_fused<T, LIM, RECON, FLUX, MINB>;
-  constexpr int bytes = (int)sizeof(FusedSmem<T>);
+  constexpr int FTY = FUSED_TY[FORM], NW = FUSED_WARPS[FORM];
+  // CTAs an SM holds at 64 registers a thread (FP32) or 128 (FP64): 65536 / (regs x NW x 32)
+  constexpr int MINB = (sizeof(T) == 4 ? 32 : 16) / NW;
+  auto kern = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB>;
+  constexpr int bytes = (int)sizeof(FusedSmem<T, FTY>);
   if (prepare_only) return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  const TmaTiles tma = tset ? tset->by_rty[3] : TmaTiles{nullptr, nullptr, nullptr};
-  kern<<<ts.ncell[2], FTHREADS, bytes, st>>>(P, ts.cell[2], U, inst, S, prog, real, tma);
+  const TmaTiles tma = tset ? tset->fused[FORM] : TmaTiles{nullptr, nullptr, nullptr};
+  if (ts.nfused[FORM] <= 0) return cudaSuccess;
+  kern<<<ts.nfused[FORM], NW * 32, bytes, st>>>(P, ts.fused[FORM], U, inst, S, prog, real, tma);
   return cudaGetLastError();
 }
 
+template <typename T, int LIM, int RECON, int FLUX>
+static cudaError_t fused_form(const ParamsT<T>& P, const TileSet& ts, int form, const T* U, InstanceState* inst,
+                              StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
+                              const TmaSet* tma, bool prepare_only) {
+  if (form == 2) return fused_launch<T, LIM, RECON, FLUX, 1>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);
+  return fused_launch<T, LIM, RECON, FLUX, 0>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);
+}
+
 template <typename T, int LIM>
-cudaError_t fused_lim(const ParamsT<T>& P, const TileSet& ts, const T* U, InstanceState* inst, StateBuffersT<T> S,
-                      const StageProgram& prog, RealizState* real, cudaStream_t st, const TmaSet* tma,
-                      bool prepare_only) {
+cudaError_t fused_lim(const ParamsT<T>& P, const TileSet& ts, int form, const T* U, InstanceState* inst,
+                      StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
+                      const TmaSet* tma, bool prepare_only) {
 #define E2D_FUSED_FLUX(RC)                                                                                          \
   switch (P.flux) {                                                                                                 \
-    case E2D_FLUX_HLLL: return fused_launch<T, LIM, RC, E2D_FLUX_HLLL>(P, ts, U, inst, S, prog, real, st, tma, prepare_only); \
-    case E2D_FLUX_HLLE: return fused_launch<T, LIM, RC, E2D_FLUX_HLLE>(P, ts, U, inst, S, prog, real, st, tma, prepare_only); \
-    default: return fused_launch<T, LIM, RC, E2D_FLUX_ROE>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);   \
+    case E2D_FLUX_HLLL: return fused_form<T, LIM, RC, E2D_FLUX_HLLL>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only); \
+    case E2D_FLUX_HLLE: return fused_form<T, LIM, RC, E2D_FLUX_HLLE>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only); \
+    default: return fused_form<T, LIM, RC, E2D_FLUX_ROE>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only);   \
   }
   if (P.recon == E2D_RECON_PRIMITIVE) {
     E2D_FUSED_FLUX(E2D_RECON_PRIMITIVE)
@@ -323,7 +332,7 @@ cudaError_t fused_lim(const ParamsT<T>& P, const TileSet& ts, const T* U, Instan
 }
 
 #define E2D_FUSED_LIM_DECL(PRE, T, LIM)                                                                           \
-  PRE template cudaError_t fused_lim<T, LIM>(const ParamsT<T>&, const TileSet&, const T*, InstanceState*,         \
+  PRE template cudaError_t fused_lim<T, LIM>(const ParamsT<T>&, const TileSet&, int, const T*, InstanceState*,    \
                                              StateBuffersT<T>, const StageProgram&, RealizState*, cudaStream_t,   \
                                              const TmaSet*, bool);
 #define E2D_EXTERN_FUSED_LIM(T)    \
@@ -332,25 +341,25 @@ cudaError_t fused_lim(const ParamsT<T>& P, const TileSet& ts, const T* U, Instan
   E2D_FUSED_LIM_DECL(extern, T, 2) \
   E2D_FUSED_LIM_DECL(extern, T, 3)
 
-// One stage (one-point face rule) in one launch; prepare_only sets the kernel's shared
-// memory limit and launches nothing (done once when a handle is created, outside any
-// stream capture).
+// One stage (one-point face rule) in one launch at stage form `form` (1: FUSED_TY[0]
+// rows, 2: FUSED_TY[1] rows); prepare_only sets the kernel's shared memory limit and
+// launches nothing (done once when a handle is created, outside any stream capture).
 template <typename T>
-cudaError_t launch_stage_fused(const ParamsT<T>& P, const TileSet& ts, const T* U, InstanceState* inst,
+cudaError_t launch_stage_fused(const ParamsT<T>& P, const TileSet& ts, int form, const T* U, InstanceState* inst,
                                StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
                                const TmaSet* tma, bool prepare_only) {
-  if (ts.ncell[2] <= 0) return cudaSuccess;
   switch (P.limiter) {
     case E2D_LIM_BARTH_JESPERSEN:
-      return fused_lim<T, E2D_LIM_BARTH_JESPERSEN>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);
-    case E2D_LIM_VAN_ALBADA: return fused_lim<T, E2D_LIM_VAN_ALBADA>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);
-    case E2D_LIM_VAN_LEER: return fused_lim<T, E2D_LIM_VAN_LEER>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);
-    default: return fused_lim<T, E2D_LIM_VENKATAKRISHNAN>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);
+      return fused_lim<T, E2D_LIM_BARTH_JESPERSEN>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only);
+    case E2D_LIM_VAN_ALBADA:
+      return fused_lim<T, E2D_LIM_VAN_ALBADA>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only);
+    case E2D_LIM_VAN_LEER: return fused_lim<T, E2D_LIM_VAN_LEER>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only);
+    default: return fused_lim<T, E2D_LIM_VENKATAKRISHNAN>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only);
   }
 }
 
 #define E2D_INSTANTIATE_FUSED_LAUNCHER(T)                                                                        \
-  template cudaError_t launch_stage_fused<T>(const ParamsT<T>&, const TileSet&, const T*, InstanceState*,         \
+  template cudaError_t launch_stage_fused<T>(const ParamsT<T>&, const TileSet&, int, const T*, InstanceState*,    \
                                              StateBuffersT<T>, const StageProgram&, RealizState*, cudaStream_t,  \
                                              const TmaSet*, bool);
 

@@ -12,7 +12,10 @@ namespace e2d {
 constexpr int TX = 32;        // cell tile width  (one warp along x)
 constexpr int TY = 8;         // cell tile height
 constexpr int MAX_STAGES = 8;
-constexpr int FUSED_TY = 16;  // tile rows of the fused stage kernel (e2d_fused.cuh)
+// tile heights of the fused stage kernel (e2d_fused.cuh): 28 rows for 16 warps and 13
+// rows for 8 warps, where the tile rows and the ring tasks fill whole rounds of warps
+constexpr int FUSED_TY[2] = {28, 13};
+constexpr int FUSED_WARPS[2] = {16, 8};
 
 // Device view of the geometry planes (in the arithmetic type of the path).
 template <typename T>
@@ -118,11 +121,13 @@ using Params = ParamsT<double>;
 using StateBuffers = StateBuffersT<double>;
 using DebugOut = DebugOutT<double>;
 
-// Tile tables: cell tiles for tile heights 4, 8 and 16 (index 0..2), face-node tiles
-// at height 8.  Each entry is (block, i0, j0, 0).
+// Tile tables: cell tiles for tile heights 4, 8 and 16 (index 0..2), the fused stage
+// kernel's tiles (FUSED_TY), face-node tiles at height 8.  Each entry is (block, i0, j0, 0).
 struct TileSet {
   const int4* cell[3];
   int ncell[3];
+  const int4* fused[2];
+  int nfused[2];
   const int4* face;
   int nface;
 };
@@ -148,9 +153,10 @@ struct TileCols {
   static constexpr int C0 = XO - 1;
 };
 // the three tile heights (4, 8, 16) of one state buffer, and the fused stage kernel's
-// box (16 rows and a 2-cell halo: 20 rows) at index 3
+// boxes (its tile rows and a 2-cell halo)
 struct TmaSet {
-  TmaTiles by_rty[4];
+  TmaTiles by_rty[3];
+  TmaTiles fused[2];
 };
 
 // Kernel variant chosen by the autotuner (0 = default) and persistent-grid flag.
@@ -160,7 +166,8 @@ struct KernelChoice {
 };
 constexpr int N_RECON_VARIANTS = 6;  // (tile height, min CTAs/SM): (8,2) (8,1) (4,2) (4,4) (16,1), (4,8) FP32 only
 constexpr int N_FLUX_VARIANTS = 3;   // min CTAs/SM: 4, 1, 6
-constexpr int N_STAGE_FORMS = 2;     // 0: three kernels per stage, 1: the fused stage kernel
+constexpr int N_STAGE_FORMS = 3;     // 0: three kernels per stage; 1, 2: the fused stage kernel at
+                                     // FUSED_TY[0] / FUSED_TY[1] rows
 
 // launchers, instantiated for double (e2d_fp64.cu) and float (e2d_fp32.cu)
 template <typename T>
@@ -189,7 +196,7 @@ cudaError_t launch_ghost_layer(const ParamsT<T>& P, const T* U, double t, const 
 // one RK stage in one launch (e2d_fused.cuh); prepare_only sets the kernel's shared
 // memory limit on the current device and launches nothing
 template <typename T>
-cudaError_t launch_stage_fused(const ParamsT<T>& P, const TileSet& ts, const T* U, InstanceState* inst,
+cudaError_t launch_stage_fused(const ParamsT<T>& P, const TileSet& ts, int form, const T* U, InstanceState* inst,
                                StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
                                const TmaSet* tma, bool prepare_only);
 cudaError_t launch_begin_step(InstanceState* inst, int ninst, double cfl, int use_min, cudaStream_t st);

@@ -63,10 +63,10 @@ struct E2DSolver {
   e2d::KernelChoice kr{0, false};     // reconstruct variant (autotuned)
   e2d::KernelChoice kf{0, false};     // flux variant
   e2d::KernelChoice ku{0, false};     // update variant
-  e2d::KernelChoice ks{0, false};     // stage form: 0 three kernels, 1 the fused stage kernel
+  e2d::KernelChoice ks{0, false};     // stage form: 0 three kernels, 1 and 2 the fused stage kernel
   // per stage: its Butcher updates leave its input buffer alone, so it may be fused
   std::vector<int> fusable;
-  bool use_fused(int s) const { return ks.variant == 1 && cfg.nqp <= 1 && fusable[s]; }
+  bool use_fused(int s) const { return ks.variant >= 1 && cfg.nqp <= 1 && fusable[s]; }
   int nbuf = 0;
   e2d::InstanceState* inst = nullptr;
   std::vector<e2d::InstanceState> hinst;

@@ -187,8 +187,9 @@ __device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, con
   // interface averages (quad_block.py:181-218) and Green-Gauss (greengauss.py:137-155)
   const T ie = half(w0 + ea), iw = half(we + w0);
   const T in = half(w0 + no), is = half(so + w0);
-  const T gx = (ie * g.LcE + iw * (-g.LcW) + in * g.LcN + is * (-g.LcS)) * g.ia;
-  const T gy = (ie * g.LsE + iw * (-g.LsW) + in * g.LsN + is * (-g.LsS)) * g.ia;
+  // ((ie LcE + iw (-LcW)) + in LcN) + is (-LcS), times 1/A
+  const T gx = fmaT(is, -g.LcS, fmaT(in, g.LcN, fmaT(ie, g.LcE, iw * (-g.LcW)))) * g.ia;
+  const T gy = fmaT(is, -g.LsS, fmaT(in, g.LsN, fmaT(ie, g.LsE, iw * (-g.LsW)))) * g.ia;
   // limiter (limiters/base.py:47-221)
   const T dmax = vmax(vmax(vmax(vmax(w0, we), ea), so), no) - w0;
   const T dmin = vmin(vmin(vmin(vmin(w0, we), ea), so), no) - w0;
@@ -200,7 +201,7 @@ __device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, con
     double davg[4];
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-      hot[s] = gx * g.hx[s] + gy * g.hy[s];
+      hot[s] = fmaT(gx, g.hx[s], gy * g.hy[s]);
       davg[s] = (w0 + hot[s]) - w0;
     }
     const SlopePick k = pick_slopes<LIM>(dmax, dmin, davg);
@@ -228,7 +229,7 @@ __device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, con
     const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-      hot[s] = gx * g.hx[s] + gy * g.hy[s];
+      hot[s] = fmaT(gx, g.hx[s], gy * g.hy[s]);
       const T davg = (fabs(hot[s]) < half_ulp64) ? T(0) : hot[s];
       const T sl = slope32(dmax, dmin, davg);
       smin = (s == 0) ? sl : vmin(smin, sl);
@@ -239,7 +240,7 @@ __device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, con
   }
   ph = is_neg(ph) ? T(0) : ph;
 #pragma unroll
-  for (int s = 0; s < 4; ++s) fv[s] = w0 + ph * hot[s];
+  for (int s = 0; s < 4; ++s) fv[s] = fmaT(ph, hot[s], w0);
   gx_out = gx;
   gy_out = gy;
   ph_out = ph;
@@ -314,14 +315,14 @@ __device__ __forceinline__ void stage_program(const ParamsT<T>& P, const StateBu
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const T base = up.src_zero ? T(0) : src[v * P.ncell + c];
-        dst[v * P.ncell + c] = base + dta * k[v];
+        dst[v * P.ncell + c] = fmaT(dta, k[v], base);
       }
     } else {
       // U^{n+1} = U^n + increment with Kahan compensation carried across steps
       T* U0 = S.buf[0];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        const T inc = (up.src_zero ? T(0) : src[v * P.ncell + c]) + dta * k[v];
+        const T inc = fmaT(dta, k[v], up.src_zero ? T(0) : src[v * P.ncell + c]);
         const T y = inc - S.comp[v * P.ncell + c];
         const T u0 = U0[v * P.ncell + c];
         const T tt = u0 + y;
@@ -585,8 +586,8 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_qp(ParamsT<T> P, const 
     const T no = sW[v][ty + 2][tx + 1];
     const T ie = half(w0 + ea), iw = half(we + w0);
     const T in = half(w0 + no), is = half(so + w0);
-    const T gx = (ie * LcE + iw * (-LcW) + in * LcN + is * (-LcS)) * ia;
-    const T gy = (ie * LsE + iw * (-LsW) + in * LsN + is * (-LsS)) * ia;
+    const T gx = fmaT(is, -LcS, fmaT(in, LcN, fmaT(ie, LcE, iw * (-LcW)))) * ia;
+    const T gy = fmaT(is, -LsS, fmaT(in, LsN, fmaT(ie, LsE, iw * (-LsW)))) * ia;
     const T dmax = vmax(vmax(vmax(vmax(w0, we), ea), so), no) - w0;
     const T dmin = vmin(vmin(vmin(vmin(w0, we), ea), so), no) - w0;
     T ph = T(0);
@@ -595,7 +596,7 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_qp(ParamsT<T> P, const 
     for (int s = 0; s < 4; ++s)
 #pragma unroll
       for (int q = 0; q < NQP; ++q) {
-        const T hot = gx * P.geo.qp[q][s][c] + gy * P.geo.qp[q][4 + s][c];
+        const T hot = fmaT(gx, P.geo.qp[q][s][c], gy * P.geo.qp[q][4 + s][c]);
         if constexpr (sizeof(T) == 4) {
           const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
           dv[s * NQP + q] = (fabs(hot) < half_ulp64) ? T(0) : hot;
@@ -635,8 +636,8 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_qp(ParamsT<T> P, const 
       T fq[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        const T hot = gxs[v] * P.geo.qp[q][s][c] + gys[v] * P.geo.qp[q][4 + s][c];
-        fq[v] = sW[v][ty + 1][tx + 1] + phs[v] * hot;
+        const T hot = fmaT(gxs[v], P.geo.qp[q][s][c], gys[v] * P.geo.qp[q][4 + s][c]);
+        fq[v] = fmaT(phs[v], hot, sW[v][ty + 1][tx + 1]);
       }
       const bool vert = s == E2D_E || s == E2D_W;
       const int64_t f = s == E2D_E ? fE : s == E2D_W ? fW : s == E2D_N ? fN : fS;
@@ -719,7 +720,7 @@ __global__ void __launch_bounds__(TX * TY) k_flux_qp(ParamsT<T> P, const int4* _
         else unrotate(Fq, fc, fs);
       }
 #pragma unroll
-      for (int v = 0; v < 4; ++v) acc[v] = acc[v] + P.qw[q] * Fq[v];
+      for (int v = 0; v < 4; ++v) acc[v] = fmaT(P.qw[q], Fq[v], acc[v]);
     }
     const T len = vert ? P.geo.vface[E2D_F_L][f] : P.geo.hface[E2D_F_L][f];
     T Iv[4] = {len * acc[0], len * acc[1], len * acc[2], len * acc[3]};

@@ -20,23 +20,25 @@ from oracle.oracle import Oracle
 pytestmark = pytest.mark.gpu
 
 ONE_POINT = [c for c in G.cases() if int(G.load(c)["nqp"] if "nqp" in G.load(c).files else 1) == 1]
-STAGE, FUSED = 3, 1
+STAGE = 3
+FORMS = [1, 2]  # the fused stage kernel with 28-row and 13-row tiles
 
 
-def _fused_solver(P, tableau):
+def _fused_solver(P, tableau, form=1):
     from pyhype_gb300._native import DeviceSolver
 
     S = DeviceSolver(P, tableau=tableau)
-    S.set_kernel_choice(STAGE, FUSED)
+    S.set_kernel_choice(STAGE, form)
     return S
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("name", ONE_POINT)
-def test_fused_steps_vs_reference(name):
+def test_fused_steps_vs_reference(name, form):
     """Per step: dt equal to the reference's, state fingerprint equal."""
     z = G.load(name)
     P = G.problem(z)
-    S = _fused_solver(P, z["tableau"])
+    S = _fused_solver(P, z["tableau"], form)
     S.set_state(P.to_soa(list(z["ic"])))
     t, tf = 0.0, G.t_final(z)
     for step in range(1, int(z["steps"]) + 1):
@@ -50,12 +52,13 @@ def test_fused_steps_vs_reference(name):
     S.close()
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("name", ["p100", "m2x4_150", "dmr5", "wedge", "jet", "bc_mixed"])
-def test_fused_device_loop_vs_reference(name):
+def test_fused_device_loop_vs_reference(name, form):
     """The graph-replayed device loop with fused stages reproduces the reference's run."""
     z = G.load(name)
     P = G.problem(z)
-    S = _fused_solver(P, z["tableau"])
+    S = _fused_solver(P, z["tableau"], form)
     S.set_state(P.to_soa(list(z["ic"])))
     n = int(z["steps"])
     t, steps = S.run(0.0, G.t_final(z), max_steps=n)
@@ -64,13 +67,14 @@ def test_fused_device_loop_vs_reference(name):
     S.close()
 
 
-def _run(P, U, a, steps, fused, tma=True):
+def _run(P, U, a, steps, form, tma=True):
+    """``steps`` steps of the device loop at stage form ``form`` (0 split, 1 / 2 fused)."""
     from pyhype_gb300._native import DeviceSolver, load
 
     L = load()
     L.e2d_bench_set_tma.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     S = DeviceSolver(P, tableau=a)
-    S.set_kernel_choice(STAGE, FUSED if fused else 0)
+    S.set_kernel_choice(STAGE, int(form))
     assert L.e2d_bench_set_tma(S.h, 1 if tma else 0) == 0
     S.set_state(U)
     t, n = S.run(0.0, 1e30, max_steps=steps)
@@ -82,18 +86,21 @@ def _run(P, U, a, steps, fused, tma=True):
 
 @pytest.mark.parametrize("name", [c for c in ONE_POINT if c != "m2x4_150"])
 def test_fp32_fused_equals_split(name):
-    """The FP32 form: fused and three-kernel stages give the same bits."""
+    """The FP32 form: fused (both tile shapes) and three-kernel stages give the same bits."""
     z = G.load(name)
     P = G.problem(z, precision=1)
     U = P.to_soa(list(z["ic"]))
     steps = min(int(z["steps"]), 6)
-    a, b = _run(P, U, z["tableau"], steps, True), _run(P, U, z["tableau"], steps, False)
-    assert np.array_equal(a, b), f"max diff {np.max(np.abs(a - b))}"
+    b = _run(P, U, z["tableau"], steps, 0)
+    for form in FORMS:
+        a = _run(P, U, z["tableau"], steps, form)
+        assert np.array_equal(a, b), f"form {form}: max diff {np.max(np.abs(a - b))}"
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("recon", ["ConservativeState", "PrimitiveState"])
-def test_fused_tma_equals_plain_staging(precision, recon):
+def test_fused_tma_equals_plain_staging(precision, recon, form):
     """Interior tiles staged by one TMA box load and by plain loads agree bit for bit,
     on blocks large enough for interior tiles (2x2 blocks of 96 x 80)."""
     from test_gpu_tma import _problem, _state
@@ -103,18 +110,18 @@ def test_fused_tma_equals_plain_staging(precision, recon):
     P = _problem(96, 80, 2, 2, recon=recon, precision=precision)
     U = _state(P, seed=7)
     a = tableau("RK4")
-    on, off = _run(P, U, a, 3, True, tma=True), _run(P, U, a, 3, True, tma=False)
+    on, off = _run(P, U, a, 3, form, tma=True), _run(P, U, a, 3, form, tma=False)
     assert np.array_equal(on, off)
-    if precision == 0:
-        assert np.array_equal(on, _run(P, U, a, 3, False))
+    assert np.array_equal(on, _run(P, U, a, 3, 0))
 
 
 SHAPES = [(17, 23, 2, 2), (2, 40, 1, 1), (40, 2, 1, 1), (34, 9, 1, 2), (66, 70, 3, 1), (33, 65, 2, 1),
-          (100, 37, 1, 2), (31, 18, 2, 1)]
+          (100, 37, 1, 2), (31, 18, 2, 1), (1, 30, 2, 1), (45, 1, 1, 2), (70, 62, 1, 1)]
 
 
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("nx,ny,bx,by", SHAPES)
-def test_fused_shapes_equal_oracle(nx, ny, bx, by):
+def test_fused_shapes_equal_oracle(nx, ny, bx, by, form):
     """Partial tiles, blocks thinner than the halo, odd row lengths: value-exact against
     the oracle over three RK4 steps (FP64), and the FP32 form equal to its split form."""
     from test_gpu_tma import _problem, _state
@@ -125,7 +132,7 @@ def test_fused_shapes_equal_oracle(nx, ny, bx, by):
     U = _state(P, seed=nx * 7 + ny)
     a = tableau("RK4")
     O = Oracle(P)
-    S = _fused_solver(P, a)
+    S = _fused_solver(P, a, form)
     S.set_state(U)
     Uo = U
     t = 0.0
@@ -138,7 +145,7 @@ def test_fused_shapes_equal_oracle(nx, ny, bx, by):
     assert np.array_equal(S.get_state(), Uo)
     S.close()
     P32 = P.with_precision(1)
-    assert np.array_equal(_run(P32, U, a, 3, True), _run(P32, U, a, 3, False))
+    assert np.array_equal(_run(P32, U, a, 3, form), _run(P32, U, a, 3, 0))
 
 
 @pytest.mark.parametrize("precision", [0, 1])
@@ -148,13 +155,13 @@ def test_fused_batched_equals_split(precision):
 
     inst = explosion_ensemble(count=6, seed=3, sizes=(64, 96, 128))
     out = []
-    for fused in (True, False):
+    for form in FORMS + [0]:
         B = EnsembleSolver(inst, precision=precision)
-        B.device.set_kernel_choice(STAGE, FUSED if fused else 0)
+        B.device.set_kernel_choice(STAGE, form)
         B.run(10)
         out.append(np.concatenate([s.ravel() for s in B.states()]))
         B.device.close()
-    assert np.array_equal(out[0], out[1])
+    assert np.array_equal(out[0], out[2]) and np.array_equal(out[1], out[2])
 
 
 def test_explicit_euler_stays_split_and_exact():
@@ -177,6 +184,6 @@ def test_fused_rejected_with_quadrature_points():
     P = G.problem(z)
     S = DeviceSolver(P, tableau=z["tableau"])
     with pytest.raises(E2DError) as e:
-        S.set_kernel_choice(STAGE, FUSED)
+        S.set_kernel_choice(STAGE, 1)
     assert e.value.code == E2D_ERR_UNSUPPORTED
     S.close()

@@ -109,7 +109,7 @@ def test_run_stops_at_t_final():
     assert np.array_equal(S.get_state(), Ut)
 
 
-@pytest.mark.parametrize("kernel,variants", [(0, range(6)), (1, range(3)), (2, range(1)), (3, range(2))])
+@pytest.mark.parametrize("kernel,variants", [(0, range(6)), (1, range(3)), (2, range(1)), (3, range(3))])
 @pytest.mark.parametrize("persistent", [False, True])
 def test_kernel_variants_bitwise(kernel, variants, persistent):
     """Every autotuner variant (tile height, occupancy target, persistent grid)
