@@ -45,6 +45,23 @@
 
 #define OR_API __attribute__((visibility("default")))
 
+/* Work arrays kept across calls, one per slot, grown when a larger problem needs more
+   and never freed: a residual of a 1024 x 1024 block needs about 512 MB of them, and
+   allocating that afresh in every call made the oracle's timings measure page faults,
+   not arithmetic.  The contents do not carry over (every use writes before it reads).
+   Not thread-safe: the oracle is driven from one host thread. */
+enum { WORK_SLOTS = 32 };
+static void* work_get(int slot, size_t bytes) {
+  static void* ptr[WORK_SLOTS];
+  static size_t cap[WORK_SLOTS];
+  if (bytes > cap[slot]) {
+    free(ptr[slot]);
+    ptr[slot] = malloc(bytes);
+    cap[slot] = ptr[slot] ? bytes : 0;
+  }
+  return ptr[slot];
+}
+
 typedef struct {
   const E2DConfig* cfg;
   const E2DBlock* blk;
@@ -467,19 +484,19 @@ static void block_residual(const Ctx* C, int b, const double* U, double t, doubl
 #define HOT(side, q, v) ((((side) * nqp + (q)) * 4 + (v)) * n)
 
   Scratch S;
-  S.W = malloc(sizeof(double) * 4 * n);
-  S.gE = malloc(sizeof(double) * 4 * ny); S.gW = malloc(sizeof(double) * 4 * ny);
-  S.gN = malloc(sizeof(double) * 4 * nx); S.gS = malloc(sizeof(double) * 4 * nx);
-  S.oE = malloc(sizeof(double) * 4 * nqp * ny); S.oW = malloc(sizeof(double) * 4 * nqp * ny);
-  S.oN = malloc(sizeof(double) * 4 * nqp * nx); S.oS = malloc(sizeof(double) * 4 * nqp * nx);
-  S.iEW = malloc(sizeof(double) * 4 * nv);
-  S.iNS = malloc(sizeof(double) * 4 * nh);
-  S.gx = malloc(sizeof(double) * 4 * n); S.gy = malloc(sizeof(double) * 4 * n);
-  S.hot = malloc(sizeof(double) * 16 * nqp * n);
-  S.phi = malloc(sizeof(double) * 4 * n);
-  S.face = malloc(sizeof(double) * 16 * nqp * n);
-  S.vf = malloc(sizeof(double) * 4 * nqp * nv);
-  S.hf = malloc(sizeof(double) * 4 * nqp * nh);
+  S.W = work_get(0, sizeof(double) * 4 * n);
+  S.gE = work_get(1, sizeof(double) * 4 * ny); S.gW = work_get(2, sizeof(double) * 4 * ny);
+  S.gN = work_get(3, sizeof(double) * 4 * nx); S.gS = work_get(4, sizeof(double) * 4 * nx);
+  S.oE = work_get(5, sizeof(double) * 4 * nqp * ny); S.oW = work_get(6, sizeof(double) * 4 * nqp * ny);
+  S.oN = work_get(7, sizeof(double) * 4 * nqp * nx); S.oS = work_get(8, sizeof(double) * 4 * nqp * nx);
+  S.iEW = work_get(9, sizeof(double) * 4 * nv);
+  S.iNS = work_get(10, sizeof(double) * 4 * nh);
+  S.gx = work_get(11, sizeof(double) * 4 * n); S.gy = work_get(12, sizeof(double) * 4 * n);
+  S.hot = work_get(13, sizeof(double) * 16 * nqp * n);
+  S.phi = work_get(14, sizeof(double) * 4 * n);
+  S.face = work_get(15, sizeof(double) * 16 * nqp * n);
+  S.vf = work_get(16, sizeof(double) * 4 * nqp * nv);
+  S.hf = work_get(17, sizeof(double) * 4 * nqp * nh);
 
   /* 1. reconstruction-type state (QuadBlock -> ReconstructionBlock.from_block) */
 #pragma omp parallel for schedule(static)
@@ -702,10 +719,6 @@ static void block_residual(const Ctx* C, int b, const double* U, double t, doubl
       }
   }
 #undef Wv
-  free(S.W); free(S.gE); free(S.gW); free(S.gN); free(S.gS);
-  free(S.oE); free(S.oW); free(S.oN); free(S.oS);
-  free(S.iEW); free(S.iNS); free(S.gx); free(S.gy); free(S.hot); free(S.phi);
-  free(S.face); free(S.vf); free(S.hf);
 }
 
 /* ------------------------------------------------------------------ public API ---- */
@@ -785,9 +798,9 @@ OR_API int oracle_step(const E2DConfig* cfg, const E2DBlock* blk, const E2DGeome
   Ctx C;
   ctx_init(&C, cfg, blk, geo);
   const int64_t N = 4 * C.ncell;
-  double* U0 = malloc(sizeof(double) * N);
-  double* cur = malloc(sizeof(double) * N);
-  double* k = malloc(sizeof(double) * N * nstages);
+  double* U0 = work_get(20, sizeof(double) * N);
+  double* cur = work_get(21, sizeof(double) * N);
+  double* k = work_get(22, sizeof(double) * N * nstages);
   memcpy(U0, U, sizeof(double) * N);
   memcpy(cur, U, sizeof(double) * N);
   for (int s = 0; s < nstages; ++s) {
@@ -804,7 +817,6 @@ OR_API int oracle_step(const E2DConfig* cfg, const E2DBlock* blk, const E2DGeome
     }
   }
   memcpy(U, cur, sizeof(double) * N);
-  free(U0); free(cur); free(k);
   return 0;
 }
 

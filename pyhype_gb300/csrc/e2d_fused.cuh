@@ -81,11 +81,19 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
   const bool cart = B->is_cartesian != 0;
   const int64_t fW = vf_at(B, i, j), fE = fW + 1;
   const int64_t fS = hf_at(B, i, j), fN = fS + B->nx;
+  // the frames of the faces to write, read before the first store
+  T fc[4] = {T(1), T(1), T(0), T(0)}, fs[4] = {T(0), T(0), T(1), T(1)};
+  if (!cart) {
+    if (which & FACE_E) { fc[0] = P.geo.vface[E2D_F_COS][fE]; fs[0] = P.geo.vface[E2D_F_SIN][fE]; }
+    if (which & FACE_W) { fc[1] = P.geo.vface[E2D_F_COS][fW]; fs[1] = P.geo.vface[E2D_F_SIN][fW]; }
+    if (which & FACE_N) { fc[2] = P.geo.hface[E2D_F_COS][fN]; fs[2] = P.geo.hface[E2D_F_SIN][fN]; }
+    if (which & FACE_S) { fc[3] = P.geo.hface[E2D_F_COS][fS]; fs[3] = P.geo.hface[E2D_F_SIN][fS]; }
+  }
   T w[4];
-  if (which & FACE_E) { vface_prim<T, RECON>(P, G, cart, fE, face[E2D_E], w); put4(sm.vL, lr, lc + 1, w); }
-  if (which & FACE_W) { vface_prim<T, RECON>(P, G, cart, fW, face[E2D_W], w); put4(sm.vR, lr, lc, w); }
-  if (which & FACE_N) { hface_prim<T, RECON>(P, G, cart, fN, face[E2D_N], w); put4(sm.hL, lr + 1, lc, w); }
-  if (which & FACE_S) { hface_prim<T, RECON>(P, G, cart, fS, face[E2D_S], w); put4(sm.hR, lr, lc, w); }
+  if (which & FACE_E) { vface_prim_cs<T, RECON>(G, cart, fc[0], fs[0], face[E2D_E], w); put4(sm.vL, lr, lc + 1, w); }
+  if (which & FACE_W) { vface_prim_cs<T, RECON>(G, cart, fc[1], fs[1], face[E2D_W], w); put4(sm.vR, lr, lc, w); }
+  if (which & FACE_N) { hface_prim_cs<T, RECON>(G, cart, fc[2], fs[2], face[E2D_N], w); put4(sm.hL, lr + 1, lc, w); }
+  if (which & FACE_S) { hface_prim_cs<T, RECON>(G, cart, fc[3], fs[3], face[E2D_S], w); put4(sm.hR, lr, lc, w); }
   if (!own) return;
   // outside states of block-boundary faces (the ghost cell is staged next to the cell)
   if (j == 0) {

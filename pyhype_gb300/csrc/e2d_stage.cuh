@@ -249,20 +249,30 @@ __device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, con
 // A face state (reconstruction variables) rotated into the frame of vertical face f
 // and converted to primitive variables (fvm/base.py:327-390).
 template <typename T, int RECON>
+__device__ __forceinline__ void vface_prim_cs(const Gas<T>& G, bool cart, T c, T s, const T* in, T* w) {
+  T q[4] = {in[0], in[1], in[2], in[3]};
+  if (!cart) rotate(q, c, s);
+  recon_to_prim<RECON>(q, G, w);
+}
+template <typename T, int RECON>
 __device__ __forceinline__ void vface_prim(const ParamsT<T>& P, const Gas<T>& G, bool cart, int64_t f, const T* in,
                                            T* w) {
-  T q[4] = {in[0], in[1], in[2], in[3]};
-  if (!cart) rotate(q, P.geo.vface[E2D_F_COS][f], P.geo.vface[E2D_F_SIN][f]);
-  recon_to_prim<RECON>(q, G, w);
+  vface_prim_cs<T, RECON>(G, cart, cart ? T(1) : P.geo.vface[E2D_F_COS][f], cart ? T(0) : P.geo.vface[E2D_F_SIN][f],
+                          in, w);
 }
 // the same for horizontal face f (the y sweep in the x frame, fvm/base.py:392-486)
 template <typename T, int RECON>
-__device__ __forceinline__ void hface_prim(const ParamsT<T>& P, const Gas<T>& G, bool cart, int64_t f, const T* in,
-                                           T* w) {
+__device__ __forceinline__ void hface_prim_cs(const Gas<T>& G, bool cart, T c, T s, const T* in, T* w) {
   T q[4] = {in[0], in[1], in[2], in[3]};
   if (cart) rotate90(q);
-  else rotate(q, P.geo.hface[E2D_F_COS][f], P.geo.hface[E2D_F_SIN][f]);
+  else rotate(q, c, s);
   recon_to_prim<RECON>(q, G, w);
+}
+template <typename T, int RECON>
+__device__ __forceinline__ void hface_prim(const ParamsT<T>& P, const Gas<T>& G, bool cart, int64_t f, const T* in,
+                                           T* w) {
+  hface_prim_cs<T, RECON>(G, cart, cart ? T(0) : P.geo.hface[E2D_F_COS][f], cart ? T(1) : P.geo.hface[E2D_F_SIN][f],
+                          in, w);
 }
 
 // Riemann flux of vertical face f in its frame, rotated back and integrated with the
@@ -301,32 +311,67 @@ __device__ __forceinline__ T cell_dudt(T IW, T IE, T IS, T IN, T A) {
 // The RK stage program at cell c: every partial Butcher sum this stage contributes
 // to, dst = src + (dt a) k, or on the FP32 path the last row's increment added to U^n
 // with Kahan compensation carried across steps.
+//
+// The buffers arrive as plain pointers, so the compiler may not move a load above an
+// earlier store; the sources of the first PRE updates (and U^n and its compensation for
+// a Kahan update) are therefore all loaded before the first store, instead of one
+// update's loads waiting behind the previous update's stores.  No load of a stage
+// reads what another update of the same stage writes (each updates its own Butcher
+// row's buffer, and the one update that writes U^n is alone in its stage), so the
+// values are those of the update-by-update order.
 template <typename T>
 __device__ __forceinline__ void stage_program(const ParamsT<T>& P, const StateBuffersT<T>& S, const StageProgram& prog,
                                               double dt, int64_t c, const T* k) {
+  constexpr int PRE = 4;  // covers every stage of the explicit tableaux up to RK4
+  T src_v[PRE][4], comp_v[4], u0_v[4];
+#pragma unroll
+  for (int u = 0; u < PRE; ++u) {
+    if (u >= prog.nupd) break;
+    const StageUpdate& up = prog.upd[u];
+    const T* src = S.at(up.src);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) src_v[u][v] = up.src_zero ? T(0) : src[v * P.ncell + c];
+    if (up.kahan) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        comp_v[v] = S.comp[v * P.ncell + c];
+        u0_v[v] = S.buf[0][v * P.ncell + c];
+      }
+    }
+  }
 #pragma unroll
   for (int u = 0; u < MAX_STAGES; ++u) {  // unrolled: the program is read from kernel parameters
     if (u >= prog.nupd) break;
     const StageUpdate& up = prog.upd[u];
     const T* src = S.at(up.src);
     const T dta = T(dt * up.a);
+    T base[4], cmp[4], u0[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      if (u < PRE) {
+        base[v] = src_v[u][v];
+      } else {
+        base[v] = up.src_zero ? T(0) : src[v * P.ncell + c];
+      }
+    }
     if (!up.kahan) {
       T* dst = S.at(up.dst);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const T base = up.src_zero ? T(0) : src[v * P.ncell + c];
-        dst[v * P.ncell + c] = fmaT(dta, k[v], base);
-      }
+      for (int v = 0; v < 4; ++v) dst[v * P.ncell + c] = fmaT(dta, k[v], base[v]);
     } else {
       // U^{n+1} = U^n + increment with Kahan compensation carried across steps
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        cmp[v] = u < PRE ? comp_v[v] : S.comp[v * P.ncell + c];
+        u0[v] = u < PRE ? u0_v[v] : S.buf[0][v * P.ncell + c];
+      }
       T* U0 = S.buf[0];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        const T inc = fmaT(dta, k[v], up.src_zero ? T(0) : src[v * P.ncell + c]);
-        const T y = inc - S.comp[v * P.ncell + c];
-        const T u0 = U0[v * P.ncell + c];
-        const T tt = u0 + y;
-        S.comp[v * P.ncell + c] = (tt - u0) - y;
+        const T inc = fmaT(dta, k[v], base[v]);
+        const T y = inc - cmp[v];
+        const T tt = u0[v] + y;
+        S.comp[v * P.ncell + c] = (tt - u0[v]) - y;
         U0[v * P.ncell + c] = tt;
       }
     }
@@ -443,14 +488,23 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
   }
 
   const bool cart = B->is_cartesian != 0;
+  // the four face frames, read before the first store of a face state (a load after a
+  // store through these plain pointers would wait for it)
+  T fc[4] = {T(1), T(1), T(0), T(0)}, fs[4] = {T(0), T(0), T(1), T(1)};
+  if (!cart) {
+    fc[0] = P.geo.vface[E2D_F_COS][fE]; fs[0] = P.geo.vface[E2D_F_SIN][fE];
+    fc[1] = P.geo.vface[E2D_F_COS][fW]; fs[1] = P.geo.vface[E2D_F_SIN][fW];
+    fc[2] = P.geo.hface[E2D_F_COS][fN]; fs[2] = P.geo.hface[E2D_F_SIN][fN];
+    fc[3] = P.geo.hface[E2D_F_COS][fS]; fs[3] = P.geo.hface[E2D_F_SIN][fS];
+  }
   T w[4];
-  vface_prim<T, RECON>(P, G, cart, fE, face[E2D_E], w);  // east face = left state of vertical face j+1
+  vface_prim_cs<T, RECON>(G, cart, fc[0], fs[0], face[E2D_E], w);  // east face = left state of vertical face j+1
   store4(F.vL, P.nvface, fE, w);
-  vface_prim<T, RECON>(P, G, cart, fW, face[E2D_W], w);  // west face = right state of vertical face j
+  vface_prim_cs<T, RECON>(G, cart, fc[1], fs[1], face[E2D_W], w);  // west face = right state of vertical face j
   store4(F.vR, P.nvface, fW, w);
-  hface_prim<T, RECON>(P, G, cart, fN, face[E2D_N], w);  // north face = left state of horizontal face i+1
+  hface_prim_cs<T, RECON>(G, cart, fc[2], fs[2], face[E2D_N], w);  // north face = left state of horizontal face i+1
   store4(F.hL, P.nhface, fN, w);
-  hface_prim<T, RECON>(P, G, cart, fS, face[E2D_S], w);  // south face = right state of horizontal face i
+  hface_prim_cs<T, RECON>(G, cart, fc[3], fs[3], face[E2D_S], w);  // south face = right state of horizontal face i
   store4(F.hR, P.nhface, fS, w);
   // outside states of block-boundary faces
   if (!edge) return;
@@ -742,21 +796,37 @@ __device__ __forceinline__ void flux_tile(const ParamsT<T>& P, const int4 tl, co
   if (i > ny || j > nx) return;
   const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
   const bool cart = B->is_cartesian != 0;
-  if (i < ny) {
-    const int64_t f = vf_at(B, i, j);
-    T L[4] = {F.vL[f], F.vL[P.nvface + f], F.vL[2 * P.nvface + f], F.vL[3 * P.nvface + f]};
-    T R[4] = {F.vR[f], F.vR[P.nvface + f], F.vR[2 * P.nvface + f], F.vR[3 * P.nvface + f]};
+  const bool hv = i < ny, hh = j < nx;
+  const int64_t fv = hv ? vf_at(B, i, j) : 0, fh = hh ? hf_at(B, i, j) : 0;
+  T vLs[4], vRs[4], hLs[4], hRs[4];
+  if constexpr (sizeof(T) == 4) {
+    // FP32 (issue- and latency-bound): both faces' states are loaded before the first
+    // store (the face arrays are plain pointers: a load after a store would wait for
+    // it).  FP64 is bound by its FP64 pipe, and the extra live values would spill.
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      if (hv) { vLs[v] = F.vL[v * P.nvface + fv]; vRs[v] = F.vR[v * P.nvface + fv]; }
+      if (hh) { hLs[v] = F.hL[v * P.nhface + fh]; hRs[v] = F.hR[v * P.nhface + fh]; }
+    }
+    T Iv[4], Ih[4];
+    if (hv) vface_flux<T, FLUX, DBG>(P, G, cart, fv, vLs, vRs, Iv, dbg);
+    if (hh) hface_flux<T, FLUX, DBG>(P, G, cart, fh, hLs, hRs, Ih, dbg);
+    if (hv) store4(F.vI, P.nvface, fv, Iv);
+    if (hh) store4(F.hI, P.nhface, fh, Ih);
+  } else {
     T I[4];
-    vface_flux<T, FLUX, DBG>(P, G, cart, f, L, R, I, dbg);
-    store4(F.vI, P.nvface, f, I);
-  }
-  if (j < nx) {
-    const int64_t f = hf_at(B, i, j);
-    T L[4] = {F.hL[f], F.hL[P.nhface + f], F.hL[2 * P.nhface + f], F.hL[3 * P.nhface + f]};
-    T R[4] = {F.hR[f], F.hR[P.nhface + f], F.hR[2 * P.nhface + f], F.hR[3 * P.nhface + f]};
-    T I[4];
-    hface_flux<T, FLUX, DBG>(P, G, cart, f, L, R, I, dbg);
-    store4(F.hI, P.nhface, f, I);
+    if (hv) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) { vLs[v] = F.vL[v * P.nvface + fv]; vRs[v] = F.vR[v * P.nvface + fv]; }
+      vface_flux<T, FLUX, DBG>(P, G, cart, fv, vLs, vRs, I, dbg);
+      store4(F.vI, P.nvface, fv, I);
+    }
+    if (hh) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) { hLs[v] = F.hL[v * P.nhface + fh]; hRs[v] = F.hR[v * P.nhface + fh]; }
+      hface_flux<T, FLUX, DBG>(P, G, cart, fh, hLs, hRs, I, dbg);
+      store4(F.hI, P.nhface, fh, I);
+    }
   }
 }
 
