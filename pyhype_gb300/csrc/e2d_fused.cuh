@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
 #pragma unroll
       for (int v = 0; v < 4; ++v) k[v] = cell_dudt(sm.vL[v][r][lane], sm.vL[v][r][lane + 1], sm.hL[v][r][lane],
                                                    sm.hL[v][r + 1][lane], A);
-      stage_program(P, S, prog, I->dt, c, k);
+      stage_program<T, 4>(P, S, prog, I->dt, c, k);
       if (prog.final_stage) {
         const T rho = S.buf[0][c], E = S.buf[0][3 * P.ncell + c];
         bad = !(rho > T(0)) || !(E > T(0));

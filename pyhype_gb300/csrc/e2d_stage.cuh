@@ -313,17 +313,19 @@ __device__ __forceinline__ T cell_dudt(T IW, T IE, T IS, T IN, T A) {
 // with Kahan compensation carried across steps.
 //
 // The buffers arrive as plain pointers, so the compiler may not move a load above an
-// earlier store; the sources of the first PRE updates (and U^n and its compensation for
-// a Kahan update) are therefore all loaded before the first store, instead of one
-// update's loads waiting behind the previous update's stores.  No load of a stage
+// earlier store.  With PRE > 0 the sources of the first PRE updates (and U^n and its
+// compensation for a Kahan update) are all loaded before the first store, instead of
+// one update's loads waiting behind the previous update's stores.  No load of a stage
 // reads what another update of the same stage writes (each updates its own Butcher
 // row's buffer, and the one update that writes U^n is alone in its stage), so the
-// values are those of the update-by-update order.
-template <typename T>
+// values are those of the update-by-update order.  The fused stage kernel, with few
+// warps per SM, takes PRE = 4 (every stage of the explicit tableaux up to RK4); the
+// split update kernel, whose latency is hidden by many resident warps, takes PRE = 0,
+// since the preloaded values would cost it registers and so occupancy.
+template <typename T, int PRE>
 __device__ __forceinline__ void stage_program(const ParamsT<T>& P, const StateBuffersT<T>& S, const StageProgram& prog,
                                               double dt, int64_t c, const T* k) {
-  constexpr int PRE = 4;  // covers every stage of the explicit tableaux up to RK4
-  T src_v[PRE][4], comp_v[4], u0_v[4];
+  T src_v[PRE > 0 ? PRE : 1][4], comp_v[4], u0_v[4];
 #pragma unroll
   for (int u = 0; u < PRE; ++u) {
     if (u >= prog.nupd) break;
@@ -871,7 +873,7 @@ __device__ __forceinline__ void update_tile(const ParamsT<T>& P, const int4 tl, 
 #pragma unroll
       for (int v = 0; v < 4; ++v) dudt_out[v * P.ncell + c] = k[v];
     }
-    stage_program(P, S, prog, I->dt, c, k);
+    stage_program<T, 0>(P, S, prog, I->dt, c, k);
     if (prog.final_stage) {
       const T rho = S.buf[0][c], E = S.buf[0][3 * P.ncell + c];
       bad = !(rho > T(0)) || !(E > T(0));
