@@ -238,8 +238,10 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     for (int item = threadIdx.x; item < NV + NH; item += FTHREADS) {
       const bool vert = item < NV;
       const int h = vert ? item : item - NV;
-      const int w = vert ? TX + 1 : TX;
-      const int r = h / w, c = h - r * w;
+      // row and column by two divisions by constants (one by a value chosen per item
+      // would be a full integer division)
+      const int r = vert ? h / (TX + 1) : h / TX;
+      const int c = h - r * (vert ? TX + 1 : TX);
       const bool live = vert ? (i0 + r < ny && j0 + c <= nx) : (i0 + r <= ny && j0 + c < nx);
       if (!live) continue;
       const int64_t f = vert ? vf_at(B, i0 + r, j0 + c) : hf_at(B, i0 + r, j0 + c);
@@ -310,7 +312,7 @@ static cudaError_t fused_launch(const ParamsT<T>& P, const TileSet& ts, const T*
   if (prepare_only) return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   const TmaTiles tma = tset ? tset->fused[FORM] : TmaTiles{nullptr, nullptr, nullptr};
   if (ts.nfused[FORM] <= 0) return cudaSuccess;
-  kern<<<ts.nfused[FORM], NW * 32, bytes, st>>>(P, ts.fused[FORM], U, inst, S, prog, real, tma);
+  kern<<<ts.nfused[FORM], NW * 32, bytes, st>>>(P, ts.fused[FORM], U, inst, S, resolve_program(prog, S), real, tma);
   return cudaGetLastError();
 }
 

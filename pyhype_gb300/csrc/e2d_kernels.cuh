@@ -83,6 +83,10 @@ struct StageUpdate {
   double a;
   int src_zero;
   int kahan;
+  // the buffers dst and src name, filled by resolve_program just before a launch (a
+  // pointer per update instead of a run-time choice among the state buffers per cell)
+  void* dstp;
+  const void* srcp;
 };
 struct StageProgram {
   int nupd;
@@ -94,15 +98,19 @@ template <typename T>
 struct StateBuffersT {
   T* buf[MAX_STAGES + 1];   // 0 = U^n, 1.. = row partial sums
   T* comp;                  // Kahan compensation of U^n (FP32 path), else null
-  // buf[k] for a run-time k by compare-and-select (a dynamic index into a kernel
-  // parameter array would copy the array to local memory)
-  __device__ __forceinline__ T* at(int k) const {
-    T* p = buf[0];
-#pragma unroll
-    for (int q = 1; q <= MAX_STAGES; ++q) p = (k == q) ? buf[q] : p;
-    return p;
-  }
 };
+
+// The program with each update's buffers resolved to pointers (ids 0..MAX_STAGES,
+// as build_program makes them).
+template <typename T>
+inline StageProgram resolve_program(const StageProgram& prog, const StateBuffersT<T>& S) {
+  StageProgram r = prog;
+  for (int u = 0; u < r.nupd; ++u) {
+    r.upd[u].dstp = S.buf[r.upd[u].dst];
+    r.upd[u].srcp = S.buf[r.upd[u].src];
+  }
+  return r;
+}
 
 template <typename T>
 struct DebugOutT {

@@ -330,7 +330,7 @@ __device__ __forceinline__ void stage_program(const ParamsT<T>& P, const StateBu
   for (int u = 0; u < PRE; ++u) {
     if (u >= prog.nupd) break;
     const StageUpdate& up = prog.upd[u];
-    const T* src = S.at(up.src);
+    const T* src = static_cast<const T*>(up.srcp);
 #pragma unroll
     for (int v = 0; v < 4; ++v) src_v[u][v] = up.src_zero ? T(0) : src[v * P.ncell + c];
     if (up.kahan) {
@@ -345,7 +345,7 @@ __device__ __forceinline__ void stage_program(const ParamsT<T>& P, const StateBu
   for (int u = 0; u < MAX_STAGES; ++u) {  // unrolled: the program is read from kernel parameters
     if (u >= prog.nupd) break;
     const StageUpdate& up = prog.upd[u];
-    const T* src = S.at(up.src);
+    const T* src = static_cast<const T*>(up.srcp);
     const T dta = T(dt * up.a);
     T base[4], cmp[4], u0[4];
 #pragma unroll
@@ -357,7 +357,7 @@ __device__ __forceinline__ void stage_program(const ParamsT<T>& P, const StateBu
       }
     }
     if (!up.kahan) {
-      T* dst = S.at(up.dst);
+      T* dst = static_cast<T*>(up.dstp);
 #pragma unroll
       for (int v = 0; v < 4; ++v) dst[v * P.ncell + c] = fmaT(dta, k[v], base[v]);
     } else {
@@ -1127,9 +1127,11 @@ cudaError_t launch_update(const ParamsT<T>& P, const TileSet& ts, KernelChoice k
   if (n <= 0) return cudaSuccess;
   if (kc.persistent) {
     auto kern = k_update<T, true>;
-    kern<<<persistent_grid(kern, TX * TY, n), TX * TY, 0, st>>>(P, ts.cell[1], n, F, S, prog, inst, real, dudt_out);
+    kern<<<persistent_grid(kern, TX * TY, n), TX * TY, 0, st>>>(P, ts.cell[1], n, F, S, resolve_program(prog, S),
+                                                                 inst, real, dudt_out);
   } else {
-    k_update<T, false><<<n, TX * TY, 0, st>>>(P, ts.cell[1], n, F, S, prog, inst, real, dudt_out);
+    k_update<T, false><<<n, TX * TY, 0, st>>>(P, ts.cell[1], n, F, S, resolve_program(prog, S), inst, real,
+                                              dudt_out);
   }
   return cudaGetLastError();
 }
