@@ -58,17 +58,32 @@ __device__ __forceinline__ void put4(T (&a)[4][R][C], int r, int c, const T* w) 
 
 enum { FACE_E = 1, FACE_W = 2, FACE_N = 4, FACE_S = 8 };
 
+// The tile's first cell (i0, j0) and its west and south faces in the planes, and the
+// block's shape: read from the block descriptor once per CTA, where each index
+// computation would otherwise load them from global memory again.
+struct TileOrigin {
+  int64_t c0, vf0, hf0;
+  int nx, ny;
+  bool cart;
+  __device__ __forceinline__ int64_t cell(int lr, int lc) const { return c0 + (int64_t)lr * nx + lc; }
+  __device__ __forceinline__ int64_t vface(int lr, int lc) const { return vf0 + (int64_t)lr * (nx + 1) + lc; }
+  __device__ __forceinline__ int64_t hface(int lr, int lc) const { return hf0 + (int64_t)lr * nx + lc; }
+};
+
 // Gradient, limiter and the face states `which` of the cell at tile-local (lr, lc),
 // lr in [-1, FTY], lc in [-1, TX]; a tile cell (own = true) also writes the outside
 // states of its block-boundary faces.
 template <typename T, int LIM, int RECON, int FTY>
-__device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G, const E2DBlock* B, FusedSmem<T, FTY>& sm,
-                                           int i0, int j0, int lr, int lc, int which, bool own, double t) {
+__device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G, const E2DBlock* B,
+                                           const TileOrigin& to, FusedSmem<T, FTY>& sm, int i0, int j0, int lr,
+                                           int lc, int which, bool own, double t) {
   constexpr int XO = TileCols<T>::XO;
   const int i = i0 + lr, j = j0 + lc;
   const int sr = lr + 2, sc = XO + lc;  // the cell's position in sW
+  const int64_t fW = to.vface(lr, lc), fE = fW + 1;
+  const int64_t fS = to.hface(lr, lc), fN = fS + to.nx;
   CellGeo<T> g;
-  load_cell_geo(P, B, i, j, g);
+  load_cell_geo_at(P, to.cell(lr, lc), fW, fS, to.nx, g);
   T face[4][4];
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
@@ -78,9 +93,7 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
 #pragma unroll
     for (int s = 0; s < 4; ++s) face[s][v] = fv[s];
   }
-  const bool cart = B->is_cartesian != 0;
-  const int64_t fW = vf_at(B, i, j), fE = fW + 1;
-  const int64_t fS = hf_at(B, i, j), fN = fS + B->nx;
+  const bool cart = to.cart;
   // the frames of the faces to write, read before the first store
   T fc[4] = {T(1), T(1), T(0), T(0)}, fs[4] = {T(0), T(0), T(1), T(1)};
   if (!cart) {
@@ -103,7 +116,7 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
     vface_prim<T, RECON>(P, G, cart, fW, o, w);
     put4(sm.vL, lr, lc, w);
   }
-  if (j == B->nx - 1) {
+  if (j == to.nx - 1) {
     const T gr[4] = {sm.sW[0][sr][sc + 1], sm.sW[1][sr][sc + 1], sm.sW[2][sr][sc + 1], sm.sW[3][sr][sc + 1]};
     T o[4];
     outside_state(P, B, E2D_E, i, t, gr, face[E2D_E], o);
@@ -117,7 +130,7 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
     hface_prim<T, RECON>(P, G, cart, fS, o, w);
     put4(sm.hL, lr, lc, w);
   }
-  if (i == B->ny - 1) {
+  if (i == to.ny - 1) {
     const T gr[4] = {sm.sW[0][sr + 1][sc], sm.sW[1][sr + 1][sc], sm.sW[2][sr + 1][sc], sm.sW[3][sr + 1][sc]};
     T o[4];
     outside_state(P, B, E2D_N, j, t, gr, face[E2D_N], o);
@@ -146,6 +159,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
   const double t = I->t;
   const int nx = B->nx, ny = B->ny;
   const int i0 = tl.y, j0 = tl.z;
+  const TileOrigin to{cell_at(B, i0, j0), vf_at(B, i0, j0), hf_at(B, i0, j0), nx, ny, B->is_cartesian != 0};
   // the halo lies inside the block: no ghost cell is staged and every ring cell is real
   const bool interior = i0 >= 2 && j0 >= 2 && i0 + FTY + 2 <= ny && j0 + TX + 2 <= nx;
 
@@ -227,13 +241,13 @@ __global__ void __launch_bounds__(NW * 32, MINB)
       which = east ? FACE_W : FACE_E;
       live = q < 2 * FTY && i0 + lr < ny && (east ? j0 + TX < nx : j0 >= 1);
     }
-    if (live) fused_cell<T, LIM, RECON, FTY>(P, G, B, sm, i0, j0, lr, lc, which, task < FTY, t);
+    if (live) fused_cell<T, LIM, RECON, FTY>(P, G, B, to, sm, i0, j0, lr, lc, which, task < FTY, t);
   }
   __syncthreads();
 
   // ---- one flux per face of the tile (one call site for both face families) ---------
   {
-    const bool cart = B->is_cartesian != 0;
+    const bool cart = to.cart;
     constexpr int NV = FTY * (TX + 1), NH = (FTY + 1) * TX;
     for (int item = threadIdx.x; item < NV + NH; item += FTHREADS) {
       const bool vert = item < NV;
@@ -244,7 +258,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
       const int c = h - r * (vert ? TX + 1 : TX);
       const bool live = vert ? (i0 + r < ny && j0 + c <= nx) : (i0 + r <= ny && j0 + c < nx);
       if (!live) continue;
-      const int64_t f = vert ? vf_at(B, i0 + r, j0 + c) : hf_at(B, i0 + r, j0 + c);
+      const int64_t f = vert ? to.vface(r, c) : to.hface(r, c);
       T L[4], R[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
@@ -278,13 +292,13 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     const int i = i0 + r, j = j0 + lane;
     bool bad = false;
     if (r < FTY && i < ny && j < nx) {
-      const int64_t c = cell_at(B, i, j);
+      const int64_t c = to.cell(r, lane);
       const T A = P.geo.cell[E2D_G_A][c];
       T k[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) k[v] = cell_dudt(sm.vL[v][r][lane], sm.vL[v][r][lane + 1], sm.hL[v][r][lane],
                                                    sm.hL[v][r + 1][lane], A);
-      stage_program<T, 4>(P, S, prog, I->dt, c, k);
+      stage_program(P, S, prog, I->dt, c, k);
       if (prog.final_stage) {
         const T rho = S.buf[0][c], E = S.buf[0][3 * P.ncell + c];
         bad = !(rho > T(0)) || !(E > T(0));

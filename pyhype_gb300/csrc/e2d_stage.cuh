@@ -162,11 +162,11 @@ struct CellGeo {
   T hx[4], hy[4];
 };
 
+// by the cell's index c, its west face fW and south face fS in a block nx cells wide
 template <typename T>
-__device__ __forceinline__ void load_cell_geo(const ParamsT<T>& P, const E2DBlock* B, int i, int j, CellGeo<T>& g) {
-  const int64_t c = cell_at(B, i, j);
-  const int64_t fW = vf_at(B, i, j), fE = fW + 1;
-  const int64_t fS = hf_at(B, i, j), fN = fS + B->nx;
+__device__ __forceinline__ void load_cell_geo_at(const ParamsT<T>& P, int64_t c, int64_t fW, int64_t fS, int nx,
+                                                 CellGeo<T>& g) {
+  const int64_t fE = fW + 1, fN = fS + nx;
   g.LcE = P.geo.vface[E2D_F_LC][fE]; g.LsE = P.geo.vface[E2D_F_LS][fE];
   g.LcW = P.geo.vface[E2D_F_LC][fW]; g.LsW = P.geo.vface[E2D_F_LS][fW];
   g.LcN = P.geo.hface[E2D_F_LC][fN]; g.LsN = P.geo.hface[E2D_F_LS][fN];
@@ -177,6 +177,10 @@ __device__ __forceinline__ void load_cell_geo(const ParamsT<T>& P, const E2DBloc
     g.hx[s] = P.geo.cell[E2D_G_HX_E + s][c];
     g.hy[s] = P.geo.cell[E2D_G_HY_E + s][c];
   }
+}
+template <typename T>
+__device__ __forceinline__ void load_cell_geo(const ParamsT<T>& P, const E2DBlock* B, int i, int j, CellGeo<T>& g) {
+  load_cell_geo_at(P, cell_at(B, i, j), vf_at(B, i, j), hf_at(B, i, j), B->nx, g);
 }
 
 // Green-Gauss gradient, limiter value and the limited face states fv (E, W, N, S) of
@@ -302,78 +306,46 @@ __device__ __forceinline__ void hface_flux(const ParamsT<T>& P, const Gas<T>& G,
 }
 
 // dUdt of one variable of a cell from its integrated face fluxes and area
-// (fvm/base.py:171-190): 0.5 * (((I_W - I_E) + I_S) - I_N) / A.
+// (fvm/base.py:171-190): 0.5 * (((I_W - I_E) + I_S) - I_N) / A.  The FP32 form divides
+// by the (positive, normal) area with rdiv.
 template <typename T>
 __device__ __forceinline__ T cell_dudt(T IW, T IE, T IS, T IN, T A) {
-  return qdiv(half(IW - IE + IS - IN), A);
+  if constexpr (sizeof(T) == 4) return rdiv(half(IW - IE + IS - IN), A);
+  else return qdiv(half(IW - IE + IS - IN), A);
 }
 
 // The RK stage program at cell c: every partial Butcher sum this stage contributes
 // to, dst = src + (dt a) k, or on the FP32 path the last row's increment added to U^n
-// with Kahan compensation carried across steps.
-//
-// The buffers arrive as plain pointers, so the compiler may not move a load above an
-// earlier store.  With PRE > 0 the sources of the first PRE updates (and U^n and its
-// compensation for a Kahan update) are all loaded before the first store, instead of
-// one update's loads waiting behind the previous update's stores.  No load of a stage
-// reads what another update of the same stage writes (each updates its own Butcher
-// row's buffer, and the one update that writes U^n is alone in its stage), so the
-// values are those of the update-by-update order.  The fused stage kernel, with few
-// warps per SM, takes PRE = 4 (every stage of the explicit tableaux up to RK4); the
-// split update kernel, whose latency is hidden by many resident warps, takes PRE = 0,
-// since the preloaded values would cost it registers and so occupancy.
-template <typename T, int PRE>
+// with Kahan compensation carried across steps.  Each update's loads wait behind the
+// previous update's stores (the buffers are plain pointers); loading every source
+// first was measured slower in both the split and the fused kernel: the values held
+// across the stores cost registers, and so occupancy or spills.
+template <typename T>
 __device__ __forceinline__ void stage_program(const ParamsT<T>& P, const StateBuffersT<T>& S, const StageProgram& prog,
                                               double dt, int64_t c, const T* k) {
-  T src_v[PRE > 0 ? PRE : 1][4], comp_v[4], u0_v[4];
-#pragma unroll
-  for (int u = 0; u < PRE; ++u) {
-    if (u >= prog.nupd) break;
-    const StageUpdate& up = prog.upd[u];
-    const T* src = static_cast<const T*>(up.srcp);
-#pragma unroll
-    for (int v = 0; v < 4; ++v) src_v[u][v] = up.src_zero ? T(0) : src[v * P.ncell + c];
-    if (up.kahan) {
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        comp_v[v] = S.comp[v * P.ncell + c];
-        u0_v[v] = S.buf[0][v * P.ncell + c];
-      }
-    }
-  }
 #pragma unroll
   for (int u = 0; u < MAX_STAGES; ++u) {  // unrolled: the program is read from kernel parameters
     if (u >= prog.nupd) break;
     const StageUpdate& up = prog.upd[u];
     const T* src = static_cast<const T*>(up.srcp);
     const T dta = T(dt * up.a);
-    T base[4], cmp[4], u0[4];
+    T base[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      if (u < PRE) {
-        base[v] = src_v[u][v];
-      } else {
-        base[v] = up.src_zero ? T(0) : src[v * P.ncell + c];
-      }
-    }
+    for (int v = 0; v < 4; ++v) base[v] = up.src_zero ? T(0) : src[v * P.ncell + c];
     if (!up.kahan) {
       T* dst = static_cast<T*>(up.dstp);
 #pragma unroll
       for (int v = 0; v < 4; ++v) dst[v * P.ncell + c] = fmaT(dta, k[v], base[v]);
     } else {
       // U^{n+1} = U^n + increment with Kahan compensation carried across steps
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        cmp[v] = u < PRE ? comp_v[v] : S.comp[v * P.ncell + c];
-        u0[v] = u < PRE ? u0_v[v] : S.buf[0][v * P.ncell + c];
-      }
       T* U0 = S.buf[0];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const T inc = fmaT(dta, k[v], base[v]);
-        const T y = inc - cmp[v];
-        const T tt = u0[v] + y;
-        S.comp[v * P.ncell + c] = (tt - u0[v]) - y;
+        const T cmp = S.comp[v * P.ncell + c], u0 = U0[v * P.ncell + c];
+        const T y = inc - cmp;
+        const T tt = u0 + y;
+        S.comp[v * P.ncell + c] = (tt - u0) - y;
         U0[v * P.ncell + c] = tt;
       }
     }
@@ -873,7 +845,7 @@ __device__ __forceinline__ void update_tile(const ParamsT<T>& P, const int4 tl, 
 #pragma unroll
       for (int v = 0; v < 4; ++v) dudt_out[v * P.ncell + c] = k[v];
     }
-    stage_program<T, 0>(P, S, prog, I->dt, c, k);
+    stage_program(P, S, prog, I->dt, c, k);
     if (prog.final_stage) {
       const T rho = S.buf[0][c], E = S.buf[0][3 * P.ncell + c];
       bad = !(rho > T(0)) || !(E > T(0));
