@@ -130,7 +130,7 @@ __device__ __forceinline__ void limiter_forward(T w0, T we, T ea, T so, T no, T 
     int imn_s = 0, imx_s = 0;
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-      sls[s] = slope32(dmax, dmin, dv[s]);
+      sls[s] = slope32(dmax, dmin, dv[s], FLOAT_TRUE_MIN);  // dv: thresholded already
       if (s > 0 && vlt(sls[s], sls[imn_s])) imn_s = s;
       if (s > 0 && vlt(sls[imx_s], sls[s])) imx_s = s;
     }

@@ -42,13 +42,13 @@ struct FusedSmem {
   // tile + 2-cell halo in reconstruction variables; block row i0 - 2 + r at row r,
   // block column j0 - XO + c at column c (XO = 16 / sizeof(T), the TMA box's start)
   T sW[4][FTY + 4][TileCols<T>::TXW];
-  // vertical face (row i0 + r, face column j0 + c): left / right primitive state in the
-  // face frame; after the flux phase vL holds the integrated flux
-  T vL[4][FTY][TX + 1];
-  T vR[4][FTY][TX + 1];
-  // horizontal face (face row i0 + r, column j0 + c)
-  T hL[4][FTY + 1][TX];
-  T hR[4][FTY + 1][TX];
+  // face states, family 0 the vertical faces (row i0 + r, face column j0 + c; r < FTY,
+  // c <= TX), family 1 the horizontal ones (face row i0 + r, column j0 + c; r <= FTY,
+  // c < TX): left and right primitive state in the face frame; after the flux phase L
+  // holds the integrated flux.  Both families take the same padded plane shape, so a
+  // face's variables sit at fixed offsets from one address whatever its family.
+  T L[2][4][FTY + 1][TX + 1];
+  T R[2][4][FTY + 1][TX + 1];
 };
 
 template <typename T, int R, int C>
@@ -103,10 +103,10 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
     if (which & FACE_S) { fc[3] = P.geo.hface[E2D_F_COS][fS]; fs[3] = P.geo.hface[E2D_F_SIN][fS]; }
   }
   T w[4];
-  if (which & FACE_E) { vface_prim_cs<T, RECON>(G, cart, fc[0], fs[0], face[E2D_E], w); put4(sm.vL, lr, lc + 1, w); }
-  if (which & FACE_W) { vface_prim_cs<T, RECON>(G, cart, fc[1], fs[1], face[E2D_W], w); put4(sm.vR, lr, lc, w); }
-  if (which & FACE_N) { hface_prim_cs<T, RECON>(G, cart, fc[2], fs[2], face[E2D_N], w); put4(sm.hL, lr + 1, lc, w); }
-  if (which & FACE_S) { hface_prim_cs<T, RECON>(G, cart, fc[3], fs[3], face[E2D_S], w); put4(sm.hR, lr, lc, w); }
+  if (which & FACE_E) { vface_prim_cs<T, RECON>(G, cart, fc[0], fs[0], face[E2D_E], w); put4(sm.L[0], lr, lc + 1, w); }
+  if (which & FACE_W) { vface_prim_cs<T, RECON>(G, cart, fc[1], fs[1], face[E2D_W], w); put4(sm.R[0], lr, lc, w); }
+  if (which & FACE_N) { hface_prim_cs<T, RECON>(G, cart, fc[2], fs[2], face[E2D_N], w); put4(sm.L[1], lr + 1, lc, w); }
+  if (which & FACE_S) { hface_prim_cs<T, RECON>(G, cart, fc[3], fs[3], face[E2D_S], w); put4(sm.R[1], lr, lc, w); }
   if (!own) return;
   // outside states of block-boundary faces (the ghost cell is staged next to the cell)
   if (j == 0) {
@@ -114,28 +114,28 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
     T o[4];
     outside_state(P, B, E2D_W, i, t, gr, face[E2D_W], o);
     vface_prim<T, RECON>(P, G, cart, fW, o, w);
-    put4(sm.vL, lr, lc, w);
+    put4(sm.L[0], lr, lc, w);
   }
   if (j == to.nx - 1) {
     const T gr[4] = {sm.sW[0][sr][sc + 1], sm.sW[1][sr][sc + 1], sm.sW[2][sr][sc + 1], sm.sW[3][sr][sc + 1]};
     T o[4];
     outside_state(P, B, E2D_E, i, t, gr, face[E2D_E], o);
     vface_prim<T, RECON>(P, G, cart, fE, o, w);
-    put4(sm.vR, lr, lc + 1, w);
+    put4(sm.R[0], lr, lc + 1, w);
   }
   if (i == 0) {
     const T gr[4] = {sm.sW[0][sr - 1][sc], sm.sW[1][sr - 1][sc], sm.sW[2][sr - 1][sc], sm.sW[3][sr - 1][sc]};
     T o[4];
     outside_state(P, B, E2D_S, j, t, gr, face[E2D_S], o);
     hface_prim<T, RECON>(P, G, cart, fS, o, w);
-    put4(sm.hL, lr, lc, w);
+    put4(sm.L[1], lr, lc, w);
   }
   if (i == to.ny - 1) {
     const T gr[4] = {sm.sW[0][sr + 1][sc], sm.sW[1][sr + 1][sc], sm.sW[2][sr + 1][sc], sm.sW[3][sr + 1][sc]};
     T o[4];
     outside_state(P, B, E2D_N, j, t, gr, face[E2D_N], o);
     hface_prim<T, RECON>(P, G, cart, fN, o, w);
-    put4(sm.hR, lr + 1, lc, w);
+    put4(sm.R[1], lr + 1, lc, w);
   }
 }
 
@@ -248,22 +248,20 @@ __global__ void __launch_bounds__(NW * 32, MINB)
   // ---- one flux per face of the tile (one call site for both face families) ---------
   {
     const bool cart = to.cart;
-    constexpr int NV = FTY * (TX + 1), NH = (FTY + 1) * TX;
-    for (int item = threadIdx.x; item < NV + NH; item += FTHREADS) {
-      const bool vert = item < NV;
-      const int h = vert ? item : item - NV;
-      // row and column by two divisions by constants (one by a value chosen per item
-      // would be a full integer division)
-      const int r = vert ? h / (TX + 1) : h / TX;
-      const int c = h - r * (vert ? TX + 1 : TX);
-      const bool live = vert ? (i0 + r < ny && j0 + c <= nx) : (i0 + r <= ny && j0 + c < nx);
+    constexpr int FC = TX + 1, PLANE = (FTY + 1) * FC;  // a family's padded plane
+    for (int item = threadIdx.x; item < 2 * PLANE; item += FTHREADS) {
+      const int fam = item >= PLANE ? 1 : 0;
+      const bool vert = fam == 0;
+      const int h = item - fam * PLANE;
+      const int r = h / FC, c = h - r * FC;
+      const bool live = vert ? (r < FTY && i0 + r < ny && j0 + c <= nx) : (c < TX && i0 + r <= ny && j0 + c < nx);
       if (!live) continue;
       const int64_t f = vert ? to.vface(r, c) : to.hface(r, c);
       T L[4], R[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        L[v] = vert ? sm.vL[v][r][c] : sm.hL[v][r][c];
-        R[v] = vert ? sm.vR[v][r][c] : sm.hR[v][r][c];
+        L[v] = sm.L[fam][v][r][c];
+        R[v] = sm.R[fam][v][r][c];
       }
       T Fq[4];
       riemann<FLUX>(L, R, G, Fq);
@@ -275,11 +273,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
       else if (!cart) unrotate(Fq, cosp[f], sinp[f]);
       const T len = lenp[f];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const T Iv = len * twice(Fq[v]);
-        if (vert) sm.vL[v][r][c] = Iv;
-        else sm.hL[v][r][c] = Iv;
-      }
+      for (int v = 0; v < 4; ++v) sm.L[fam][v][r][c] = len * twice(Fq[v]);
     }
   }
   __syncthreads();
@@ -296,8 +290,8 @@ __global__ void __launch_bounds__(NW * 32, MINB)
       const T A = P.geo.cell[E2D_G_A][c];
       T k[4];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) k[v] = cell_dudt(sm.vL[v][r][lane], sm.vL[v][r][lane + 1], sm.hL[v][r][lane],
-                                                   sm.hL[v][r + 1][lane], A);
+      for (int v = 0; v < 4; ++v) k[v] = cell_dudt(sm.L[0][v][r][lane], sm.L[0][v][r][lane + 1], sm.L[1][v][r][lane],
+                                                   sm.L[1][v][r + 1][lane], A);
       stage_program(P, S, prog, I->dt, c, k);
       if (prog.final_stage) {
         const T rho = S.buf[0][c], E = S.buf[0][3 * P.ncell + c];

@@ -231,11 +231,11 @@ __device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, con
     // and switch branches where the FP64 path does not, so the FP32 form applies the
     // FP64 threshold, 2^-53 times the power of two of w0.
     const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
+    const T floor = fmaxf(half_ulp64, FLOAT_TRUE_MIN);
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
       hot[s] = fmaT(gx, g.hx[s], gy * g.hy[s]);
-      const T davg = (fabs(hot[s]) < half_ulp64) ? T(0) : hot[s];
-      const T sl = slope32(dmax, dmin, davg);
+      const T sl = slope32(dmax, dmin, hot[s], floor);
       smin = (s == 0) ? sl : vmin(smin, sl);
       smax = (s == 0) ? sl : vmax(smax, sl);
     }
