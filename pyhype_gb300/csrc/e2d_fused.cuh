@@ -21,7 +21,7 @@
 //   update    dUdt of every tile cell and the stage program (partial Butcher sums,
 //             Kahan-compensated last row on the FP32 path), positivity on the last stage.
 // Every value is computed by the same functions the split kernels use
-// (limit_cell_var, vface_prim/hface_prim, vface_flux/hface_flux, cell_dudt,
+// (limit_cell4, vface_prim/hface_prim, vface_flux/hface_flux, cell_dudt,
 // stage_program), so the two forms give the same results.
 //
 // The cost of fusion is the ring: gradient and limiter of the 2 (32 + FTY) ring cells
@@ -85,13 +85,13 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
   CellGeo<T> g;
   load_cell_geo_at(P, to.cell(lr, lc), fW, fS, to.nx, g);
   T face[4][4];
-#pragma unroll
-  for (int v = 0; v < 4; ++v) {
-    T fv[4], gx, gy, ph;
-    limit_cell_var<T, LIM>(sm.sW[v][sr][sc], sm.sW[v][sr][sc - 1], sm.sW[v][sr][sc + 1], sm.sW[v][sr - 1][sc],
-                           sm.sW[v][sr + 1][sc], g, fv, gx, gy, ph);
-#pragma unroll
-    for (int s = 0; s < 4; ++s) face[s][v] = fv[s];
+  {
+    // stencil points: the cell, W, E, S, N
+    auto st = [&](int v, int p) -> T {
+      return sm.sW[v][sr + (p == 3 ? -1 : p == 4 ? 1 : 0)][sc + (p == 1 ? -1 : p == 2 ? 1 : 0)];
+    };
+    T gx[4], gy[4], ph[4];
+    limit_cell4<T, LIM>(st, g, face, gx, gy, ph);
   }
   const bool cart = to.cart;
   // the frames of the faces to write, read before the first store

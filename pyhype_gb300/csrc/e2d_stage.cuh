@@ -183,6 +183,34 @@ __device__ __forceinline__ void load_cell_geo(const ParamsT<T>& P, const E2DBloc
   load_cell_geo_at(P, cell_at(B, i, j), vf_at(B, i, j), hf_at(B, i, j), B->nx, g);
 }
 
+// FP32 form: the limiter value of one variable at one cell from its five-point
+// stencil and its four unlimited face differences hot (E, W, N, S): every face's
+// slope from the reciprocal approximation (slope32), psi only at the smallest and, for
+// the limiters with a maximum, the largest of them (the functions are unimodal:
+// psi_has_peak), a negative value clipped to 0.
+template <int LIM>
+__device__ __forceinline__ float phi32(float w0, float we, float ea, float so, float no, const float (&hot)[4]) {
+  const float dmax = vmax(vmax(vmax(vmax(w0, we), ea), so), no) - w0;
+  const float dmin = vmin(vmin(vmin(vmin(w0, we), ea), so), no) - w0;
+  // FP64's round trip (w0 + hot) - w0 is hot itself unless |hot| is below half an FP64
+  // ulp of w0, where it is zero and the slope takes its davg == 0 branch (psi(1)).  In
+  // FP32 the same round trip would zero every |hot| below 2^-25 |w0| and switch
+  // branches where the FP64 path does not, so the FP32 form applies the FP64
+  // threshold, 2^-53 times the power of two of w0.
+  const float half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * 1.1102230246251565e-16f;
+  const float floor = fmaxf(half_ulp64, FLOAT_TRUE_MIN);
+  float smin = 0.f, smax = 0.f;
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const float sl = slope32(dmax, dmin, hot[s], floor);
+    smin = (s == 0) ? sl : vmin(smin, sl);
+    smax = (s == 0) ? sl : vmax(smax, sl);
+  }
+  float ph = psi_s<LIM>(smin);
+  if constexpr (psi_has_peak<LIM>()) ph = vmin(ph, psi_s<LIM>(smax));
+  return is_neg(ph) ? 0.f : ph;
+}
+
 // Green-Gauss gradient, limiter value and the limited face states fv (E, W, N, S) of
 // one variable at one cell from its five-point stencil (reconstruction variables).
 template <typename T, int LIM>
@@ -195,11 +223,11 @@ __device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, con
   const T gx = fmaT(is, -g.LcS, fmaT(in, g.LcN, fmaT(ie, g.LcE, iw * (-g.LcW)))) * g.ia;
   const T gy = fmaT(is, -g.LsS, fmaT(in, g.LsN, fmaT(ie, g.LsE, iw * (-g.LsW)))) * g.ia;
   // limiter (limiters/base.py:47-221)
-  const T dmax = vmax(vmax(vmax(vmax(w0, we), ea), so), no) - w0;
-  const T dmin = vmin(vmin(vmin(vmin(w0, we), ea), so), no) - w0;
   T hot[4];
   T ph = T(0);
   if constexpr (sizeof(T) == 8) {
+    const T dmax = vmax(vmax(vmax(vmax(w0, we), ea), so), no) - w0;
+    const T dmin = vmin(vmin(vmin(vmin(w0, we), ea), so), no) - w0;
     // FP64: psi only at the faces that decide the minimum (e2d_slope_pick.cuh); all
     // four when the pick cannot rule a face out.  Same expressions, same phi.
     double davg[4];
@@ -221,26 +249,9 @@ __device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, con
       }
     }
   } else {
-    // FP32: every face's slope from the reciprocal approximation (slope32), psi only at
-    // the smallest and, for the limiters with a maximum, the largest of them (the
-    // functions are unimodal: psi_has_peak)
-    T smin = T(0), smax = T(0);
-    // FP64's round trip (w0 + hot) - w0 is hot itself unless |hot| is below half an
-    // FP64 ulp of w0, where it is zero and the slope takes its davg == 0 branch
-    // (psi(1)).  In FP32 the same round trip would zero every |hot| below 2^-25 |w0|
-    // and switch branches where the FP64 path does not, so the FP32 form applies the
-    // FP64 threshold, 2^-53 times the power of two of w0.
-    const T half_ulp64 = __int_as_float(__float_as_int(w0) & 0x7f800000) * T(1.1102230246251565e-16);
-    const T floor = fmaxf(half_ulp64, FLOAT_TRUE_MIN);
 #pragma unroll
-    for (int s = 0; s < 4; ++s) {
-      hot[s] = fmaT(gx, g.hx[s], gy * g.hy[s]);
-      const T sl = slope32(dmax, dmin, hot[s], floor);
-      smin = (s == 0) ? sl : vmin(smin, sl);
-      smax = (s == 0) ? sl : vmax(smax, sl);
-    }
-    ph = psi_s<LIM>(smin);
-    if constexpr (psi_has_peak<LIM>()) ph = vmin(ph, psi_s<LIM>(smax));
+    for (int s = 0; s < 4; ++s) hot[s] = fmaT(gx, g.hx[s], gy * g.hy[s]);
+    ph = phi32<LIM>(w0, we, ea, so, no, hot);
   }
   ph = is_neg(ph) ? T(0) : ph;
 #pragma unroll
@@ -248,6 +259,61 @@ __device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, con
   gx_out = gx;
   gy_out = gy;
   ph_out = ph;
+}
+
+// The four variables of one cell: face[s][v] the limited state of side s (E, W, N, S),
+// gx/gy/ph the gradient and limiter value of variable v.  st(v, p) is variable v's
+// stencil value at point p (0 the cell, 1 its west, 2 east, 3 south, 4 north
+// neighbour).  FP32 evaluates the interface averages, gradients, face differences and
+// face states of two variables at a time in paired instructions (same values).
+template <typename T, int LIM, typename Stencil>
+__device__ __forceinline__ void limit_cell4(const Stencil& st, const CellGeo<T>& g, T (&face)[4][4], T (&gx)[4],
+                                            T (&gy)[4], T (&ph)[4]) {
+  if constexpr (sizeof(T) == 8) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      T fv[4];
+      limit_cell_var<T, LIM>(st(v, 0), st(v, 1), st(v, 2), st(v, 3), st(v, 4), g, fv, gx[v], gy[v], ph[v]);
+#pragma unroll
+      for (int s = 0; s < 4; ++s) face[s][v] = fv[s];
+    }
+  } else {
+    const float2 H = pair(0.5f, 0.5f);
+    const float2 LcE = pair(g.LcE, g.LcE), nLcW = pair(-g.LcW, -g.LcW), LcN = pair(g.LcN, g.LcN),
+                 nLcS = pair(-g.LcS, -g.LcS), LsE = pair(g.LsE, g.LsE), nLsW = pair(-g.LsW, -g.LsW),
+                 LsN = pair(g.LsN, g.LsN), nLsS = pair(-g.LsS, -g.LsS), IA = pair(g.ia, g.ia);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int a = 2 * q, b = 2 * q + 1;
+      const float2 w0 = pair(st(a, 0), st(b, 0)), we = pair(st(a, 1), st(b, 1)), ea = pair(st(a, 2), st(b, 2)),
+                   so = pair(st(a, 3), st(b, 3)), no = pair(st(a, 4), st(b, 4));
+      // the scalar form's expressions (limit_cell_var), lane by lane
+      const float2 ie = mul2(H, add2(w0, ea)), iw = mul2(H, add2(we, w0));
+      const float2 in = mul2(H, add2(w0, no)), is = mul2(H, add2(so, w0));
+      const float2 gxp = mul2(fma2(is, nLcS, fma2(in, LcN, fma2(ie, LcE, mul2(iw, nLcW)))), IA);
+      const float2 gyp = mul2(fma2(is, nLsS, fma2(in, LsN, fma2(ie, LsE, mul2(iw, nLsW)))), IA);
+      float2 hot[4];
+      float ha[4], hb[4];
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        hot[s] = fma2(gxp, pair(g.hx[s], g.hx[s]), mul2(gyp, pair(g.hy[s], g.hy[s])));
+        ha[s] = hot[s].x;
+        hb[s] = hot[s].y;
+      }
+      const float pa = phi32<LIM>(w0.x, we.x, ea.x, so.x, no.x, ha);
+      const float pb = phi32<LIM>(w0.y, we.y, ea.y, so.y, no.y, hb);
+      const float2 php = pair(pa, pb);
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        const float2 f = fma2(php, hot[s], w0);
+        face[s][a] = f.x;
+        face[s][b] = f.y;
+      }
+      gx[a] = gxp.x; gx[b] = gxp.y;
+      gy[a] = gyp.x; gy[b] = gyp.y;
+      ph[a] = pa; ph[b] = pb;
+    }
+  }
 }
 
 // A face state (reconstruction variables) rotated into the frame of vertical face f
@@ -447,17 +513,20 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
   load_cell_geo(P, B, i, j, g);
 
   T face[4][4];  // [side][var] limited face states, reconstruction variables
-#pragma unroll
-  for (int v = 0; v < 4; ++v) {
-    T fv[4], gx, gy, ph;
-    limit_cell_var<T, LIM>(sW[v][ty + 1][C0 + tx + 1], sW[v][ty + 1][C0 + tx], sW[v][ty + 1][C0 + tx + 2],
-                           sW[v][ty][C0 + tx + 1], sW[v][ty + 2][C0 + tx + 1], g, fv, gx, gy, ph);
-#pragma unroll
-    for (int s = 0; s < 4; ++s) face[s][v] = fv[s];
+  {
+    // stencil points: the cell, W, E, S, N
+    auto st = [&](int v, int p) -> T {
+      return sW[v][ty + 1 + (p == 3 ? -1 : p == 4 ? 1 : 0)][C0 + tx + 1 + (p == 1 ? -1 : p == 2 ? 1 : 0)];
+    };
+    T gx[4], gy[4], ph[4];
+    limit_cell4<T, LIM>(st, g, face, gx, gy, ph);
     if (DBG) {
-      if (dbg.gx) dbg.gx[v * P.ncell + c] = gx;
-      if (dbg.gy) dbg.gy[v * P.ncell + c] = gy;
-      if (dbg.phi) dbg.phi[v * P.ncell + c] = ph;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        if (dbg.gx) dbg.gx[v * P.ncell + c] = gx[v];
+        if (dbg.gy) dbg.gy[v * P.ncell + c] = gy[v];
+        if (dbg.phi) dbg.phi[v * P.ncell + c] = ph[v];
+      }
     }
   }
 
