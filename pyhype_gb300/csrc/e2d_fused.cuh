@@ -51,6 +51,15 @@ struct FusedSmem {
   T R[2][4][FTY + 1][TX + 1];
 };
 
+// L2 prefetch of elements [first, last] of one plane, a line at a time (every address
+// inside the plane; a bulk prefetch per range measured slower).
+template <typename T>
+__device__ __forceinline__ void prefetch_l2(const T* plane, int64_t first, int64_t last) {
+  const char* p = reinterpret_cast<const char*>(plane);
+  for (int64_t b = (first * (int64_t)sizeof(T)) & ~(int64_t)127; b <= last * (int64_t)sizeof(T); b += 128)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p + b));
+}
+
 template <typename T, int R, int C>
 __device__ __forceinline__ void put4(T (&a)[4][R][C], int r, int c, const T* w) {
   a[0][r][c] = w[0]; a[1][r][c] = w[1]; a[2][r][c] = w[2]; a[3][r][c] = w[3];
@@ -139,6 +148,64 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
   }
 }
 
+// Everything of the tile that the stage reads from global memory besides the staged
+// state, prefetched into L2 by the whole CTA at its start: the cell geometry of the
+// tile and its ring (area, 1/A, the face points' offsets), the face geometry of their
+// faces (length, L cos, L sin, and the frames of a curvilinear block), and the stage
+// program's sources for the tile's cells.  The geometry planes are larger than L2 and
+// come from HBM every stage; prefetched, the reconstruction's loads wait for L2
+// instead of HBM.  Rows and columns are clamped to the block.
+template <typename T, int FTY>
+__device__ void prefetch_tile(const ParamsT<T>& P, const TileOrigin& to, int i0, int j0,
+                              const StateBuffersT<T>& S, const StageProgram& prog) {
+  // items by constant-sized groups (divisions by constants): cell planes x FTY + 2
+  // rows, face planes x FTY + 2 (vertical) or FTY + 3 (horizontal) rows, source
+  // planes x FTY rows; rows outside the block are skipped
+  constexpr int RR = FTY + 2, NCI = 10 * RR, NVI = 5 * RR, NHI = 5 * (RR + 1);
+  const int r_lo = (i0 >= 1 ? -1 : 0), r_hi = min(FTY, to.ny - 1 - i0);  // tile rows and the ring, local
+  const int c_lo = (j0 >= 1 ? -1 : 0), c_hi = min(TX, to.nx - 1 - j0);
+  const int nfp = to.cart ? 3 : 5;  // face planes: L, L cos, L sin (, cos, sin)
+  const int tr = min(FTY, to.ny - i0), tc = min(TX, to.nx - j0);  // the tile's own cells
+  int nsrc = 0;  // source plane sets: each update's source, and U^n and its compensation for a Kahan update
+#pragma unroll
+  for (int u = 0; u < MAX_STAGES; ++u) {
+    if (u >= prog.nupd) break;
+    nsrc += (prog.upd[u].src_zero ? 0 : 1) + (prog.upd[u].kahan ? 2 : 0);
+  }
+  const int total = NCI + NVI + NHI + nsrc * 4 * FTY;
+  for (int it = threadIdx.x; it < total; it += blockDim.x) {
+    if (it < NCI) {  // A, 1/A and the offsets (E2D_G_A .. E2D_G_HY_S)
+      const int k = it / RR, r = it - k * RR - 1;
+      if (r >= r_lo && r <= r_hi) prefetch_l2(P.geo.cell[k], to.cell(r, c_lo), to.cell(r, c_hi));
+    } else if (it < NCI + NVI) {
+      const int q = it - NCI, k = q / RR, r = q - k * RR - 1;
+      if (k < nfp && r >= r_lo && r <= r_hi) prefetch_l2(P.geo.vface[k], to.vface(r, c_lo), to.vface(r, c_hi + 1));
+    } else if (it < NCI + NVI + NHI) {
+      const int q = it - NCI - NVI, k = q / (RR + 1), r = q - k * (RR + 1) - 1;
+      if (k < nfp && r >= r_lo && r <= r_hi + 1) prefetch_l2(P.geo.hface[k], to.hface(r, c_lo), to.hface(r, c_hi));
+    } else {
+      const int q = it - NCI - NVI - NHI, v = (q / FTY) & 3, r = q - (q / FTY) * FTY;
+      int n = q / (4 * FTY);  // the n-th source plane set
+      const T* base = nullptr;
+#pragma unroll
+      for (int u = 0; u < MAX_STAGES; ++u) {
+        if (u >= prog.nupd || base != nullptr) break;
+        const StageUpdate& up = prog.upd[u];
+        if (!up.src_zero) {
+          if (n == 0) base = static_cast<const T*>(up.srcp);
+          --n;
+        }
+        if (up.kahan && base == nullptr) {
+          if (n == 0) base = S.comp;
+          else if (n == 1) base = S.buf[0];
+          n -= 2;
+        }
+      }
+      if (base != nullptr && r < tr) prefetch_l2(base + (int64_t)v * P.ncell, to.cell(r, 0), to.cell(r, tc - 1));
+    }
+  }
+}
+
 template <typename T, int LIM, int RECON, int FLUX, int FTY, int NW, int MINB>
 __global__ void __launch_bounds__(NW * 32, MINB)
     k_stage_fused(ParamsT<T> P, const int4* __restrict__ tiles, const T* __restrict__ U,
@@ -160,6 +227,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
   const int nx = B->nx, ny = B->ny;
   const int i0 = tl.y, j0 = tl.z;
   const TileOrigin to{cell_at(B, i0, j0), vf_at(B, i0, j0), hf_at(B, i0, j0), nx, ny, B->is_cartesian != 0};
+  prefetch_tile<T, FTY>(P, to, i0, j0, S, prog);
   // the halo lies inside the block: no ghost cell is staged and every ring cell is real
   const bool interior = i0 >= 2 && j0 >= 2 && i0 + FTY + 2 <= ny && j0 + TX + 2 <= nx;
 
