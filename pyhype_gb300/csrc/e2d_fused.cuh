@@ -316,13 +316,24 @@ __global__ void __launch_bounds__(NW * 32, MINB)
   // ---- one flux per face of the tile (one call site for both face families) ---------
   {
     const bool cart = to.cart;
-    constexpr int FC = TX + 1, PLANE = (FTY + 1) * FC;  // a family's padded plane
-    for (int item = threadIdx.x; item < 2 * PLANE; item += FTHREADS) {
-      const int fam = item >= PLANE ? 1 : 0;
-      const bool vert = fam == 0;
-      const int h = item - fam * PLANE;
-      const int r = h / FC, c = h - r * FC;
-      const bool live = vert ? (r < FTY && i0 + r < ny && j0 + c <= nx) : (c < TX && i0 + r <= ny && j0 + c < nx);
+    // a warp per row of faces: the horizontal face rows 0..FTY, the vertical face rows
+    // 0..FTY-1 (columns 0..31), then the tile's east edge (column TX, 32 rows a job)
+    constexpr int NJ = (FTY + 1) + FTY + (FTY + 31) / 32;
+    for (int job = warp; job < NJ; job += NW) {
+      int r, c;
+      const bool vert = job > FTY;
+      if (!vert) {
+        r = job;
+        c = lane;
+      } else if (job <= 2 * FTY) {
+        r = job - FTY - 1;
+        c = lane;
+      } else {
+        r = (job - 2 * FTY - 1) * 32 + lane;
+        c = TX;
+      }
+      const int fam = vert ? 0 : 1;
+      const bool live = vert ? (r < FTY && i0 + r < ny && j0 + c <= nx) : (i0 + r <= ny && j0 + c < nx);
       if (!live) continue;
       const int64_t f = vert ? to.vface(r, c) : to.hface(r, c);
       T L[4], R[4];

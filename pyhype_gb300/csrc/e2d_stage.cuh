@@ -206,8 +206,9 @@ __device__ __forceinline__ float phi32(float w0, float we, float ea, float so, f
     smin = (s == 0) ? sl : vmin(smin, sl);
     smax = (s == 0) ? sl : vmax(smax, sl);
   }
-  float ph = psi_s<LIM>(smin);
-  if constexpr (psi_has_peak<LIM>()) ph = vmin(ph, psi_s<LIM>(smax));
+  float ph;
+  if constexpr (psi_has_peak<LIM>()) ph = psi_min_pair<LIM>(smin, smax);
+  else ph = psi_s<LIM>(smin);
   return is_neg(ph) ? 0.f : ph;
 }
 
