@@ -708,6 +708,14 @@ def main():
     from pyhype_gb300.roofline import (BYTES_PER_CELL_STAGE_FP32, BYTES_PER_CELL_STAGE_FP64, FP64_INST_PER_CELL,
                                        FP64_INST_PER_SM_CLOCK, kernel_flops)
 
+    # the CPU baseline first, while this process has done no GPU work: timed after the
+    # GPU sections it ran up to 20 % slower than the same loop in a fresh process
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu_baseline and args.precision == "fp64":
+        try:
+            cpu = cpu_baseline(args.n, args.cpu_steps)
+        except Exception as exc:  # the GPU number stands without it
+            cpu = exc
     torch.cuda.set_device(local)
     solver, cfg = make_solver(args.n)
     dev = solver.device
@@ -993,9 +1001,11 @@ def main():
         "gpu_launches": int(args.steps * (3 + 3 * stages)),
         "clocks": clocks,
     }
-    if rank == 0 and ws == 1 and not args.skip_cpu_baseline:
+    if cpu is not None:
         try:
-            line["cpu_baseline"], U0, first = cpu_baseline(args.n, args.cpu_steps)
+            if isinstance(cpu, Exception):
+                raise cpu
+            line["cpu_baseline"], U0, first = cpu
             # full-size parity: the device's first FP64 step from the same seeded state
             if not np.array_equal(U0, P.to_soa([b.state.data for b in solver.blocks])):
                 raise RuntimeError("CPU and GPU arms start from different states")

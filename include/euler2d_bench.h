@@ -50,14 +50,16 @@ E2D_API int e2d_bench_set_tma(E2DHandle h, int32_t enable);
    (8,1), (4,2), (4,4), (16,1), and (4,8) in the FP32 form, where the FP64 path
    runs variant 0), 1 = flux (variants 0..2: min CTAs per SM 4, 1, 6),
    2 = update (variant 0), 3 = stage form (variant 0: the three kernels above per
-   stage; 1: one fused stage kernel per stage, tiles of 16 x 32 cells with their face
-   states and fluxes in shared memory; stages whose updates overwrite their own
-   input, and problems with several face quadrature points, stay split).          */
+   stage; 1 and 2: one fused stage kernel per stage, with tiles of 28 x 32 cells and
+   16 warps (1) or 13 x 32 cells and 8 warps (2), face states and fluxes in shared
+   memory; stages whose updates overwrite their own input, and problems with several
+   face quadrature points, stay split).  A handle starts at form 2 in the FP32 form
+   and form 0 in FP64, the fastest of each on the benchmark problems.             */
 E2D_API int e2d_set_kernel_choice(E2DHandle h, int32_t kernel, int32_t variant, int32_t persistent);
 /* Autotuner: times every variant and grid shape of the reconstruct and flux kernels
    and the grid shape of the update kernel on the current state (`reps` launches each,
    CUDA events on the handle's stream), keeps the fastest, then compares one stage of
-   those three against one fused stage and keeps the faster form.  Returns the choices
+   those three against one fused stage of each tile shape and keeps the fastest form.  Returns the choices
    in chosen[0..7] = {reconstruct variant, persistent, flux variant, persistent,
    update variant, persistent, stage form, 0}.  Graphs captured before are dropped. */
 E2D_API int e2d_autotune(E2DHandle h, int32_t reps, int32_t* chosen);

@@ -693,6 +693,10 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
                    : launch_stage_fused<double>(h->pd.P, h->ts, form, nullptr, h->inst, h->pd.S, StageProgram{},
                                                 h->real, h->stream, nullptr, true))) != cudaSuccess)
       return bail(fail(E2D_ERR_CUDA, "fused stage kernel set-up: %s", cudaGetErrorString(ce)));
+  // the FP32 form starts with the fused stage kernel at 13-row tiles, its fastest form
+  // on the benchmark problems (e2d_autotune chooses again per problem); FP64 keeps the
+  // three kernels, its fastest
+  if (h->prec == E2D_FP32 && h->cfg.nqp <= 1) h->ks = KernelChoice{2, false};
 
   // default integrator: the classical RK4 rows (explicit_runge_kutta.py:212-224)
   const double rk4[16] = {0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1, 0, 1.0 / 6, 1.0 / 3, 1.0 / 3, 1.0 / 6};
