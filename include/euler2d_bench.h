@@ -75,6 +75,14 @@ E2D_API int e2d_check_wait_bound(int32_t complete, int32_t limit, int32_t* arriv
    values in caller device buffers, on the default stream (synchronised).  For
    testing the routine against IEEE division.                                   */
 E2D_API int e2d_check_div32(const float* a_dev, const float* b_dev, float* q_dev, int64_t n);
+/* The FP32 form's division without div32's range test (rdiv, for the state algebra's
+   positive divisors), elementwise as e2d_check_div32.                              */
+E2D_API int e2d_check_rdiv32(const float* a_dev, const float* b_dev, float* q_dev, int64_t n);
+/* The FP32 form's paired limiter-function evaluation: pair_out[i] = the paired
+   min(psi(sa[i]), psi(sb[i])), scalar_out[i] = the same from two scalar evaluations,
+   for Venkatakrishnan or van Albada (the limiters with a maximum).                 */
+E2D_API int e2d_check_psi_pair(int32_t limiter, const float* sa_dev, const float* sb_dev, float* pair_out_dev,
+                               float* scalar_out_dev, int64_t n);
 
 #ifdef __cplusplus
 }

@@ -36,6 +36,22 @@ __global__ void k_div32(const float* __restrict__ a, const float* __restrict__ b
     q[i] = e2d::div32(a[i], b[i]);
 }
 
+__global__ void k_rdiv32(const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ q,
+                         int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    q[i] = e2d::rdiv(a[i], b[i]);
+}
+
+// min(psi(s_a), psi(s_b)) by the paired evaluation and by two scalar psi_s
+template <int LIM>
+__global__ void k_psi_pair(const float* __restrict__ sa, const float* __restrict__ sb, float* __restrict__ pair_out,
+                           float* __restrict__ scalar_out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    pair_out[i] = e2d::psi_min_pair<LIM>(sa[i], sb[i]);
+    scalar_out[i] = e2d::vmin(e2d::psi_s<LIM>(sa[i]), e2d::psi_s<LIM>(sb[i]));
+  }
+}
+
 // One warp waits on a shared-memory barrier phase with the reconstruction kernel's
 // bounded wait.  complete != 0: thread 0 arrives (the phase completes); else thread 0
 // announces 16 bytes of transfer that no copy delivers, so the phase cannot complete
@@ -78,6 +94,27 @@ extern "C" int e2d_check_div32(const float* a, const float* b, float* q, int64_t
   if (!a || !b || !q || n < 0) return E2D_ERR_INVALID;
   if (n == 0) return 0;
   k_div32<<<1024, 256>>>(a, b, q, n);
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return E2D_ERR_CUDA;
+  return 0;
+}
+
+extern "C" int e2d_check_rdiv32(const float* a, const float* b, float* q, int64_t n) {
+  if (!a || !b || !q || n < 0) return E2D_ERR_INVALID;
+  if (n == 0) return 0;
+  k_rdiv32<<<1024, 256>>>(a, b, q, n);
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return E2D_ERR_CUDA;
+  return 0;
+}
+
+extern "C" int e2d_check_psi_pair(int32_t limiter, const float* sa, const float* sb, float* pair_out,
+                                  float* scalar_out, int64_t n) {
+  if (!sa || !sb || !pair_out || !scalar_out || n < 0) return E2D_ERR_INVALID;
+  if (limiter != E2D_LIM_VENKATAKRISHNAN && limiter != E2D_LIM_VAN_ALBADA) return E2D_ERR_INVALID;
+  if (n == 0) return 0;
+  if (limiter == E2D_LIM_VENKATAKRISHNAN)
+    k_psi_pair<E2D_LIM_VENKATAKRISHNAN><<<1024, 256>>>(sa, sb, pair_out, scalar_out, n);
+  else
+    k_psi_pair<E2D_LIM_VAN_ALBADA><<<1024, 256>>>(sa, sb, pair_out, scalar_out, n);
   if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return E2D_ERR_CUDA;
   return 0;
 }

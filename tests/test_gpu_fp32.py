@@ -154,3 +154,60 @@ def test_div32_matches_ieee_division():
             ref = a / b
         same = (q.view(np.uint32) == ref.view(np.uint32)) | ((q == 0) & (ref == 0)) | (np.isnan(q) & np.isnan(ref))
         assert same.all(), f"{name}: {int((~same).sum())} of {n} differ, e.g. {a[~same][:3]} / {b[~same][:3]}"
+
+
+def test_rdiv_matches_ieee_division_inside_its_range():
+    """rdiv (div32's sequence without the range test, for the state algebra's divisors)
+    equals IEEE float32 division for operands within 2^-60..2^61 and zero numerators."""
+    import ctypes
+
+    import torch
+
+    from pyhype_gb300 import _native
+
+    L = _native.load()
+    L.e2d_check_rdiv32.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
+    rng = np.random.default_rng(8)
+    n = 1 << 21
+    cases = {
+        "inside the range": (_floats(rng, n, -60, 60), _floats(rng, n, -60, 60)),
+        "densities and pressures": (_floats(rng, n, -12, 12), np.abs(_floats(rng, n, -12, 12))),
+        "zero numerators": (np.where(rng.random(n) < 0.3, np.float32(0), _floats(rng, n, -30, 30)).astype(np.float32),
+                            _floats(rng, n, -30, 30)),
+    }
+    for name, (a, b) in cases.items():
+        ad, bd = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+        qd = torch.empty_like(ad)
+        assert L.e2d_check_rdiv32(ad.data_ptr(), bd.data_ptr(), qd.data_ptr(), n) == 0
+        q = qd.cpu().numpy()
+        ref = a / b
+        same = (q.view(np.uint32) == ref.view(np.uint32)) | ((q == 0) & (ref == 0))
+        assert same.all(), f"{name}: {int((~same).sum())} of {n} differ, e.g. {a[~same][:3]} / {b[~same][:3]}"
+
+
+@pytest.mark.parametrize("limiter", [0, 2])  # Venkatakrishnan, van Albada
+def test_paired_limiter_functions_equal_scalar(limiter):
+    """The paired evaluation of min(psi(s_a), psi(s_b)) gives the two scalar
+    evaluations' value bit for bit: slopes at 0, 1 (psi_s's exact value), the peaks,
+    the cap and beyond, subnormal and random values."""
+    import ctypes
+
+    import torch
+
+    from pyhype_gb300 import _native
+
+    L = _native.load()
+    L.e2d_check_psi_pair.argtypes = [ctypes.c_int32] + [ctypes.c_void_p] * 4 + [ctypes.c_int64]
+    rng = np.random.default_rng(9 + limiter)
+    special = np.array([0.0, 1e-45, 1e-30, 0.5, 1.0, 2.0, 1 + 2 ** 0.5, 2 + 2 * 2 ** 0.5, 10.0, 1e8, 1e15, 1e20,
+                        np.inf], dtype=np.float32)
+    n = 1 << 20
+    sa = np.concatenate([np.repeat(special, special.size), np.abs(_floats(rng, n, -30, 30))]).astype(np.float32)
+    sb = np.concatenate([np.tile(special, special.size), np.abs(_floats(rng, n, -30, 30))]).astype(np.float32)
+    a, b = torch.from_numpy(sa).cuda(), torch.from_numpy(sb).cuda()
+    p, q = torch.empty_like(a), torch.empty_like(a)
+    assert L.e2d_check_psi_pair(limiter, a.data_ptr(), b.data_ptr(), p.data_ptr(), q.data_ptr(), sa.size) == 0
+    pv, qv = p.cpu().numpy(), q.cpu().numpy()
+    same = pv.view(np.uint32) == qv.view(np.uint32)
+    assert same.all(), f"{int((~same).sum())} differ, e.g. s = {sa[~same][:3]}, {sb[~same][:3]}"
+
