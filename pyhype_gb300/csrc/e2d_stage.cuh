@@ -948,38 +948,49 @@ __global__ void __launch_bounds__(TX * TY) k_update(ParamsT<T> P, const int4* __
 // CFL time step: min over cells of min(dx/(|u|+a), dy/(|v|+a)) per instance
 // (quad_block.py:423-436)
 // --------------------------------------------------------------------------------------
+// One CTA of DT_THREADS threads per cell tile (TY rows x 32 cells, one instance), each
+// thread TY / (DT_THREADS / 32) cells of its column: the cells' loads are independent
+// and in flight together, the reduction is one atomic per tile.  The minimum is exact,
+// so its order changes nothing.
+constexpr int DT_THREADS = 64;
 template <typename T>
-__global__ void __launch_bounds__(TX * TY) k_dt(ParamsT<T> P, const int4* __restrict__ tiles,
-                                                const T* __restrict__ U, InstanceState* __restrict__ inst) {
+__global__ void __launch_bounds__(DT_THREADS) k_dt(ParamsT<T> P, const int4* __restrict__ tiles,
+                                                   const T* __restrict__ U, InstanceState* __restrict__ inst) {
+  constexpr int ROWS = DT_THREADS / 32, PER = TY / ROWS;
   const int4 tl = tiles[blockIdx.x];
   const E2DBlock* B = P.blocks + tl.x;
   InstanceState* I = inst + B->instance;
-  const int ty = threadIdx.x / TX, tx = threadIdx.x - (threadIdx.x / TX) * TX;
-  const int i = tl.y + ty, j = tl.z + tx;
-  double m = __longlong_as_double(0x7ff0000000000000LL);
-  if (i < B->ny && j < B->nx) {
-    const int64_t c = cell_at(B, i, j);
-    T q[4], w[4];
-    load_cell(U, P.ncell, c, q);
-    const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
-    cons_to_prim(q, G, w);
-    const T a = sqrt(pdiv(P.gas[0] * w[3], w[0]));
-    const T tx_ = pdiv(P.geo.cell[E2D_G_CFL_DX][c], fabs(w[1]) + a);
-    const T ty_ = pdiv(P.geo.cell[E2D_G_CFL_DY][c], fabs(w[2]) + a);
-    m = double(vmin(tx_, ty_));  // the reduction itself is FP64 on every path
+  const int tx = threadIdx.x & 31, r0 = threadIdx.x >> 5;
+  const int j = tl.z + tx;
+  const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
+  unsigned long long bits = 0x7ff0000000000000ULL;  // +inf
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int i = tl.y + r0 + k * ROWS;
+    if (i < B->ny && j < B->nx) {
+      const int64_t c = cell_at(B, i, j);
+      T q[4], w[4];
+      load_cell(U, P.ncell, c, q);
+      cons_to_prim(q, G, w);
+      const T a = sqrt(pdiv(P.gas[0] * w[3], w[0]));
+      const T tx_ = pdiv(P.geo.cell[E2D_G_CFL_DX][c], fabs(w[1]) + a);
+      const T ty_ = pdiv(P.geo.cell[E2D_G_CFL_DY][c], fabs(w[2]) + a);
+      // the reduction itself is FP64 on every path
+      const unsigned long long b = (unsigned long long)__double_as_longlong(double(vmin(tx_, ty_)));
+      bits = b < bits ? b : bits;
+    }
   }
-  unsigned long long bits = (unsigned long long)__double_as_longlong(m);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long other = __shfl_xor_sync(0xffffffffu, bits, o);
     bits = other < bits ? other : bits;
   }
-  __shared__ unsigned long long wmin[TX * TY / 32];
-  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = bits;
+  __shared__ unsigned long long wmin[ROWS];
+  if (tx == 0) wmin[r0] = bits;
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long b = wmin[0];
-    for (int w = 1; w < TX * TY / 32; ++w) b = wmin[w] < b ? wmin[w] : b;
+    for (int w = 1; w < ROWS; ++w) b = wmin[w] < b ? wmin[w] : b;
     atomicMin(&I->min_bits, b);
   }
 }
@@ -1182,7 +1193,7 @@ template <typename T>
 cudaError_t launch_dt(const ParamsT<T>& P, const int4* tiles, int n, const T* U, InstanceState* inst,
                       cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  k_dt<T><<<n, TX * TY, 0, st>>>(P, tiles, U, inst);
+  k_dt<T><<<n, DT_THREADS, 0, st>>>(P, tiles, U, inst);
   return cudaGetLastError();
 }
 
