@@ -78,6 +78,9 @@ E2D_API int e2d_check_div32(const float* a_dev, const float* b_dev, float* q_dev
 /* The FP32 form's division without div32's range test (rdiv, for the state algebra's
    positive divisors), elementwise as e2d_check_div32.                              */
 E2D_API int e2d_check_rdiv32(const float* a_dev, const float* b_dev, float* q_dev, int64_t n);
+/* The FP64 divergence's division by an area through its correctly rounded reciprocal
+   (div_recip with y = 1/b): q[i] = x[i] / b[i] for b[i] > 0, elementwise.        */
+E2D_API int e2d_check_div_recip(const double* x_dev, const double* b_dev, double* q_dev, int64_t n);
 /* The FP32 form's paired limiter-function evaluation: pair_out[i] = the paired
    min(psi(sa[i]), psi(sb[i])), scalar_out[i] = the same from two scalar evaluations,
    for Venkatakrishnan or van Albada (the limiters with a maximum).                 */

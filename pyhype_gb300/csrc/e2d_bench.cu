@@ -42,6 +42,13 @@ __global__ void k_rdiv32(const float* __restrict__ a, const float* __restrict__ 
     q[i] = e2d::rdiv(a[i], b[i]);
 }
 
+// x / b by the geometry's route: div_recip with y = 1/b from IEEE division
+__global__ void k_div_recip(const double* __restrict__ x, const double* __restrict__ b, double* __restrict__ q,
+                            int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    q[i] = e2d::div_recip(x[i], b[i], 1.0 / b[i]);
+}
+
 // min(psi(s_a), psi(s_b)) by the paired evaluation and by two scalar psi_s
 template <int LIM>
 __global__ void k_psi_pair(const float* __restrict__ sa, const float* __restrict__ sb, float* __restrict__ pair_out,
@@ -102,6 +109,14 @@ extern "C" int e2d_check_rdiv32(const float* a, const float* b, float* q, int64_
   if (!a || !b || !q || n < 0) return E2D_ERR_INVALID;
   if (n == 0) return 0;
   k_rdiv32<<<1024, 256>>>(a, b, q, n);
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return E2D_ERR_CUDA;
+  return 0;
+}
+
+extern "C" int e2d_check_div_recip(const double* x, const double* b, double* q, int64_t n) {
+  if (!x || !b || !q || n < 0) return E2D_ERR_INVALID;
+  if (n == 0) return 0;
+  k_div_recip<<<1024, 256>>>(x, b, q, n);
   if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return E2D_ERR_CUDA;
   return 0;
 }

@@ -367,10 +367,11 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     if (r < FTY && i < ny && j < nx) {
       const int64_t c = to.cell(r, lane);
       const T A = P.geo.cell[E2D_G_A][c];
+      const T iA = sizeof(T) == 8 ? P.geo.cell[E2D_G_INV_A][c] : T(0);
       T k[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) k[v] = cell_dudt(sm.L[0][v][r][lane], sm.L[0][v][r][lane + 1], sm.L[1][v][r][lane],
-                                                   sm.L[1][v][r + 1][lane], A);
+                                                   sm.L[1][v][r + 1][lane], A, iA);
       stage_program(P, S, prog, I->dt, c, k);
       if (prog.final_stage) {
         const T rho = S.buf[0][c], E = S.buf[0][3 * P.ncell + c];

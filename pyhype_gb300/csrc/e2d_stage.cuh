@@ -372,13 +372,14 @@ __device__ __forceinline__ void hface_flux(const ParamsT<T>& P, const Gas<T>& G,
   I[0] = len * twice(Fy[0]); I[1] = len * twice(Fy[1]); I[2] = len * twice(Fy[2]); I[3] = len * twice(Fy[3]);
 }
 
-// dUdt of one variable of a cell from its integrated face fluxes and area
-// (fvm/base.py:171-190): 0.5 * (((I_W - I_E) + I_S) - I_N) / A.  The FP32 form divides
-// by the (positive, normal) area with rdiv.
+// dUdt of one variable of a cell from its integrated face fluxes, area A and 1/A
+// (fvm/base.py:171-190): 0.5 * (((I_W - I_E) + I_S) - I_N) / A.  FP64 divides with the
+// geometry's correctly rounded 1/A (div_recip: the IEEE quotient); the FP32 form by
+// the (positive, normal) area with rdiv.
 template <typename T>
-__device__ __forceinline__ T cell_dudt(T IW, T IE, T IS, T IN, T A) {
+__device__ __forceinline__ T cell_dudt(T IW, T IE, T IS, T IN, T A, T iA) {
   if constexpr (sizeof(T) == 4) return rdiv(half(IW - IE + IS - IN), A);
-  else return qdiv(half(IW - IE + IS - IN), A);
+  else return div_recip(half(IW - IE + IS - IN), A, iA);
 }
 
 // The RK stage program at cell c: every partial Butcher sum this stage contributes
@@ -906,11 +907,12 @@ __device__ __forceinline__ void update_tile(const ParamsT<T>& P, const int4 tl, 
     const int64_t fW = vf_at(B, i, j), fE = fW + 1;
     const int64_t fS = hf_at(B, i, j), fN = fS + B->nx;
     const T A = P.geo.cell[E2D_G_A][c];
+    const T iA = sizeof(T) == 8 ? P.geo.cell[E2D_G_INV_A][c] : T(0);
     T k[4];
 #pragma unroll
     for (int v = 0; v < 4; ++v)
       k[v] = cell_dudt(F.vI[v * P.nvface + fW], F.vI[v * P.nvface + fE], F.hI[v * P.nhface + fS],
-                       F.hI[v * P.nhface + fN], A);
+                       F.hI[v * P.nhface + fN], A, iA);
     if (dudt_out) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) dudt_out[v * P.ncell + c] = k[v];
