@@ -173,6 +173,18 @@ int forward_step(E2DSolver* h, T* stage_out, T* face_out) {
   for (int s = 0; s < h->nstages; ++s) {
     const T* in = p.S.buf[h->stage_input[s]];
     FaceArraysT<T> F = p.F;
+    if (h->use_fused(s)) {
+      // one launch; kept for the reverse pass it records the stage's input and face
+      // states, the same values the split kernels leave
+      FusedRecordT<T> rec{};
+      if (stage_out) {
+        F = face_slot<T>(h, face_out + (size_t)s * face_set_size(h));
+        rec = FusedRecordT<T>{stage_out + (size_t)s * n, F.vL, F.vR, F.hL, F.hR};
+      }
+      CK(launch_stage_fused<T>(p.P, h->ts, h->ks.variant, in, h->inst, p.S, h->prog[s], h->real, h->stream,
+                               h->tma_for(in), false, rec));
+      continue;
+    }
     if (stage_out) {
       T* Y = stage_out + (size_t)s * n;
       CK(cudaMemcpyAsync(Y, in, sizeof(T) * n, cudaMemcpyDeviceToDevice, h->stream));

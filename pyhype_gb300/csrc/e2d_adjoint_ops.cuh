@@ -11,6 +11,22 @@
 
 namespace e2d {
 
+// Divisions of the reverse state algebra by positive divisors (densities and their
+// square roots, sound speeds, Q0, the limiter functions' denominators, the Harten
+// width, gamma - 1): FP64 as the forward's qdiv/pdiv; the FP32 form without div32's
+// range test (rdiv: the same quotient for operands within 2^-60..2^61).  The HLL
+// family's divisions by wave speeds, which may approach zero, keep qdiv/pdiv.
+template <typename T>
+__device__ __forceinline__ T aqdiv(T a, T b) {
+  if constexpr (sizeof(T) == 4) return rdiv(a, b);
+  else return qdiv(a, b);
+}
+template <typename T>
+__device__ __forceinline__ T apdiv(T a, T b) {
+  if constexpr (sizeof(T) == 4) return rdiv(a, b);
+  else return pdiv(a, b);
+}
+
 template <typename T>
 __device__ __forceinline__ T sgn(T x) { return x > T(0) ? T(1) : (x < T(0) ? T(-1) : T(0)); }
 
@@ -18,16 +34,16 @@ __device__ __forceinline__ T sgn(T x) { return x > T(0) ? T(1) : (x < T(0) ? T(-
 template <typename T>
 __device__ __forceinline__ void cons_to_prim_vjp(const T* U, const Gas<T>& G, const T* lW, T* lU) {
   const T rho = U[0];
-  const T u = qdiv(U[1], rho), v = qdiv(U[2], rho);
+  const T u = aqdiv(U[1], rho), v = aqdiv(U[2], rho);
   // p = gm1 * (E - rho * 0.5 * (u*u + v*v))
   const T lp = lW[3];
   T lu = lW[1] - lp * G.gm1 * rho * u;
   T lv = lW[2] - lp * G.gm1 * rho * v;
   T lrho = lW[0] - half(lp * G.gm1) * (u * u + v * v);
   // u = rhou / rho, v = rhov / rho
-  lU[1] += qdiv(lu, rho);
-  lU[2] += qdiv(lv, rho);
-  lU[0] += lrho - qdiv(lu * u + lv * v, rho);
+  lU[1] += aqdiv(lu, rho);
+  lU[2] += aqdiv(lv, rho);
+  lU[0] += lrho - aqdiv(lu * u + lv * v, rho);
   lU[3] += lp * G.gm1;
 }
 
@@ -49,15 +65,15 @@ __device__ __forceinline__ T psi_deriv(T s) {
   if (LIM == E2D_LIM_BARTH_JESPERSEN) return (s < T(1)) ? T(1) : T(0);  // min(1, s)
   if (LIM == E2D_LIM_VAN_LEER) {  // (|s| + s)/(s + 1), with d|s|/ds = 0 at s = 0
     const T d = s + T(1);
-    return pdiv((sgn(s) + T(1)) - qdiv(fabs(s) + s, d), d);
+    return apdiv((sgn(s) + T(1)) - aqdiv(fabs(s) + s, d), d);
   }
   if (vlt(sizeof(T) == 4 ? T(SLOPE_CAP_FP32) : T(SLOPE_CAP_FP64), s)) return T(0);  // capped: constant
   if (LIM == E2D_LIM_VAN_ALBADA) {  // (s^2 + s)/(s^2 + 1)
     const T d = s * s + T(1);
-    return pdiv(pdiv(T(1) + twice(s) - s * s, d), d);
+    return apdiv(apdiv(T(1) + twice(s) - s * s, d), d);
   }
   const T d = s * s + s + T(2);  // Venkatakrishnan (s^2 + 2s)/(s^2 + s + 2)
-  return pdiv(pdiv(T(4) + T(4) * s - s * s, d), d);
+  return apdiv(apdiv(T(4) + T(4) * s - s * s, d), d);
 }
 
 // F = roe_flux(WL, WR): lamWL += (dF/dWL)^T lamF, lamWR += (dF/dWR)^T lamF
@@ -65,23 +81,23 @@ template <typename T>
 __device__ void roe_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* lF, T* lL, T* lR) {
   // ---- forward (same expressions as roe_flux) ----
   const T sqL = sqrt(L[0]), sqR = sqrt(R[0]);
-  const T inv = pdiv(T(1), sqL + sqR);
+  const T inv = apdiv(T(1), sqL + sqR);
   const T Q0 = sqrt(L[0] * R[0]);
   const T n1 = L[1] * sqL + R[1] * sqR, n2 = L[2] * sqL + R[2] * sqR, n3 = L[3] * sqL + R[3] * sqR;
   const T Q1 = n1 * inv, Q2 = n2 * inv, Q3 = n3 * inv;
-  const T aR = sqrt(pdiv(G.g * R[3], R[0])), aL = sqrt(pdiv(G.g * L[3], L[0])), aQ = sqrt(pdiv(G.g * Q3, Q0));
+  const T aR = sqrt(apdiv(G.g * R[3], R[0])), aL = sqrt(apdiv(G.g * L[3], L[0])), aQ = sqrt(apdiv(G.g * Q3, Q0));
   const T Lm0 = Q1 - aQ, Lp0 = Q1 + aQ;
   const T slowR = R[1] - aR, fastR = R[1] + aR, slowL = L[1] - aL, fastL = L[1] + aL;
   const T tp0 = twice(slowR - slowL), tm0 = twice(fastR - fastL);
   const bool tp_pos = is_pos(tp0), tm_pos = is_pos(tm0);
   const T tp = tp_pos ? tp0 : T(1e-8), tm = tm_pos ? tm0 : T(1e-8);
   const bool cm = vlt(T(fabs(Lm0)), tp), cp = vlt(T(fabs(Lp0)), tm);
-  const T Lm = cm ? half(qdiv(Lm0 * Lm0, tp) + tp) : Lm0;
-  const T Lp = cp ? half(qdiv(Lp0 * Lp0, tm) + tm) : Lp0;
+  const T Lm = cm ? half(aqdiv(Lm0 * Lm0, tp) + tp) : Lm0;
+  const T Lp = cp ? half(aqdiv(Lp0 * Lp0, tm) + tm) : Lp0;
   const T Ek = half(Q1 * Q1 + Q2 * Q2);
-  const T H = pdiv(G.gm * Q3, Q0) + Ek;
+  const T H = apdiv(G.gm * Q3, Q0) + Ek;
   const T ua = Q1 * aQ;
-  const T ia = pdiv(T(1), aQ);
+  const T ia = apdiv(T(1), aQ);
   const T one_a2 = ia * ia;
   const T h = half(one_a2);
   const T r2a = half(Q0) * ia;
@@ -118,20 +134,20 @@ __device__ void roe_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* l
   // ua = Q1*aQ ; H = gm*Q3/Q0 + Ek ; Ek = 0.5*(Q1^2 + Q2^2)
   lQ1 += aQ * lua;
   laQ += Q1 * lua;
-  T lQ3 = pdiv(G.gm, Q0) * lH;
-  lQ0 += pdiv(-G.gm * Q3, Q0 * Q0) * lH;
+  T lQ3 = apdiv(G.gm, Q0) * lH;
+  lQ0 += apdiv(-G.gm * Q3, Q0 * Q0) * lH;
   lEk += lH;
   lQ1 += Q1 * lEk;
   lQ2 += Q2 * lEk;
   // Harten
   T lLm0 = lLm, lLp0 = lLp, ltp = T(0), ltm = T(0);
   if (cm) {
-    lLm0 = lLm * qdiv(Lm0, tp);
-    ltp = half(lLm) * (T(1) - qdiv(Lm0 * Lm0, tp * tp));
+    lLm0 = lLm * aqdiv(Lm0, tp);
+    ltp = half(lLm) * (T(1) - aqdiv(Lm0 * Lm0, tp * tp));
   }
   if (cp) {
-    lLp0 = lLp * qdiv(Lp0, tm);
-    ltm = half(lLp) * (T(1) - qdiv(Lp0 * Lp0, tm * tm));
+    lLp0 = lLp * aqdiv(Lp0, tm);
+    ltm = half(lLp) * (T(1) - aqdiv(Lp0 * Lp0, tm * tm));
   }
   if (!tp_pos) ltp = T(0);
   if (!tm_pos) ltm = T(0);
@@ -142,12 +158,12 @@ __device__ void roe_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* l
   T lR1 = lslowR + lfastR, lL1 = lslowL + lfastL;
   const T laR = lfastR - lslowR, laL = lfastL - lslowL;
   // sound speeds a = sqrt(g p / rho)
-  T lR0 = qdiv(-laR * G.g * R[3], twice(aR) * R[0] * R[0]);
-  T lR3 = qdiv(laR * G.g, twice(aR) * R[0]);
-  T lL0 = qdiv(-laL * G.g * L[3], twice(aL) * L[0] * L[0]);
-  T lL3 = qdiv(laL * G.g, twice(aL) * L[0]);
-  lQ3 += qdiv(laQ * G.g, twice(aQ) * Q0);
-  lQ0 += qdiv(-laQ * G.g * Q3, twice(aQ) * Q0 * Q0);
+  T lR0 = aqdiv(-laR * G.g * R[3], twice(aR) * R[0] * R[0]);
+  T lR3 = aqdiv(laR * G.g, twice(aR) * R[0]);
+  T lL0 = aqdiv(-laL * G.g * L[3], twice(aL) * L[0] * L[0]);
+  T lL3 = aqdiv(laL * G.g, twice(aL) * L[0]);
+  lQ3 += aqdiv(laQ * G.g, twice(aQ) * Q0);
+  lQ0 += aqdiv(-laQ * G.g * Q3, twice(aQ) * Q0 * Q0);
   // Roe averages
   const T linv = lQ1 * n1 + lQ2 * n2 + lQ3 * n3;
   lL1 += lQ1 * inv * sqL;
@@ -157,8 +173,8 @@ __device__ void roe_flux_vjp(const T* L, const T* R, const Gas<T>& G, const T* l
   lR3 += lQ3 * inv * sqR;
   T lsqL = (lQ1 * L[1] + lQ2 * L[2] + lQ3 * L[3]) * inv - inv * inv * linv;
   T lsqR = (lQ1 * R[1] + lQ2 * R[2] + lQ3 * R[3]) * inv - inv * inv * linv;
-  lL0 += qdiv(lQ0 * R[0], twice(Q0)) + qdiv(lsqL, twice(sqL));
-  lR0 += qdiv(lQ0 * L[0], twice(Q0)) + qdiv(lsqR, twice(sqR));
+  lL0 += aqdiv(lQ0 * R[0], twice(Q0)) + aqdiv(lsqL, twice(sqL));
+  lR0 += aqdiv(lQ0 * L[0], twice(Q0)) + aqdiv(lsqR, twice(sqR));
   // dW = R - L
   lR0 += ld0; lR1 += ld1; lR2 += ld2; lR3 += ld3;
   lL0 -= ld0; lL1 -= ld1; lL2 -= ld2; lL3 -= ld3;
@@ -204,15 +220,15 @@ template <typename T>
 __device__ __forceinline__ void hll_bounds(const T* L, const T* R, const Gas<T>& G, HllBounds<T>& b) {
   b.sqL = sqrt(L[0]);
   b.sqR = sqrt(R[0]);
-  b.inv = pdiv(T(1), b.sqL + b.sqR);
+  b.inv = apdiv(T(1), b.sqL + b.sqR);
   b.Q0 = sqrt(L[0] * R[0]);
   b.n1 = L[1] * b.sqL + R[1] * b.sqR;
   b.n3 = L[3] * b.sqL + R[3] * b.sqR;
   b.Q1 = b.n1 * b.inv;
   b.Q3 = b.n3 * b.inv;
-  b.aL = sqrt(pdiv(G.g * L[3], L[0]));
-  b.aR = sqrt(pdiv(G.g * R[3], R[0]));
-  b.aQ = sqrt(pdiv(G.g * b.Q3, b.Q0));
+  b.aL = sqrt(apdiv(G.g * L[3], L[0]));
+  b.aR = sqrt(apdiv(G.g * R[3], R[0]));
+  b.aQ = sqrt(apdiv(G.g * b.Q3, b.Q0));
   b.rs0 = b.Q1 - b.aQ;
   b.rf0 = b.Q1 + b.aQ;
   const T slowL = L[1] - b.aL, fastL = L[1] + b.aL, slowR = R[1] - b.aR, fastR = R[1] + b.aR;
@@ -223,8 +239,8 @@ __device__ __forceinline__ void hll_bounds(const T* L, const T* R, const Gas<T>&
   b.tm = b.tm_pos ? tm0 : T(1e-8);
   b.cs = vlt(T(fabs(b.rs0)), b.tp);
   b.cf = vlt(T(fabs(b.rf0)), b.tm);
-  const T rs = b.cs ? half(qdiv(b.rs0 * b.rs0, b.tp) + b.tp) : b.rs0;
-  const T rf = b.cf ? half(qdiv(b.rf0 * b.rf0, b.tm) + b.tm) : b.rf0;
+  const T rs = b.cs ? half(aqdiv(b.rs0 * b.rs0, b.tp) + b.tp) : b.rs0;
+  const T rf = b.cf ? half(aqdiv(b.rf0 * b.rf0, b.tm) + b.tm) : b.rf0;
   b.plus_fastR = !vlt(fastR, rf);
   b.minus_slowL = !vlt(rs, slowL);
   b.Lp = b.plus_fastR ? fastR : rf;
@@ -242,12 +258,12 @@ __device__ __forceinline__ void hll_bounds_vjp(const T* L, const T* R, const Gas
   // Harten's correction of the Roe speeds
   T lrs0 = lrs, lrf0 = lrf, ltp = T(0), ltm = T(0);
   if (b.cs) {
-    lrs0 = lrs * qdiv(b.rs0, b.tp);
-    ltp = half(lrs) * (T(1) - qdiv(b.rs0 * b.rs0, b.tp * b.tp));
+    lrs0 = lrs * aqdiv(b.rs0, b.tp);
+    ltp = half(lrs) * (T(1) - aqdiv(b.rs0 * b.rs0, b.tp * b.tp));
   }
   if (b.cf) {
-    lrf0 = lrf * qdiv(b.rf0, b.tm);
-    ltm = half(lrf) * (T(1) - qdiv(b.rf0 * b.rf0, b.tm * b.tm));
+    lrf0 = lrf * aqdiv(b.rf0, b.tm);
+    ltm = half(lrf) * (T(1) - aqdiv(b.rf0 * b.rf0, b.tm * b.tm));
   }
   if (!b.tp_pos) ltp = T(0);
   if (!b.tm_pos) ltm = T(0);
@@ -262,12 +278,12 @@ __device__ __forceinline__ void hll_bounds_vjp(const T* L, const T* R, const Gas
   lL[1] += lslowL + lfastL;
   const T laR = lfastR - lslowR, laL = lfastL - lslowL;
   // sound speeds a = sqrt(g p / rho)
-  lR[0] += qdiv(-laR * G.g * R[3], twice(b.aR) * R[0] * R[0]);
-  lR[3] += qdiv(laR * G.g, twice(b.aR) * R[0]);
-  lL[0] += qdiv(-laL * G.g * L[3], twice(b.aL) * L[0] * L[0]);
-  lL[3] += qdiv(laL * G.g, twice(b.aL) * L[0]);
-  const T lQ3 = qdiv(laQ * G.g, twice(b.aQ) * b.Q0);
-  const T lQ0 = qdiv(-laQ * G.g * b.Q3, twice(b.aQ) * b.Q0 * b.Q0);
+  lR[0] += aqdiv(-laR * G.g * R[3], twice(b.aR) * R[0] * R[0]);
+  lR[3] += aqdiv(laR * G.g, twice(b.aR) * R[0]);
+  lL[0] += aqdiv(-laL * G.g * L[3], twice(b.aL) * L[0] * L[0]);
+  lL[3] += aqdiv(laL * G.g, twice(b.aL) * L[0]);
+  const T lQ3 = aqdiv(laQ * G.g, twice(b.aQ) * b.Q0);
+  const T lQ0 = aqdiv(-laQ * G.g * b.Q3, twice(b.aQ) * b.Q0 * b.Q0);
   // Roe average (Q2 does not enter these fluxes)
   const T linv = lQ1 * b.n1 + lQ3 * b.n3;
   lL[1] += lQ1 * b.inv * b.sqL;
@@ -276,8 +292,8 @@ __device__ __forceinline__ void hll_bounds_vjp(const T* L, const T* R, const Gas
   lR[3] += lQ3 * b.inv * b.sqR;
   const T lsqL = (lQ1 * L[1] + lQ3 * L[3]) * b.inv - b.inv * b.inv * linv;
   const T lsqR = (lQ1 * R[1] + lQ3 * R[3]) * b.inv - b.inv * b.inv * linv;
-  lL[0] += qdiv(lQ0 * R[0], twice(b.Q0)) + qdiv(lsqL, twice(b.sqL));
-  lR[0] += qdiv(lQ0 * L[0], twice(b.Q0)) + qdiv(lsqR, twice(b.sqR));
+  lL[0] += aqdiv(lQ0 * R[0], twice(b.Q0)) + aqdiv(lsqL, twice(b.sqL));
+  lR[0] += aqdiv(lQ0 * L[0], twice(b.Q0)) + aqdiv(lsqR, twice(b.sqR));
 }
 
 // U = prim_to_cons(W) and F = {U1, U1 W1 + W3, U1 W2, W1 (U3 + W3)} (PrimitiveState.F
@@ -303,7 +319,7 @@ __device__ __forceinline__ void cons_and_flux_vjp(const T* W, const Gas<T>& G, c
   lW[0] += lU[0] + lU[1] * W[1] + lU[2] * W[2] + lU[3] * half(W[1] * W[1] + W[2] * W[2]);
   lW[1] += lU[1] * W[0] + lU[3] * W[0] * W[1];
   lW[2] += lU[2] * W[0] + lU[3] * W[0] * W[2];
-  lW[3] += pdiv(lU[3], G.gm1);
+  lW[3] += apdiv(lU[3], G.gm1);
 }
 
 // F = hlll_flux(WL, WR) (pyhype/flux/HLLL.py:25-103).  Subgradients: the branch the

@@ -327,7 +327,7 @@ static int bench_kernels_t(E2DHandle h, int32_t steps, double* ms, int64_t* laun
       if (h->use_fused(s)) {
         CK(rec(5));
         CK(launch_stage_fused<T>(p.P, h->ts, h->ks.variant, in, h->inst, p.S, h->prog[s], h->real, h->stream,
-                                 h->tma_for(in), false));
+                                 h->tma_for(in), false, FusedRecordT<T>{}));
         CK(fin());
         continue;
       }
@@ -455,7 +455,7 @@ static int time_kernel(E2DHandle h, int which, int reps, float* ms) {
     else if (which == 1) CK(launch_flux<T>(p.P, h->ts, h->kf, h->inst, p.F, nullptr, h->stream));
     else if (which == 2) CK(launch_update<T>(p.P, h->ts, h->ku, p.F, p.S, none, h->inst, h->real, nullptr, h->stream));
     else CK(launch_stage_fused<T>(p.P, h->ts, h->ks.variant, p.S.buf[0], h->inst, p.S, none, h->real, h->stream,
-                                  h->tma_for(p.S.buf[0]), false));
+                                  h->tma_for(p.S.buf[0]), false, FusedRecordT<T>{}));
   }
   CK(cudaEventRecord(e1, h->stream));
   CK(cudaEventSynchronize(e1));
@@ -689,9 +689,9 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
   for (int form = 1; form < N_STAGE_FORMS; ++form)
     if ((ce = (h->prec == E2D_FP32
                    ? launch_stage_fused<float>(h->pf.P, h->ts, form, nullptr, h->inst, h->pf.S, StageProgram{}, h->real,
-                                               h->stream, nullptr, true)
+                                               h->stream, nullptr, true, FusedRecordT<float>{})
                    : launch_stage_fused<double>(h->pd.P, h->ts, form, nullptr, h->inst, h->pd.S, StageProgram{},
-                                                h->real, h->stream, nullptr, true))) != cudaSuccess)
+                                                h->real, h->stream, nullptr, true, FusedRecordT<double>{}))) != cudaSuccess)
       return bail(fail(E2D_ERR_CUDA, "fused stage kernel set-up: %s", cudaGetErrorString(ce)));
   // the FP32 form starts with the fused stage kernel at 13-row tiles, its fastest form
   // on the benchmark problems (e2d_autotune chooses again per problem); FP64 keeps the
@@ -797,7 +797,7 @@ static int enqueue_stages(E2DHandle h, T* dudt_out, const DebugOutT<T>* dbg) {
     const T* in = p.S.buf[h->stage_input[s]];
     if (!dudt_out && !dbg && h->use_fused(s)) {
       CK(launch_stage_fused<T>(p.P, h->ts, h->ks.variant, in, h->inst, p.S, h->prog[s], h->real, h->stream,
-                               h->tma_for(in), false));
+                               h->tma_for(in), false, FusedRecordT<T>{}));
       continue;
     }
     CK(launch_reconstruct<T>(p.P, h->ts, h->kr, in, h->inst, p.F, dbg, h->stream, h->tma_for(in)));

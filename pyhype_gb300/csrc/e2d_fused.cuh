@@ -210,7 +210,7 @@ template <typename T, int LIM, int RECON, int FLUX, int FTY, int NW, int MINB>
 __global__ void __launch_bounds__(NW * 32, MINB)
     k_stage_fused(ParamsT<T> P, const int4* __restrict__ tiles, const T* __restrict__ U,
                   InstanceState* __restrict__ inst, StateBuffersT<T> S, StageProgram prog,
-                  RealizState* __restrict__ real, TmaTiles tma) {
+                  RealizState* __restrict__ real, TmaTiles tma, FusedRecordT<T> rec) {
   constexpr int FTHREADS = NW * 32;
   constexpr int RING_COL_TASKS = (2 * FTY + 31) / 32;  // the W and E ring columns, 32 cells a task
   static_assert(FTY + 2 + RING_COL_TASKS <= 2 * NW, "tile rows and ring tasks must fill two rounds of warps");
@@ -342,6 +342,16 @@ __global__ void __launch_bounds__(NW * 32, MINB)
         L[v] = sm.L[fam][v][r][c];
         R[v] = sm.R[fam][v][r][c];
       }
+      if (rec.vL) {  // the face states for the adjoint, where the split reconstruction puts them
+        T* rl = vert ? rec.vL : rec.hL;
+        T* rr = vert ? rec.vR : rec.hR;
+        const int64_t nf = vert ? P.nvface : P.nhface;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          rl[v * nf + f] = L[v];
+          rr[v * nf + f] = R[v];
+        }
+      }
       T Fq[4];
       riemann<FLUX>(L, R, G, Fq);
       // rotated back to the x/y frame and integrated, as vface_flux / hface_flux
@@ -366,6 +376,10 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     bool bad = false;
     if (r < FTY && i < ny && j < nx) {
       const int64_t c = to.cell(r, lane);
+      if (rec.y) {  // the stage's input state for the adjoint
+#pragma unroll
+        for (int v = 0; v < 4; ++v) rec.y[v * P.ncell + c] = U[v * P.ncell + c];
+      }
       const T A = P.geo.cell[E2D_G_A][c];
       const T iA = sizeof(T) == 8 ? P.geo.cell[E2D_G_INV_A][c] : T(0);
       T k[4];
@@ -391,7 +405,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
 template <typename T, int LIM, int RECON, int FLUX, int FORM>
 static cudaError_t fused_launch(const ParamsT<T>& P, const TileSet& ts, const T* U, InstanceState* inst,
                                 StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
-                                const TmaSet* tset, bool prepare_only) {
+                                const TmaSet* tset, bool prepare_only, const FusedRecordT<T>& rec) {
   constexpr int FTY = FUSED_TY[FORM], NW = FUSED_WARPS[FORM];
   // CTAs an SM holds at 64 registers a thread (FP32) or 128 (FP64): 65536 / (regs x NW x 32)
   constexpr int MINB = (sizeof(T) == 4 ? 32 : 16) / NW;
@@ -400,27 +414,28 @@ static cudaError_t fused_launch(const ParamsT<T>& P, const TileSet& ts, const T*
   if (prepare_only) return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   const TmaTiles tma = tset ? tset->fused[FORM] : TmaTiles{nullptr, nullptr, nullptr};
   if (ts.nfused[FORM] <= 0) return cudaSuccess;
-  kern<<<ts.nfused[FORM], NW * 32, bytes, st>>>(P, ts.fused[FORM], U, inst, S, resolve_program(prog, S), real, tma);
+  kern<<<ts.nfused[FORM], NW * 32, bytes, st>>>(P, ts.fused[FORM], U, inst, S, resolve_program(prog, S), real, tma,
+                                                rec);
   return cudaGetLastError();
 }
 
 template <typename T, int LIM, int RECON, int FLUX>
 static cudaError_t fused_form(const ParamsT<T>& P, const TileSet& ts, int form, const T* U, InstanceState* inst,
                               StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
-                              const TmaSet* tma, bool prepare_only) {
-  if (form == 2) return fused_launch<T, LIM, RECON, FLUX, 1>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);
-  return fused_launch<T, LIM, RECON, FLUX, 0>(P, ts, U, inst, S, prog, real, st, tma, prepare_only);
+                              const TmaSet* tma, bool prepare_only, const FusedRecordT<T>& rec) {
+  if (form == 2) return fused_launch<T, LIM, RECON, FLUX, 1>(P, ts, U, inst, S, prog, real, st, tma, prepare_only, rec);
+  return fused_launch<T, LIM, RECON, FLUX, 0>(P, ts, U, inst, S, prog, real, st, tma, prepare_only, rec);
 }
 
 template <typename T, int LIM>
 cudaError_t fused_lim(const ParamsT<T>& P, const TileSet& ts, int form, const T* U, InstanceState* inst,
                       StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
-                      const TmaSet* tma, bool prepare_only) {
+                      const TmaSet* tma, bool prepare_only, const FusedRecordT<T>& rec) {
 #define E2D_FUSED_FLUX(RC)                                                                                          \
   switch (P.flux) {                                                                                                 \
-    case E2D_FLUX_HLLL: return fused_form<T, LIM, RC, E2D_FLUX_HLLL>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only); \
-    case E2D_FLUX_HLLE: return fused_form<T, LIM, RC, E2D_FLUX_HLLE>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only); \
-    default: return fused_form<T, LIM, RC, E2D_FLUX_ROE>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only);   \
+    case E2D_FLUX_HLLL: return fused_form<T, LIM, RC, E2D_FLUX_HLLL>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only, rec); \
+    case E2D_FLUX_HLLE: return fused_form<T, LIM, RC, E2D_FLUX_HLLE>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only, rec); \
+    default: return fused_form<T, LIM, RC, E2D_FLUX_ROE>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only, rec);   \
   }
   if (P.recon == E2D_RECON_PRIMITIVE) {
     E2D_FUSED_FLUX(E2D_RECON_PRIMITIVE)
@@ -432,7 +447,7 @@ cudaError_t fused_lim(const ParamsT<T>& P, const TileSet& ts, int form, const T*
 #define E2D_FUSED_LIM_DECL(PRE, T, LIM)                                                                           \
   PRE template cudaError_t fused_lim<T, LIM>(const ParamsT<T>&, const TileSet&, int, const T*, InstanceState*,    \
                                              StateBuffersT<T>, const StageProgram&, RealizState*, cudaStream_t,   \
-                                             const TmaSet*, bool);
+                                             const TmaSet*, bool, const FusedRecordT<T>&);
 #define E2D_EXTERN_FUSED_LIM(T)    \
   E2D_FUSED_LIM_DECL(extern, T, 0) \
   E2D_FUSED_LIM_DECL(extern, T, 1) \
@@ -445,20 +460,20 @@ cudaError_t fused_lim(const ParamsT<T>& P, const TileSet& ts, int form, const T*
 template <typename T>
 cudaError_t launch_stage_fused(const ParamsT<T>& P, const TileSet& ts, int form, const T* U, InstanceState* inst,
                                StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
-                               const TmaSet* tma, bool prepare_only) {
+                               const TmaSet* tma, bool prepare_only, const FusedRecordT<T>& rec) {
   switch (P.limiter) {
     case E2D_LIM_BARTH_JESPERSEN:
-      return fused_lim<T, E2D_LIM_BARTH_JESPERSEN>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only);
+      return fused_lim<T, E2D_LIM_BARTH_JESPERSEN>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only, rec);
     case E2D_LIM_VAN_ALBADA:
-      return fused_lim<T, E2D_LIM_VAN_ALBADA>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only);
-    case E2D_LIM_VAN_LEER: return fused_lim<T, E2D_LIM_VAN_LEER>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only);
-    default: return fused_lim<T, E2D_LIM_VENKATAKRISHNAN>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only);
+      return fused_lim<T, E2D_LIM_VAN_ALBADA>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only, rec);
+    case E2D_LIM_VAN_LEER: return fused_lim<T, E2D_LIM_VAN_LEER>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only, rec);
+    default: return fused_lim<T, E2D_LIM_VENKATAKRISHNAN>(P, ts, form, U, inst, S, prog, real, st, tma, prepare_only, rec);
   }
 }
 
 #define E2D_INSTANTIATE_FUSED_LAUNCHER(T)                                                                        \
   template cudaError_t launch_stage_fused<T>(const ParamsT<T>&, const TileSet&, int, const T*, InstanceState*,    \
                                              StateBuffersT<T>, const StageProgram&, RealizState*, cudaStream_t,  \
-                                             const TmaSet*, bool);
+                                             const TmaSet*, bool, const FusedRecordT<T>&);
 
 }  // namespace e2d

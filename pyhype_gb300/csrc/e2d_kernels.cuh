@@ -201,12 +201,23 @@ cudaError_t launch_totals(const ParamsT<T>& P, const int4* tiles, int n, const T
 template <typename T>
 cudaError_t launch_ghost_layer(const ParamsT<T>& P, const T* U, double t, const int64_t* base, double* out,
                                int64_t nghost, int maxlen, cudaStream_t st);
+// What a fused stage records for the adjoint's reverse pass (null: nothing): its
+// input state (4 planes, y) and its face states in the split reconstruction's face
+// arrays (vL, vR, hL, hR)
+template <typename T>
+struct FusedRecordT {
+  T* y;
+  T* vL;
+  T* vR;
+  T* hL;
+  T* hR;
+};
 // one RK stage in one launch (e2d_fused.cuh); prepare_only sets the kernel's shared
 // memory limit on the current device and launches nothing
 template <typename T>
 cudaError_t launch_stage_fused(const ParamsT<T>& P, const TileSet& ts, int form, const T* U, InstanceState* inst,
                                StateBuffersT<T> S, const StageProgram& prog, RealizState* real, cudaStream_t st,
-                               const TmaSet* tma, bool prepare_only);
+                               const TmaSet* tma, bool prepare_only, const FusedRecordT<T>& rec);
 cudaError_t launch_begin_step(InstanceState* inst, int ninst, double cfl, int use_min, cudaStream_t st);
 cudaError_t launch_end_step(InstanceState* inst, int ninst, const RealizState* real, cudaStream_t st);
 cudaError_t launch_set_time(InstanceState* inst, int ninst, double t, double dt, cudaStream_t st);

@@ -275,3 +275,24 @@ def test_fp32_adjoint_close_to_fp64():
     print(f"FP32 adjoint: J rel {rel_J:.2e}; dJ/d(r, w, cx) fp64 {grads['fp64']} fp32 {grads['fp32']} rel {rel}")
     assert rel_J < 1e-5
     assert rel[0] < 1e-3 and rel[1] < 1e-3
+
+
+@pytest.mark.parametrize("flux", ["Roe", "HLLL"])
+def test_fp32_adjoint_fused_recompute_equals_split(flux):
+    """The FP32 form's reverse pass recomputes each checkpoint segment with the fused
+    stage kernel, which records the stage inputs and face states the reverse kernels
+    read; with the three split kernels (stage form 0) instead, J and dJ/dU0 are the
+    same bits."""
+    from pyhype_gb300.adjoint import AdjointSolver, adjoint_problem, smoothed_explosion
+
+    P = adjoint_problem(n=64, flux=flux)
+    out = []
+    for form in (2, 0):
+        A = AdjointSolver(P, "RK4", side="N", nsteps=12, ckpt_every=5, precision="fp32")
+        A.device.set_kernel_choice(3, form)
+        U0 = smoothed_explosion(P, 4.0, 2.0, 5.3).detach().clone()
+        J = A.forward(U0)
+        g = A.backward().cpu().numpy()
+        out.append((J, g))
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
