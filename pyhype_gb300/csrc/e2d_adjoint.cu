@@ -173,9 +173,9 @@ int forward_step(E2DSolver* h, T* stage_out, T* face_out) {
   for (int s = 0; s < h->nstages; ++s) {
     const T* in = p.S.buf[h->stage_input[s]];
     FaceArraysT<T> F = p.F;
-    if (h->use_fused(s)) {
-      // one launch; kept for the reverse pass it records the stage's input and face
-      // states, the same values the split kernels leave
+    if (sizeof(T) == 4 && h->use_fused(s)) {
+      // FP32: one launch; kept for the reverse pass it records the stage's input and
+      // face states, the same values the split kernels leave (FP64 recomputes split)
       FusedRecordT<T> rec{};
       if (stage_out) {
         F = face_slot<T>(h, face_out + (size_t)s * face_set_size(h));

@@ -206,7 +206,7 @@ __device__ void prefetch_tile(const ParamsT<T>& P, const TileOrigin& to, int i0,
   }
 }
 
-template <typename T, int LIM, int RECON, int FLUX, int FTY, int NW, int MINB>
+template <typename T, int LIM, int RECON, int FLUX, int FTY, int NW, int MINB, bool REC>
 __global__ void __launch_bounds__(NW * 32, MINB)
     k_stage_fused(ParamsT<T> P, const int4* __restrict__ tiles, const T* __restrict__ U,
                   InstanceState* __restrict__ inst, StateBuffersT<T> S, StageProgram prog,
@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
         L[v] = sm.L[fam][v][r][c];
         R[v] = sm.R[fam][v][r][c];
       }
-      if (rec.vL) {  // the face states for the adjoint, where the split reconstruction puts them
+      if (REC && rec.vL) {  // the face states for the adjoint, where the split reconstruction puts them
         T* rl = vert ? rec.vL : rec.hL;
         T* rr = vert ? rec.vR : rec.hR;
         const int64_t nf = vert ? P.nvface : P.nhface;
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
     bool bad = false;
     if (r < FTY && i < ny && j < nx) {
       const int64_t c = to.cell(r, lane);
-      if (rec.y) {  // the stage's input state for the adjoint
+      if (REC && rec.y) {  // the stage's input state for the adjoint
 #pragma unroll
         for (int v = 0; v < 4; ++v) rec.y[v * P.ncell + c] = U[v * P.ncell + c];
       }
@@ -409,13 +409,21 @@ static cudaError_t fused_launch(const ParamsT<T>& P, const TileSet& ts, const T*
   constexpr int FTY = FUSED_TY[FORM], NW = FUSED_WARPS[FORM];
   // CTAs an SM holds at 64 registers a thread (FP32) or 128 (FP64): 65536 / (regs x NW x 32)
   constexpr int MINB = (sizeof(T) == 4 ? 32 : 16) / NW;
-  auto kern = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB>;
+  // the recording variant (FP32 only: the adjoint recomputes FP64 segments split)
+  auto kern = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, false>;
+  auto kern_rec = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, sizeof(T) == 4>;
   constexpr int bytes = (int)sizeof(FusedSmem<T, FTY>);
-  if (prepare_only) return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (prepare_only) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern_rec, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return e;
+  }
   const TmaTiles tma = tset ? tset->fused[FORM] : TmaTiles{nullptr, nullptr, nullptr};
   if (ts.nfused[FORM] <= 0) return cudaSuccess;
-  kern<<<ts.nfused[FORM], NW * 32, bytes, st>>>(P, ts.fused[FORM], U, inst, S, resolve_program(prog, S), real, tma,
-                                                rec);
+  const bool record = rec.y != nullptr || rec.vL != nullptr;
+  if (record && sizeof(T) != 4) return cudaErrorInvalidValue;
+  (record ? kern_rec : kern)<<<ts.nfused[FORM], NW * 32, bytes, st>>>(P, ts.fused[FORM], U, inst, S,
+                                                                      resolve_program(prog, S), real, tma, rec);
   return cudaGetLastError();
 }
 
