@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(TX * TY) k_flux_vjp(ParamsT<T> P, const int4* 
   const int i = tl.y + ty, j = tl.z + tx;
   if (i > ny || j > nx) return;
   const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
-  const bool cart = B->is_cartesian != 0;
+  const bool cart = block_cart(P, B, tl.x);
   const T* ia = P.geo.cell[E2D_G_INV_A];
   // dUdt = 0.5*(I_W - I_E + I_S - I_N)/A: a face is the W (S) face of the cell above
   // it in index order and the E (N) face of the cell below.
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(TX * VTY, 4) k_reconstruct_vjp(ParamsT<T> P, c
     hx[s] = P.geo.cell[E2D_G_HX_E + s][c];
     hy[s] = P.geo.cell[E2D_G_HY_E + s][c];
   }
-  const bool cart = B->is_cartesian != 0;
+  const bool cart = block_cart(P, B, tl.x);
   const T cE = P.geo.vface[E2D_F_COS][fE], sE = P.geo.vface[E2D_F_SIN][fE];
   const T cW = P.geo.vface[E2D_F_COS][fW], sW_ = P.geo.vface[E2D_F_SIN][fW];
   const T cN = P.geo.hface[E2D_F_COS][fN], sN = P.geo.hface[E2D_F_SIN][fN];

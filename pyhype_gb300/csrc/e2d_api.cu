@@ -240,6 +240,25 @@ static int upload_geometry(E2DSolver* h, const E2DGeometry* geo) {
     if (int e = put(q, geo->hface[k], nh)) return e;
     p.P.geo.hface[k] = q;
   }
+  // FP32 form: blocks whose face frames are axis-aligned to FP32's resolution
+  p.P.axis32 = nullptr;
+  h->axis32.assign(h->hblocks.size(), 0);
+  if (sizeof(T) == 4) {
+    const float eps = 0x1p-24f;
+    for (size_t b = 0; b < h->hblocks.size(); ++b) {
+      const E2DBlock& B = h->hblocks[b];
+      bool ok = true;
+      for (int64_t f = B.vface_offset; ok && f < B.vface_offset + (int64_t)B.ny * (B.nx + 1); ++f)
+        ok = (float)geo->vface[E2D_F_COS][f] == 1.0f && std::fabs((float)geo->vface[E2D_F_SIN][f]) < eps;
+      for (int64_t f = B.hface_offset; ok && f < B.hface_offset + (int64_t)(B.ny + 1) * B.nx; ++f)
+        ok = (float)geo->hface[E2D_F_SIN][f] == 1.0f && std::fabs((float)geo->hface[E2D_F_COS][f]) < eps;
+      h->axis32[b] = ok ? 1 : 0;
+    }
+    int* d = nullptr;
+    if (int e = h->alloc(&d, h->axis32.size())) return e;
+    CK(cudaMemcpy(d, h->axis32.data(), sizeof(int) * h->axis32.size(), cudaMemcpyHostToDevice));
+    p.P.axis32 = d;
+  }
   for (int qi = 0; qi < E2D_MAX_QP; ++qi)
     for (int k = 0; k < 8; ++k) p.P.geo.qp[qi][k] = nullptr;
   if (nqp > 1)
@@ -639,6 +658,9 @@ int e2d_create(const E2DConfig* cfg, const E2DBlock* blocks, const E2DGeometry* 
       h->ts.cell[v] = d;
       h->ts.ncell[v] = (int)ct.size();
     }
+    h->ts.all_cartesian = true;  // as block_cart decides on the device
+    for (int b = 0; b < cfg->nblocks; ++b)
+      h->ts.all_cartesian = h->ts.all_cartesian && (h->hblocks[b].is_cartesian || h->axis32[b]);
     for (int v = 0; v < 2; ++v) {  // the fused stage kernel's tiles
       std::vector<int4> ct;
       for (int b = 0; b < cfg->nblocks; ++b) {

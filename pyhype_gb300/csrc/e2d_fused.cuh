@@ -82,7 +82,7 @@ struct TileOrigin {
 // Gradient, limiter and the face states `which` of the cell at tile-local (lr, lc),
 // lr in [-1, FTY], lc in [-1, TX]; a tile cell (own = true) also writes the outside
 // states of its block-boundary faces.
-template <typename T, int LIM, int RECON, int FTY>
+template <typename T, int LIM, int RECON, int FTY, bool CART>
 __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G, const E2DBlock* B,
                                            const TileOrigin& to, FusedSmem<T, FTY>& sm, int i0, int j0, int lr,
                                            int lc, int which, bool own, double t) {
@@ -102,7 +102,7 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
     T gx[4], gy[4], ph[4];
     limit_cell4<T, LIM>(st, g, face, gx, gy, ph);
   }
-  const bool cart = to.cart;
+  const bool cart = CART || to.cart;
   // the frames of the faces to write, read before the first store
   T fc[4] = {T(1), T(1), T(0), T(0)}, fs[4] = {T(0), T(0), T(1), T(1)};
   if (!cart) {
@@ -206,7 +206,7 @@ __device__ void prefetch_tile(const ParamsT<T>& P, const TileOrigin& to, int i0,
   }
 }
 
-template <typename T, int LIM, int RECON, int FLUX, int FTY, int NW, int MINB, bool REC>
+template <typename T, int LIM, int RECON, int FLUX, int FTY, int NW, int MINB, bool REC, bool CART>
 __global__ void __launch_bounds__(NW * 32, MINB)
     k_stage_fused(ParamsT<T> P, const int4* __restrict__ tiles, const T* __restrict__ U,
                   InstanceState* __restrict__ inst, StateBuffersT<T> S, StageProgram prog,
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
   const double t = I->t;
   const int nx = B->nx, ny = B->ny;
   const int i0 = tl.y, j0 = tl.z;
-  const TileOrigin to{cell_at(B, i0, j0), vf_at(B, i0, j0), hf_at(B, i0, j0), nx, ny, B->is_cartesian != 0};
+  const TileOrigin to{cell_at(B, i0, j0), vf_at(B, i0, j0), hf_at(B, i0, j0), nx, ny, block_cart(P, B, tl.x)};
   prefetch_tile<T, FTY>(P, to, i0, j0, S, prog);
   // the halo lies inside the block: no ghost cell is staged and every ring cell is real
   const bool interior = i0 >= 2 && j0 >= 2 && i0 + FTY + 2 <= ny && j0 + TX + 2 <= nx;
@@ -309,13 +309,13 @@ __global__ void __launch_bounds__(NW * 32, MINB)
       which = east ? FACE_W : FACE_E;
       live = q < 2 * FTY && i0 + lr < ny && (east ? j0 + TX < nx : j0 >= 1);
     }
-    if (live) fused_cell<T, LIM, RECON, FTY>(P, G, B, to, sm, i0, j0, lr, lc, which, task < FTY, t);
+    if (live) fused_cell<T, LIM, RECON, FTY, CART>(P, G, B, to, sm, i0, j0, lr, lc, which, task < FTY, t);
   }
   __syncthreads();
 
   // ---- one flux per face of the tile (one call site for both face families) ---------
   {
-    const bool cart = to.cart;
+    const bool cart = CART || to.cart;
     // a warp per row of faces: the horizontal face rows 0..FTY, the vertical face rows
     // 0..FTY-1 (columns 0..31), then the tile's east edge (column TX, 32 rows a job)
     constexpr int NJ = (FTY + 1) + FTY + (FTY + 31) / 32;
@@ -409,12 +409,16 @@ static cudaError_t fused_launch(const ParamsT<T>& P, const TileSet& ts, const T*
   constexpr int FTY = FUSED_TY[FORM], NW = FUSED_WARPS[FORM];
   // CTAs an SM holds at 64 registers a thread (FP32) or 128 (FP64): 65536 / (regs x NW x 32)
   constexpr int MINB = (sizeof(T) == 4 ? 32 : 16) / NW;
-  // the recording variant (FP32 only: the adjoint recomputes FP64 segments split)
-  auto kern = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, false>;
-  auto kern_rec = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, sizeof(T) == 4>;
+  // variants: any blocks; all blocks Cartesian (rotations and face frames compiled
+  // out); recording for the adjoint (FP32 only: the adjoint recomputes FP64 segments
+  // split)
+  auto kern = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, false, false>;
+  auto kern_cart = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, false, true>;
+  auto kern_rec = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, sizeof(T) == 4, false>;
   constexpr int bytes = (int)sizeof(FusedSmem<T, FTY>);
   if (prepare_only) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern_cart, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(kern_rec, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return e;
   }
@@ -422,8 +426,8 @@ static cudaError_t fused_launch(const ParamsT<T>& P, const TileSet& ts, const T*
   if (ts.nfused[FORM] <= 0) return cudaSuccess;
   const bool record = rec.y != nullptr || rec.vL != nullptr;
   if (record && sizeof(T) != 4) return cudaErrorInvalidValue;
-  (record ? kern_rec : kern)<<<ts.nfused[FORM], NW * 32, bytes, st>>>(P, ts.fused[FORM], U, inst, S,
-                                                                      resolve_program(prog, S), real, tma, rec);
+  auto k = record ? kern_rec : (ts.all_cartesian ? kern_cart : kern);
+  k<<<ts.nfused[FORM], NW * 32, bytes, st>>>(P, ts.fused[FORM], U, inst, S, resolve_program(prog, S), real, tma, rec);
   return cudaGetLastError();
 }
 

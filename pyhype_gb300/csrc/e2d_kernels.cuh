@@ -71,7 +71,20 @@ struct ParamsT {
   int flux, limiter, recon;
   int nqp;                  // face quadrature points (1, 2, 3)
   T qw[E2D_MAX_QP];         // their weights (2; 1, 1; 5/9, 8/9, 5/9)
+  const int* axis32;        // FP32 form: per block, 1 where every face frame is axis-aligned
+                            // to FP32's resolution (null on the FP64 path)
 };
+
+// A block whose faces the kernels treat as axis-aligned (no rotations, no frame loads):
+// the reference's test on its corner vertices (quad_block.py:96-113), or in the FP32
+// form a block whose every vertical face has cos 1 and |sin| < 2^-24 and every
+// horizontal face sin 1 and |cos| < 2^-24 in FP32.  A rotation by such a frame changes
+// an FP32 velocity component only where it is below 2^-24 of the other component, a
+// difference the FP32 state cannot hold.
+template <typename T>
+__device__ __forceinline__ bool block_cart(const ParamsT<T>& P, const E2DBlock* B, int b) {
+  return B->is_cartesian != 0 || (sizeof(T) == 4 && P.axis32 != nullptr && P.axis32[b] != 0);
+}
 
 // One update of the RK stage program: dst = src + (dt * a) * k (buffers by id).
 // src_zero: the partial sum starts here (src value 0, used for increments).
@@ -138,6 +151,7 @@ struct TileSet {
   int nfused[2];
   const int4* face;
   int nface;
+  bool all_cartesian;  // every block's faces are axis-aligned (the fused kernel's Cartesian variant)
 };
 // Tensor-memory-access (TMA) tile loads of one state buffer for the reconstruction
 // kernel's interior tiles (tiles whose one-cell halo lies inside their block), at one

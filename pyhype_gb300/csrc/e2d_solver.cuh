@@ -66,6 +66,7 @@ struct E2DSolver {
   e2d::KernelChoice ks{0, false};     // stage form: 0 three kernels, 1 and 2 the fused stage kernel
   // per stage: its Butcher updates leave its input buffer alone, so it may be fused
   std::vector<int> fusable;
+  std::vector<int> axis32;       // per block (FP32 form): face frames axis-aligned to FP32's resolution
   bool use_fused(int s) const { return ks.variant >= 1 && cfg.nqp <= 1 && fusable[s]; }
   int nbuf = 0;
   e2d::InstanceState* inst = nullptr;

@@ -532,7 +532,7 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
     }
   }
 
-  const bool cart = B->is_cartesian != 0;
+  const bool cart = block_cart(P, B, tl.x);
   // the four face frames, read before the first store of a face state (a load after a
   // store through these plain pointers would wait for it)
   T fc[4] = {T(1), T(1), T(0), T(0)}, fs[4] = {T(0), T(0), T(1), T(1)};
@@ -727,7 +727,7 @@ __global__ void __launch_bounds__(TX * TY) k_reconstruct_qp(ParamsT<T> P, const 
     gys[v] = gy;
   }
 
-  const bool cart = B->is_cartesian != 0;
+  const bool cart = block_cart(P, B, tl.x);
 #pragma unroll
   for (int s = 0; s < 4; ++s)
 #pragma unroll
@@ -793,7 +793,7 @@ __global__ void __launch_bounds__(TX * TY) k_flux_qp(ParamsT<T> P, const int4* _
   const int i = tl.y + ty, j = tl.z + tx;
   if (i > ny || j > nx) return;
   const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
-  const bool cart = B->is_cartesian != 0;
+  const bool cart = block_cart(P, B, tl.x);
 #pragma unroll
   for (int dir = 0; dir < 2; ++dir) {
     const bool vert = dir == 0;
@@ -840,7 +840,7 @@ __device__ __forceinline__ void flux_tile(const ParamsT<T>& P, const int4 tl, co
   const int i = tl.y + ty, j = tl.z + tx;
   if (i > ny || j > nx) return;
   const Gas<T> G{P.gas[0], P.gas[1], P.gas[2], P.gas[3]};
-  const bool cart = B->is_cartesian != 0;
+  const bool cart = block_cart(P, B, tl.x);
   const bool hv = i < ny, hh = j < nx;
   const int64_t fv = hv ? vf_at(B, i, j) : 0, fh = hh ? hf_at(B, i, j) : 0;
   T vLs[4], vRs[4], hLs[4], hRs[4];
