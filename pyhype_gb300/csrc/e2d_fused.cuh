@@ -206,7 +206,10 @@ __device__ void prefetch_tile(const ParamsT<T>& P, const TileOrigin& to, int i0,
   }
 }
 
-template <typename T, int LIM, int RECON, int FLUX, int FTY, int NW, int MINB, bool REC, bool CART>
+// REC: record for the adjoint; CART: every block Cartesian (block_cart); FINAL: the
+// stage is the step's last (1), is not (0), or reads it from the program (2); NU: the
+// stage has at most NU updates
+template <typename T, int LIM, int RECON, int FLUX, int FTY, int NW, int MINB, bool REC, bool CART, int FINAL, int NU>
 __global__ void __launch_bounds__(NW * 32, MINB)
     k_stage_fused(ParamsT<T> P, const int4* __restrict__ tiles, const T* __restrict__ U,
                   InstanceState* __restrict__ inst, StateBuffersT<T> S, StageProgram prog,
@@ -368,6 +371,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
   __syncthreads();
 
   // ---- dUdt and the stage program of every tile cell --------------------------------
+  const bool final_stage = FINAL == 2 ? prog.final_stage != 0 : FINAL == 1;
   int nbad = 0;
 #pragma unroll
   for (int round = 0; round < (FTY + NW - 1) / NW; ++round) {  // every thread runs every round
@@ -386,16 +390,16 @@ __global__ void __launch_bounds__(NW * 32, MINB)
 #pragma unroll
       for (int v = 0; v < 4; ++v) k[v] = cell_dudt(sm.L[0][v][r][lane], sm.L[0][v][r][lane + 1], sm.L[1][v][r][lane],
                                                    sm.L[1][v][r + 1][lane], A, iA);
-      stage_program(P, S, prog, I->dt, c, k);
-      if (prog.final_stage) {
+      stage_program<T, NU>(P, S, prog, I->dt, c, k);
+      if (final_stage) {
         const T rho = S.buf[0][c], E = S.buf[0][3 * P.ncell + c];
         bad = !(rho > T(0)) || !(E > T(0));
         if (bad) atomicMin(&real->first, ((unsigned long long)tl.x << 40) | (unsigned long long)(c - B->cell_offset));
       }
     }
-    if (prog.final_stage) nbad += __syncthreads_count(bad);
+    if (final_stage) nbad += __syncthreads_count(bad);
   }
-  if (prog.final_stage && threadIdx.x == 0 && nbad) {
+  if (final_stage && threadIdx.x == 0 && nbad) {
     atomicAdd(&real->nbad, (unsigned long long)nbad);
     atomicAdd(&inst[B->instance].nbad, nbad);  // halts this instance only
   }
@@ -409,24 +413,29 @@ static cudaError_t fused_launch(const ParamsT<T>& P, const TileSet& ts, const T*
   constexpr int FTY = FUSED_TY[FORM], NW = FUSED_WARPS[FORM];
   // CTAs an SM holds at 64 registers a thread (FP32) or 128 (FP64): 65536 / (regs x NW x 32)
   constexpr int MINB = (sizeof(T) == 4 ? 32 : 16) / NW;
-  // variants: any blocks; all blocks Cartesian (rotations and face frames compiled
-  // out); recording for the adjoint (FP32 only: the adjoint recomputes FP64 segments
-  // split)
-  auto kern = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, false, false>;
-  auto kern_cart = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, false, true>;
-  auto kern_rec = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, sizeof(T) == 4, false>;
+  // variants: any blocks (everything read at run time); all blocks Cartesian, and for
+  // FP32 also the stage's place and update count compiled in; recording for the adjoint
+  // (FP32 only: the adjoint recomputes FP64 segments split)
+  constexpr bool F32 = sizeof(T) == 4;
+  auto kern = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, false, false, 2, MAX_STAGES>;
+  auto kern_cart = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, false, true, 2, MAX_STAGES>;
+  auto kern_c0 = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, false, true, F32 ? 0 : 2, F32 ? 2 : MAX_STAGES>;
+  auto kern_c1 = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, false, true, F32 ? 1 : 2, F32 ? 2 : MAX_STAGES>;
+  auto kern_rec = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, F32, false, 2, MAX_STAGES>;
   constexpr int bytes = (int)sizeof(FusedSmem<T, FTY>);
   if (prepare_only) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern_cart, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern_rec, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e = cudaSuccess;
+    for (auto k : {kern, kern_cart, kern_c0, kern_c1, kern_rec})
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return e;
   }
   const TmaTiles tma = tset ? tset->fused[FORM] : TmaTiles{nullptr, nullptr, nullptr};
   if (ts.nfused[FORM] <= 0) return cudaSuccess;
   const bool record = rec.y != nullptr || rec.vL != nullptr;
-  if (record && sizeof(T) != 4) return cudaErrorInvalidValue;
-  auto k = record ? kern_rec : (ts.all_cartesian ? kern_cart : kern);
+  if (record && !F32) return cudaErrorInvalidValue;
+  auto k = record ? kern_rec
+                  : !ts.all_cartesian ? kern
+                  : (F32 && prog.nupd <= 2) ? (prog.final_stage ? kern_c1 : kern_c0) : kern_cart;
   k<<<ts.nfused[FORM], NW * 32, bytes, st>>>(P, ts.fused[FORM], U, inst, S, resolve_program(prog, S), real, tma, rec);
   return cudaGetLastError();
 }

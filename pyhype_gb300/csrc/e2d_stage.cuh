@@ -388,11 +388,13 @@ __device__ __forceinline__ T cell_dudt(T IW, T IE, T IS, T IN, T A, T iA) {
 // previous update's stores (the buffers are plain pointers); loading every source
 // first was measured slower in both the split and the fused kernel: the values held
 // across the stores cost registers, and so occupancy or spills.
-template <typename T>
+// NU bounds the updates a stage has (the loop is unrolled NU times; programs of the
+// explicit tableaux up to RK4 have at most two per stage).
+template <typename T, int NU = MAX_STAGES>
 __device__ __forceinline__ void stage_program(const ParamsT<T>& P, const StateBuffersT<T>& S, const StageProgram& prog,
                                               double dt, int64_t c, const T* k) {
 #pragma unroll
-  for (int u = 0; u < MAX_STAGES; ++u) {  // unrolled: the program is read from kernel parameters
+  for (int u = 0; u < NU; ++u) {  // unrolled: the program is read from kernel parameters
     if (u >= prog.nupd) break;
     const StageUpdate& up = prog.upd[u];
     const T* src = static_cast<const T*>(up.srcp);
