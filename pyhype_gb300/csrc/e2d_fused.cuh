@@ -155,7 +155,7 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
 // program's sources for the tile's cells.  The geometry planes are larger than L2 and
 // come from HBM every stage; prefetched, the reconstruction's loads wait for L2
 // instead of HBM.  Rows and columns are clamped to the block.
-template <typename T, int FTY>
+template <typename T, int FTY, int NU>
 __device__ void prefetch_tile(const ParamsT<T>& P, const TileOrigin& to, int i0, int j0,
                               const StateBuffersT<T>& S, const StageProgram& prog) {
   // items by constant-sized groups (divisions by constants): cell planes x FTY + 2
@@ -168,7 +168,7 @@ __device__ void prefetch_tile(const ParamsT<T>& P, const TileOrigin& to, int i0,
   const int tr = min(FTY, to.ny - i0), tc = min(TX, to.nx - j0);  // the tile's own cells
   int nsrc = 0;  // source plane sets: each update's source, and U^n and its compensation for a Kahan update
 #pragma unroll
-  for (int u = 0; u < MAX_STAGES; ++u) {
+  for (int u = 0; u < NU; ++u) {
     if (u >= prog.nupd) break;
     nsrc += (prog.upd[u].src_zero ? 0 : 1) + (prog.upd[u].kahan ? 2 : 0);
   }
@@ -188,7 +188,7 @@ __device__ void prefetch_tile(const ParamsT<T>& P, const TileOrigin& to, int i0,
       int n = q / (4 * FTY);  // the n-th source plane set
       const T* base = nullptr;
 #pragma unroll
-      for (int u = 0; u < MAX_STAGES; ++u) {
+      for (int u = 0; u < NU; ++u) {
         if (u >= prog.nupd || base != nullptr) break;
         const StageUpdate& up = prog.upd[u];
         if (!up.src_zero) {
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
   const int nx = B->nx, ny = B->ny;
   const int i0 = tl.y, j0 = tl.z;
   const TileOrigin to{cell_at(B, i0, j0), vf_at(B, i0, j0), hf_at(B, i0, j0), nx, ny, block_cart(P, B, tl.x)};
-  prefetch_tile<T, FTY>(P, to, i0, j0, S, prog);
+  prefetch_tile<T, FTY, NU>(P, to, i0, j0, S, prog);
   // the halo lies inside the block: no ghost cell is staged and every ring cell is real
   const bool interior = i0 >= 2 && j0 >= 2 && i0 + FTY + 2 <= ny && j0 + TX + 2 <= nx;
 
