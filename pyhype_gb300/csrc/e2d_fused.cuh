@@ -155,16 +155,18 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
 // program's sources for the tile's cells.  The geometry planes are larger than L2 and
 // come from HBM every stage; prefetched, the reconstruction's loads wait for L2
 // instead of HBM.  Rows and columns are clamped to the block.
-template <typename T, int FTY, int NU>
+template <typename T, int FTY, int NU, bool CART>
 __device__ void prefetch_tile(const ParamsT<T>& P, const TileOrigin& to, int i0, int j0,
                               const StateBuffersT<T>& S, const StageProgram& prog) {
   // items by constant-sized groups (divisions by constants): cell planes x FTY + 2
   // rows, face planes x FTY + 2 (vertical) or FTY + 3 (horizontal) rows, source
-  // planes x FTY rows; rows outside the block are skipped
-  constexpr int RR = FTY + 2, NCI = 10 * RR, NVI = 5 * RR, NHI = 5 * (RR + 1);
+  // planes x FTY rows; rows outside the block are skipped.  A Cartesian variant reads
+  // no face frames, so it prefetches 3 face planes, not 5.
+  constexpr int NF = CART ? 3 : 5;
+  constexpr int RR = FTY + 2, NCI = 10 * RR, NVI = NF * RR, NHI = NF * (RR + 1);
   const int r_lo = (i0 >= 1 ? -1 : 0), r_hi = min(FTY, to.ny - 1 - i0);  // tile rows and the ring, local
   const int c_lo = (j0 >= 1 ? -1 : 0), c_hi = min(TX, to.nx - 1 - j0);
-  const int nfp = to.cart ? 3 : 5;  // face planes: L, L cos, L sin (, cos, sin)
+  const int nfp = (CART || to.cart) ? 3 : 5;  // face planes: L, L cos, L sin (, cos, sin)
   const int tr = min(FTY, to.ny - i0), tc = min(TX, to.nx - j0);  // the tile's own cells
   int nsrc = 0;  // source plane sets: each update's source, and U^n and its compensation for a Kahan update
 #pragma unroll
@@ -230,7 +232,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
   const int nx = B->nx, ny = B->ny;
   const int i0 = tl.y, j0 = tl.z;
   const TileOrigin to{cell_at(B, i0, j0), vf_at(B, i0, j0), hf_at(B, i0, j0), nx, ny, block_cart(P, B, tl.x)};
-  prefetch_tile<T, FTY, NU>(P, to, i0, j0, S, prog);
+  prefetch_tile<T, FTY, NU, CART>(P, to, i0, j0, S, prog);
   // the halo lies inside the block: no ghost cell is staged and every ring cell is real
   const bool interior = i0 >= 2 && j0 >= 2 && i0 + FTY + 2 <= ny && j0 + TX + 2 <= nx;
 
