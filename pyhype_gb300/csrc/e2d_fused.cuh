@@ -424,10 +424,11 @@ static cudaError_t fused_launch(const ParamsT<T>& P, const TileSet& ts, const T*
   auto kern_c0 = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, false, true, F32 ? 0 : 2, F32 ? 2 : MAX_STAGES>;
   auto kern_c1 = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, false, true, F32 ? 1 : 2, F32 ? 2 : MAX_STAGES>;
   auto kern_rec = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, F32, false, 2, MAX_STAGES>;
+  auto kern_rec_cart = k_stage_fused<T, LIM, RECON, FLUX, FTY, NW, MINB, F32, true, 2, MAX_STAGES>;
   constexpr int bytes = (int)sizeof(FusedSmem<T, FTY>);
   if (prepare_only) {
     cudaError_t e = cudaSuccess;
-    for (auto k : {kern, kern_cart, kern_c0, kern_c1, kern_rec})
+    for (auto k : {kern, kern_cart, kern_c0, kern_c1, kern_rec, kern_rec_cart})
       if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return e;
   }
@@ -435,7 +436,7 @@ static cudaError_t fused_launch(const ParamsT<T>& P, const TileSet& ts, const T*
   if (ts.nfused[FORM] <= 0) return cudaSuccess;
   const bool record = rec.y != nullptr || rec.vL != nullptr;
   if (record && !F32) return cudaErrorInvalidValue;
-  auto k = record ? kern_rec
+  auto k = record ? (ts.all_cartesian ? kern_rec_cart : kern_rec)
                   : !ts.all_cartesian ? kern
                   : (F32 && prog.nupd <= 2) ? (prog.final_stage ? kern_c1 : kern_c0) : kern_cart;
   k<<<ts.nfused[FORM], NW * 32, bytes, st>>>(P, ts.fused[FORM], U, inst, S, resolve_program(prog, S), real, tma, rec);
