@@ -91,8 +91,11 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
   const int sr = lr + 2, sc = XO + lc;  // the cell's position in sW
   const int64_t fW = to.vface(lr, lc), fE = fW + 1;
   const int64_t fS = to.hface(lr, lc), fN = fS + to.nx;
+  // the FP32 form on a block it takes as Cartesian: the gradient without the normals'
+  // cross-axis terms (limit_cell4); compiled in for the Cartesian variant, chosen per
+  // block in the general one
+  constexpr bool F32 = sizeof(T) == 4;
   CellGeo<T> g;
-  load_cell_geo_at(P, to.cell(lr, lc), fW, fS, to.nx, g);
   T face[4][4];
   {
     // stencil points: the cell, W, E, S, N
@@ -100,7 +103,8 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
       return sm.sW[v][sr + (p == 3 ? -1 : p == 4 ? 1 : 0)][sc + (p == 1 ? -1 : p == 2 ? 1 : 0)];
     };
     T gx[4], gy[4], ph[4];
-    limit_cell4<T, LIM>(st, g, face, gx, gy, ph);
+    load_cell_geo_at<T, CART && F32>(P, to.cell(lr, lc), fW, fS, to.nx, g);
+    limit_cell4<T, LIM, CART && F32>(st, g, face, gx, gy, ph, F32 && to.cart);
   }
   const bool cart = CART || to.cart;
   // the frames of the faces to write, read before the first store

@@ -162,15 +162,27 @@ struct CellGeo {
   T hx[4], hy[4];
 };
 
-// by the cell's index c, its west face fW and south face fS in a block nx cells wide
-template <typename T>
+// by the cell's index c, its west face fW and south face fS in a block nx cells wide.
+// AXG (the FP32 form on a block it takes as Cartesian): the normals' cross-axis
+// components (L sin of vertical faces, L cos of horizontal ones, below 2^-24 of L)
+// are not read; the gradient leaves their terms out (limit_cell4).  Kernels that
+// choose that gradient per block at run time load every component.
+template <typename T, bool AXG = false>
 __device__ __forceinline__ void load_cell_geo_at(const ParamsT<T>& P, int64_t c, int64_t fW, int64_t fS, int nx,
                                                  CellGeo<T>& g) {
   const int64_t fE = fW + 1, fN = fS + nx;
-  g.LcE = P.geo.vface[E2D_F_LC][fE]; g.LsE = P.geo.vface[E2D_F_LS][fE];
-  g.LcW = P.geo.vface[E2D_F_LC][fW]; g.LsW = P.geo.vface[E2D_F_LS][fW];
-  g.LcN = P.geo.hface[E2D_F_LC][fN]; g.LsN = P.geo.hface[E2D_F_LS][fN];
-  g.LcS = P.geo.hface[E2D_F_LC][fS]; g.LsS = P.geo.hface[E2D_F_LS][fS];
+  g.LcE = P.geo.vface[E2D_F_LC][fE];
+  g.LcW = P.geo.vface[E2D_F_LC][fW];
+  g.LsN = P.geo.hface[E2D_F_LS][fN];
+  g.LsS = P.geo.hface[E2D_F_LS][fS];
+  if constexpr (AXG) {
+    g.LsE = g.LsW = g.LcN = g.LcS = T(0);
+  } else {
+    g.LsE = P.geo.vface[E2D_F_LS][fE];
+    g.LsW = P.geo.vface[E2D_F_LS][fW];
+    g.LcN = P.geo.hface[E2D_F_LC][fN];
+    g.LcS = P.geo.hface[E2D_F_LC][fS];
+  }
   g.ia = P.geo.cell[E2D_G_INV_A][c];
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
@@ -180,7 +192,7 @@ __device__ __forceinline__ void load_cell_geo_at(const ParamsT<T>& P, int64_t c,
 }
 template <typename T>
 __device__ __forceinline__ void load_cell_geo(const ParamsT<T>& P, const E2DBlock* B, int i, int j, CellGeo<T>& g) {
-  load_cell_geo_at(P, cell_at(B, i, j), vf_at(B, i, j), hf_at(B, i, j), B->nx, g);
+  load_cell_geo_at<T>(P, cell_at(B, i, j), vf_at(B, i, j), hf_at(B, i, j), B->nx, g);
 }
 
 // FP32 form: the limiter value of one variable at one cell from its five-point
@@ -266,10 +278,14 @@ __device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, con
 // gx/gy/ph the gradient and limiter value of variable v.  st(v, p) is variable v's
 // stencil value at point p (0 the cell, 1 its west, 2 east, 3 south, 4 north
 // neighbour).  FP32 evaluates the interface averages, gradients, face differences and
-// face states of two variables at a time in paired instructions (same values).
-template <typename T, int LIM, typename Stencil>
+// face states of two variables at a time in paired instructions (same values).  AXG
+// (FP32 only): the gradient of a block the FP32 form takes as Cartesian, without the
+// normals' cross-axis terms, (ie LcE - iw LcW) / A and (in LsN - is LsS) / A; axg
+// chooses that gradient at run time (one limiter body, the two sums selected).
+template <typename T, int LIM, bool AXG = false, typename Stencil>
 __device__ __forceinline__ void limit_cell4(const Stencil& st, const CellGeo<T>& g, T (&face)[4][4], T (&gx)[4],
-                                            T (&gy)[4], T (&ph)[4]) {
+                                            T (&gy)[4], T (&ph)[4], bool axg = false) {
+  static_assert(!AXG || sizeof(T) == 4, "the FP64 path keeps every term");
   if constexpr (sizeof(T) == 8) {
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
@@ -291,8 +307,11 @@ __device__ __forceinline__ void limit_cell4(const Stencil& st, const CellGeo<T>&
       // the scalar form's expressions (limit_cell_var), lane by lane
       const float2 ie = mul2(H, add2(w0, ea)), iw = mul2(H, add2(we, w0));
       const float2 in = mul2(H, add2(w0, no)), is = mul2(H, add2(so, w0));
-      const float2 gxp = mul2(fma2(is, nLcS, fma2(in, LcN, fma2(ie, LcE, mul2(iw, nLcW)))), IA);
-      const float2 gyp = mul2(fma2(is, nLsS, fma2(in, LsN, fma2(ie, LsE, mul2(iw, nLsW)))), IA);
+      const bool ax = AXG || axg;
+      const float2 sx = fma2(ie, LcE, mul2(iw, nLcW));
+      const float2 gxp = mul2(ax ? sx : fma2(is, nLcS, fma2(in, LcN, sx)), IA);
+      const float2 sy = ax ? mul2(in, LsN) : fma2(in, LsN, fma2(ie, LsE, mul2(iw, nLsW)));
+      const float2 gyp = mul2(fma2(is, nLsS, sy), IA);
       float2 hot[4];
       float ha[4], hb[4];
 #pragma unroll
@@ -513,6 +532,9 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
   const int64_t c = cell_at(B, i, j);
   const int64_t fE = vf_at(B, i, j + 1), fW = vf_at(B, i, j);
   const int64_t fN = hf_at(B, i + 1, j), fS = hf_at(B, i, j);
+  // the FP32 form on a block it takes as Cartesian: the gradient without the normals'
+  // cross-axis terms (as the fused kernel computes it)
+  const bool axg = sizeof(T) == 4 && block_cart(P, B, tl.x);
   CellGeo<T> g;
   load_cell_geo(P, B, i, j, g);
 
@@ -523,7 +545,7 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
       return sW[v][ty + 1 + (p == 3 ? -1 : p == 4 ? 1 : 0)][C0 + tx + 1 + (p == 1 ? -1 : p == 2 ? 1 : 0)];
     };
     T gx[4], gy[4], ph[4];
-    limit_cell4<T, LIM>(st, g, face, gx, gy, ph);
+    limit_cell4<T, LIM, false>(st, g, face, gx, gy, ph, axg);
     if (DBG) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
