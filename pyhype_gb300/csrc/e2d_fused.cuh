@@ -91,9 +91,9 @@ __device__ __forceinline__ void fused_cell(const ParamsT<T>& P, const Gas<T>& G,
   const int sr = lr + 2, sc = XO + lc;  // the cell's position in sW
   const int64_t fW = to.vface(lr, lc), fE = fW + 1;
   const int64_t fS = to.hface(lr, lc), fN = fS + to.nx;
-  // the FP32 form on a block it takes as Cartesian: the gradient without the normals'
-  // cross-axis terms (limit_cell4); compiled in for the Cartesian variant, chosen per
-  // block in the general one
+  // the FP32 form on a block it takes as Cartesian: the gradient and the face
+  // differences without cross-axis terms (limit_cell4); compiled in for the Cartesian
+  // variant, chosen per block in the general one
   constexpr bool F32 = sizeof(T) == 4;
   CellGeo<T> g;
   T face[4][4];
@@ -165,12 +165,16 @@ __device__ void prefetch_tile(const ParamsT<T>& P, const TileOrigin& to, int i0,
   // items by constant-sized groups (divisions by constants): cell planes x FTY + 2
   // rows, face planes x FTY + 2 (vertical) or FTY + 3 (horizontal) rows, source
   // planes x FTY rows; rows outside the block are skipped.  A Cartesian variant reads
-  // no face frames, so it prefetches 3 face planes, not 5.
-  constexpr int NF = CART ? 3 : 5;
-  constexpr int RR = FTY + 2, NCI = 10 * RR, NVI = NF * RR, NHI = NF * (RR + 1);
+  // no face frames, so it prefetches 3 face planes, not 5; in FP32 it reads no
+  // cross-axis components either (load_cell_geo_at): A, 1/A, the east and west
+  // points' x offsets and the north and south points' y offsets, and per face family
+  // L and its normal's own-axis component.
+  constexpr bool AX = CART && sizeof(T) == 4;
+  constexpr int NCP = AX ? 6 : 10, NF = AX ? 2 : CART ? 3 : 5;
+  constexpr int RR = FTY + 2, NCI = NCP * RR, NVI = NF * RR, NHI = NF * (RR + 1);
   const int r_lo = (i0 >= 1 ? -1 : 0), r_hi = min(FTY, to.ny - 1 - i0);  // tile rows and the ring, local
   const int c_lo = (j0 >= 1 ? -1 : 0), c_hi = min(TX, to.nx - 1 - j0);
-  const int nfp = (CART || to.cart) ? 3 : 5;  // face planes: L, L cos, L sin (, cos, sin)
+  const int nfp = AX ? 2 : (CART || to.cart) ? 3 : 5;  // face planes: L, L cos, L sin (, cos, sin)
   const int tr = min(FTY, to.ny - i0), tc = min(TX, to.nx - j0);  // the tile's own cells
   int nsrc = 0;  // source plane sets: each update's source, and U^n and its compensation for a Kahan update
 #pragma unroll
@@ -180,15 +184,17 @@ __device__ void prefetch_tile(const ParamsT<T>& P, const TileOrigin& to, int i0,
   }
   const int total = NCI + NVI + NHI + nsrc * 4 * FTY;
   for (int it = threadIdx.x; it < total; it += blockDim.x) {
-    if (it < NCI) {  // A, 1/A and the offsets (E2D_G_A .. E2D_G_HY_S)
+    if (it < NCI) {  // A, 1/A and the offsets (E2D_G_A .. E2D_G_HY_S; AX: HX_E, HX_W, HY_N, HY_S)
       const int k = it / RR, r = it - k * RR - 1;
-      if (r >= r_lo && r <= r_hi) prefetch_l2(P.geo.cell[k], to.cell(r, c_lo), to.cell(r, c_hi));
-    } else if (it < NCI + NVI) {
+      const int plane = (AX && k >= 4) ? k + 4 : k;
+      if (r >= r_lo && r <= r_hi) prefetch_l2(P.geo.cell[plane], to.cell(r, c_lo), to.cell(r, c_hi));
+    } else if (it < NCI + NVI) {  // L, L cos (, L sin, cos, sin)
       const int q = it - NCI, k = q / RR, r = q - k * RR - 1;
       if (k < nfp && r >= r_lo && r <= r_hi) prefetch_l2(P.geo.vface[k], to.vface(r, c_lo), to.vface(r, c_hi + 1));
-    } else if (it < NCI + NVI + NHI) {
+    } else if (it < NCI + NVI + NHI) {  // L, L cos, L sin (, cos, sin); AX: L, L sin
       const int q = it - NCI - NVI, k = q / (RR + 1), r = q - k * (RR + 1) - 1;
-      if (k < nfp && r >= r_lo && r <= r_hi + 1) prefetch_l2(P.geo.hface[k], to.hface(r, c_lo), to.hface(r, c_hi));
+      const int plane = (AX && k == 1) ? (int)E2D_F_LS : k;
+      if (k < nfp && r >= r_lo && r <= r_hi + 1) prefetch_l2(P.geo.hface[plane], to.hface(r, c_lo), to.hface(r, c_hi));
     } else {
       const int q = it - NCI - NVI - NHI, v = (q / FTY) & 3, r = q - (q / FTY) * FTY;
       int n = q / (4 * FTY);  // the n-th source plane set

@@ -163,10 +163,12 @@ struct CellGeo {
 };
 
 // by the cell's index c, its west face fW and south face fS in a block nx cells wide.
-// AXG (the FP32 form on a block it takes as Cartesian): the normals' cross-axis
-// components (L sin of vertical faces, L cos of horizontal ones, below 2^-24 of L)
-// are not read; the gradient leaves their terms out (limit_cell4).  Kernels that
-// choose that gradient per block at run time load every component.
+// AXG (the FP32 form on a block it takes as Cartesian): the cross-axis components are
+// not read, of the normals (L sin of vertical faces, L cos of horizontal ones, below
+// 2^-24 of L) and of the face points' offsets from the centroid (y of the east and
+// west points, x of the north and south ones: on such a cell below 2^-24 of its
+// width); the gradient and the face differences leave their terms out (limit_cell4).
+// Kernels that choose that form per block at run time load every component.
 template <typename T, bool AXG = false>
 __device__ __forceinline__ void load_cell_geo_at(const ParamsT<T>& P, int64_t c, int64_t fW, int64_t fS, int nx,
                                                  CellGeo<T>& g) {
@@ -184,10 +186,17 @@ __device__ __forceinline__ void load_cell_geo_at(const ParamsT<T>& P, int64_t c,
     g.LcS = P.geo.hface[E2D_F_LC][fS];
   }
   g.ia = P.geo.cell[E2D_G_INV_A][c];
-#pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    g.hx[s] = P.geo.cell[E2D_G_HX_E + s][c];
-    g.hy[s] = P.geo.cell[E2D_G_HY_E + s][c];
+  g.hx[E2D_E] = P.geo.cell[E2D_G_HX_E][c];
+  g.hx[E2D_W] = P.geo.cell[E2D_G_HX_W][c];
+  g.hy[E2D_N] = P.geo.cell[E2D_G_HY_N][c];
+  g.hy[E2D_S] = P.geo.cell[E2D_G_HY_S][c];
+  if constexpr (AXG) {
+    g.hy[E2D_E] = g.hy[E2D_W] = g.hx[E2D_N] = g.hx[E2D_S] = T(0);
+  } else {
+    g.hy[E2D_E] = P.geo.cell[E2D_G_HY_E][c];
+    g.hy[E2D_W] = P.geo.cell[E2D_G_HY_W][c];
+    g.hx[E2D_N] = P.geo.cell[E2D_G_HX_N][c];
+    g.hx[E2D_S] = P.geo.cell[E2D_G_HX_S][c];
   }
 }
 template <typename T>
@@ -279,9 +288,11 @@ __device__ __forceinline__ void limit_cell_var(T w0, T we, T ea, T so, T no, con
 // stencil value at point p (0 the cell, 1 its west, 2 east, 3 south, 4 north
 // neighbour).  FP32 evaluates the interface averages, gradients, face differences and
 // face states of two variables at a time in paired instructions (same values).  AXG
-// (FP32 only): the gradient of a block the FP32 form takes as Cartesian, without the
-// normals' cross-axis terms, (ie LcE - iw LcW) / A and (in LsN - is LsS) / A; axg
-// chooses that gradient at run time (one limiter body, the two sums selected).
+// (FP32 only): on a block the FP32 form takes as Cartesian, the gradient without the
+// normals' cross-axis terms, (ie LcE - iw LcW) / A and (in LsN - is LsS) / A, and the
+// face differences without the offsets' cross-axis terms, gx hx at the east and west
+// points and gy hy at the north and south ones; axg chooses that form at run time
+// (one limiter body, the shorter sums selected).
 template <typename T, int LIM, bool AXG = false, typename Stencil>
 __device__ __forceinline__ void limit_cell4(const Stencil& st, const CellGeo<T>& g, T (&face)[4][4], T (&gx)[4],
                                             T (&gy)[4], T (&ph)[4], bool axg = false) {
@@ -316,7 +327,8 @@ __device__ __forceinline__ void limit_cell4(const Stencil& st, const CellGeo<T>&
       float ha[4], hb[4];
 #pragma unroll
       for (int s = 0; s < 4; ++s) {
-        hot[s] = fma2(gxp, pair(g.hx[s], g.hx[s]), mul2(gyp, pair(g.hy[s], g.hy[s])));
+        const float2 hx = pair(g.hx[s], g.hx[s]), hy = pair(g.hy[s], g.hy[s]);
+        hot[s] = ax ? (s == E2D_E || s == E2D_W ? mul2(gxp, hx) : mul2(gyp, hy)) : fma2(gxp, hx, mul2(gyp, hy));
         ha[s] = hot[s].x;
         hb[s] = hot[s].y;
       }
@@ -532,8 +544,8 @@ __device__ __forceinline__ void reconstruct_tile(const ParamsT<T>& P, const int4
   const int64_t c = cell_at(B, i, j);
   const int64_t fE = vf_at(B, i, j + 1), fW = vf_at(B, i, j);
   const int64_t fN = hf_at(B, i + 1, j), fS = hf_at(B, i, j);
-  // the FP32 form on a block it takes as Cartesian: the gradient without the normals'
-  // cross-axis terms (as the fused kernel computes it)
+  // the FP32 form on a block it takes as Cartesian: the gradient and the face
+  // differences without cross-axis terms (as the fused kernel computes them)
   const bool axg = sizeof(T) == 4 && block_cart(P, B, tl.x);
   CellGeo<T> g;
   load_cell_geo(P, B, i, j, g);
