@@ -46,11 +46,14 @@ FP64_INST_PER_SM_CLOCK = 2
 
 # Geometry planes a stage reads once per cell: A, 1/A, the 8 face-point offsets, and
 # of the two faces the cell owns (its west and south faces) L, L cos, L sin, cos, sin.
-# The face frames (cos, sin) are read only for blocks that take the rotation path; the
+# The face frames (cos, sin) are read only for blocks that take the rotation path.  The
 # FP32 form takes the benchmark's blocks, whose frames are axis-aligned to FP32's
-# resolution, as Cartesian and reads 4 planes fewer.
+# resolution, as Cartesian: it reads no frames (4 planes) and no cross-axis components
+# (6 planes: the y offsets of the east and west face points, the x offsets of the
+# north and south ones, L sin of the west face and L cos of the south face).
 GEOMETRY_PLANES_PER_CELL = 2 + 8 + 2 * 5
 FRAME_PLANES_PER_CELL = 2 * 2
+CROSS_AXIS_PLANES_PER_CELL = 4 + 2
 
 
 def stage_state_values(tableau, kahan: bool) -> list:
@@ -89,24 +92,26 @@ def stage_state_values(tableau, kahan: bool) -> list:
     return out
 
 
-def bytes_per_cell_stage(tableau, elem: int, kahan: bool, frames: bool = True) -> float:
+def bytes_per_cell_stage(tableau, elem: int, kahan: bool, frames: bool = True, cross_axis: bool = True) -> float:
     """Algorithmic HBM bytes per cell-stage of a whole step: the stage program's state
     values, the geometry planes once per cell and stage (without the face frames when
-    the blocks are taken as Cartesian), and the CFL dt's state and two geometry planes
-    once per step, averaged over the stages.  Face states, fluxes and halo re-reads are
+    the blocks are taken as Cartesian, and without the cross-axis components when the
+    FP32 form takes them so), and the CFL dt's state and two geometry planes once per
+    step, averaged over the stages.  Face states, fluxes and halo re-reads are
     implementation traffic, not counted."""
     vals = stage_state_values(tableau, kahan)
     S = len(vals)
-    geo = GEOMETRY_PLANES_PER_CELL - (0 if frames else FRAME_PLANES_PER_CELL)
+    geo = (GEOMETRY_PLANES_PER_CELL - (0 if frames else FRAME_PLANES_PER_CELL)
+           - (0 if cross_axis else CROSS_AXIS_PLANES_PER_CELL))
     per_stage = sum(vals) / S + geo
     return elem * (per_stage + 6.0 / S)
 
 
 # the benchmark's RK4: FP64 128 + 160 + 12 = 300 B (rotation path); FP32 form (Kahan,
-# blocks taken as Cartesian) 76 + 64 + 6 = 146 B
+# blocks taken as Cartesian) 76 + 40 + 6 = 122 B
 _RK4 = [[0.5, 0, 0, 0], [0, 0.5, 0, 0], [0, 0, 1, 0], [1 / 6, 1 / 3, 1 / 3, 1 / 6]]
 BYTES_PER_CELL_STAGE_FP64 = bytes_per_cell_stage(_RK4, 8, False)
-BYTES_PER_CELL_STAGE_FP32 = bytes_per_cell_stage(_RK4, 4, True, frames=False)
+BYTES_PER_CELL_STAGE_FP32 = bytes_per_cell_stage(_RK4, 4, True, frames=False, cross_axis=False)
 
 
 def kernel_flops(kind: str, ncell: int, nvface: int, nhface: int) -> float:
